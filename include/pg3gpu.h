@@ -1,0 +1,205 @@
+/*
+ * pg3gpu.h -- C ABI of the GB300 (sm_103a) path-tracing hot path.
+ *
+ * This library replaces the reference renderer's path-tracing core behind its
+ * renderer interface:
+ *
+ *   reference                                          here
+ *   ---------------------------------------------------------------------------
+ *   AbstractRenderer(const Config&) ctor               pg3gpu_create
+ *     (src/renderer.hxx:236-240)
+ *   PathTracerBase::RunIteration(Algorithm, uint32_t)  pg3gpu_run_iteration
+ *     (src/path_tracer_base.hxx:57-90,
+ *      src/path_tracer.hxx:16-41)
+ *   AbstractRenderer::GetFramebuffer(Framebuffer&)     pg3gpu_read_framebuffer
+ *     (src/renderer.hxx:255-262)
+ *   AbstractRenderer::WasUsed()                        pg3gpu_iterations(ctx) > 0
+ *     (src/renderer.hxx:269)
+ *   GetRendererIntrospectionData()                     pg3gpu_get_stats
+ *     (src/renderer.hxx:263-266, path stats :11-228)
+ *   PG3_FATAL_ERROR on bad input                       nonzero status + pg3gpu_last_error
+ *     (src/debugging.hxx:44-66, src/pg3render.cxx:46-48)
+ *
+ * Conventions: every call returns an int status (PG3GPU_OK == 0); no call
+ * keeps a pointer to caller memory after it returns (scene data are copied to
+ * the device in pg3gpu_create); no torch or CUDA types appear in signatures
+ * (streams are passed as void*). A context belongs to one thread at a time,
+ * like the reference's renderers (src/pg3render.cxx:84-128).
+ */
+#ifndef PG3GPU_H
+#define PG3GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    PG3GPU_OK = 0,
+    PG3GPU_ERR_INVALID_ARGUMENT = 1, /* bad scene / option / pointer */
+    PG3GPU_ERR_UNSUPPORTED = 2,      /* valid for the reference, not implemented here */
+    PG3GPU_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    PG3GPU_ERR_OUT_OF_MEMORY = 4,
+    PG3GPU_ERR_DEVICE_LIMIT = 5      /* a kernel hit a bounded loop / stack limit; see last_error */
+};
+
+/* ---- enumerations (values follow the reference where it has them) ----- */
+/* Algorithm ids of src/config.hxx:23-34 that this library renders. */
+enum { PG3GPU_ALG_PATH_TRACING_NAIVE = 6, PG3GPU_ALG_PATH_TRACING = 7 };
+
+enum { PG3GPU_MAT_LAMBERT = 0, PG3GPU_MAT_GGX_CONDUCTOR = 1, PG3GPU_MAT_GGX_DIELECTRIC = 2 };
+enum { PG3GPU_BG_NONE = 0, PG3GPU_BG_CONSTANT = 1, PG3GPU_BG_ENVMAP = 2 };
+/* Environment-map light samplers (compile-time choice in src/hard_config.hxx:17-18, run-time here). */
+enum { PG3GPU_EM_CDF = 0, PG3GPU_EM_COSINE = 1, PG3GPU_EM_STEERABLE = 2 };
+enum { PG3GPU_TRAVERSAL_AUTO = 0, PG3GPU_TRAVERSAL_LIST = 1, PG3GPU_TRAVERSAL_BVH = 2 };
+enum { PG3GPU_PIPELINE_AUTO = 0, PG3GPU_PIPELINE_MEGAKERNEL = 1, PG3GPU_PIPELINE_WAVEFRONT = 2 };
+
+/* ---- scene description (copied at create time) ------------------------- */
+typedef struct pg3gpu_camera {       /* Camera::Setup arguments, src/camera.hxx:13-59 */
+    float position[3];
+    float forward[3];
+    float up[3];
+    uint32_t width, height;
+    float hfov_deg;
+} pg3gpu_camera;
+
+typedef struct pg3gpu_material {
+    int32_t kind;                    /* PG3GPU_MAT_* */
+    float albedo[3];                 /* Lambert reflectance (src/materials.hxx:262-266) */
+    float alpha;                     /* GGX roughness, clamped to [0.001, 1] (src/materials.hxx:805) */
+    float ior;                       /* inner IOR n */
+    float ior_outer;                 /* outer IOR */
+    float absorb;                    /* conductor absorbance k */
+} pg3gpu_material;
+
+typedef struct pg3gpu_triangle {     /* Triangle(p0, p1, p2, matId), src/scene_graph.hxx:88-101 */
+    float p[9];
+    int32_t material;
+} pg3gpu_triangle;
+
+typedef struct pg3gpu_sphere {       /* Sphere(center, radius, matId), src/scene_graph.hxx:162-173 */
+    float center[3];
+    float radius;
+    int32_t material;
+} pg3gpu_sphere;
+
+typedef struct pg3gpu_area_light {   /* AreaLight over one scene triangle, src/lights.hxx:55-112 */
+    uint32_t triangle;               /* index into triangles; its material becomes the emitter */
+    float radiance[3];
+} pg3gpu_area_light;
+
+typedef struct pg3gpu_scene {
+    pg3gpu_camera camera;
+    const pg3gpu_material *materials;
+    uint32_t num_materials;
+    const pg3gpu_triangle *triangles;
+    uint32_t num_triangles;
+    const pg3gpu_sphere *spheres;
+    uint32_t num_spheres;
+    const pg3gpu_area_light *area_lights;
+    uint32_t num_area_lights;
+    int32_t background;              /* PG3GPU_BG_* ; the background is the last light id */
+    float background_radiance[3];    /* PG3GPU_BG_CONSTANT */
+    const float *env_map;            /* PG3GPU_BG_ENVMAP: host RGB float32, env_height rows of
+                                        env_width pixels, row 0 at theta = 0 (src/em_image.hxx:51-93) */
+    uint32_t env_width, env_height;
+} pg3gpu_scene;
+
+/* ---- options (src/config.hxx:1100-1137, src/hard_config.hxx:7-27) ------- */
+typedef struct pg3gpu_options {
+    int32_t algorithm;               /* PG3GPU_ALG_* (mAlgorithm) */
+    uint32_t min_path_length;        /* mMinPathLength (>= 1) */
+    uint32_t max_path_length;        /* mMaxPathLength; 0 = Russian roulette ends paths */
+    uint32_t rr_min_path_length;     /* extension: >0 applies Russian roulette from this path length
+                                        on even when max_path_length is set; 0 = reference rule */
+    float indirect_clipping;         /* mIndirectIllumClipping; only 0 is implemented */
+    uint32_t splitting_budget;       /* mSplittingBudget; only 1 is implemented */
+    int32_t em_sampler;              /* PG3GPU_EM_* */
+    int32_t traversal;               /* PG3GPU_TRAVERSAL_* */
+    int32_t pipeline;                /* PG3GPU_PIPELINE_* */
+    uint32_t steer_subdiv_level;     /* steerable sampler: icosahedron subdivision level (3 -> 1280 triangles) */
+    uint64_t seed;                   /* mBaseSeed: keys every random stream */
+    uint32_t max_paths_in_flight;    /* 0 = automatic; upper bound on paths per launch chunk */
+    uint32_t reserved[5];
+} pg3gpu_options;
+
+/* Path statistics: counts of the reference's PathTerminationReason
+ * (src/renderer.hxx:11-28) plus traced-ray totals. */
+typedef struct pg3gpu_stats {
+    uint64_t paths;
+    uint64_t extension_rays;         /* closest-hit rays (camera + BSDF continuations) */
+    uint64_t shadow_rays;
+    uint64_t terminated_by_russian_roulette;
+    uint64_t terminated_by_background;
+    uint64_t terminated_by_blocker;
+    uint64_t terminated_by_max_limit;
+    uint64_t terminated_by_safety_limit;
+    double last_iteration_ms;        /* device time of the last pg3gpu_run_iteration */
+} pg3gpu_stats;
+
+typedef struct pg3gpu_ctx pg3gpu_ctx;
+
+/* Fills opts with the reference's unbiased defaults for this path:
+ * algorithm PT, min 1, max 0 (RR), clipping 0, splitting 1, CDF sampler. */
+void pg3gpu_default_options(pg3gpu_options *opts);
+
+/* Uploads the scene, builds the acceleration structure and the light-sampling
+ * tables on `device`, and returns a context with a cleared framebuffer.
+ * Replaces AbstractRenderer's constructor (src/renderer.hxx:236-240). */
+int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, pg3gpu_ctx **out);
+
+int pg3gpu_destroy(pg3gpu_ctx *ctx);
+
+/* All work of the context is issued on this CUDA stream (cudaStream_t as void*;
+ * NULL = the legacy default stream). */
+int pg3gpu_set_stream(pg3gpu_ctx *ctx, void *cuda_stream);
+
+/* Renders `spp` samples per pixel (iterations `iteration` .. iteration+spp-1 of
+ * the reference's RunIteration loop) and adds them to the framebuffer.
+ * Asynchronous with respect to the host; `algorithm` is PG3GPU_ALG_*.
+ * Replaces PathTracerBase::RunIteration (src/path_tracer_base.hxx:57-90). */
+int pg3gpu_run_iteration(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp);
+
+/* Waits for the context's stream and reports any kernel-side limit flag. */
+int pg3gpu_synchronize(pg3gpu_ctx *ctx);
+
+/* Copies the accumulated image to host memory: mean_rgb = sum / iterations
+ * (width*height*3 doubles, row 0 at the top), like GetFramebuffer
+ * (src/renderer.hxx:255-262). var_rgb (may be NULL) receives the per-pixel
+ * sample variance of the radiance estimates. iterations (may be NULL)
+ * receives the number of accumulated samples per pixel. */
+int pg3gpu_read_framebuffer(pg3gpu_ctx *ctx, double *mean_rgb, double *var_rgb, uint64_t *iterations);
+
+/* Clears the framebuffer and the iteration counter. */
+int pg3gpu_clear_framebuffer(pg3gpu_ctx *ctx);
+
+/* Number of samples per pixel accumulated so far (WasUsed() == (n > 0)). */
+uint64_t pg3gpu_iterations(const pg3gpu_ctx *ctx);
+
+/* Renders samples `iteration` .. iteration+spp-1 and writes each sample's
+ * radiance to host memory out_rgb[(s * height * width + pixel) * 3 + c]
+ * without touching the framebuffer (path-by-path comparisons). */
+int pg3gpu_render_samples(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp, float *out_rgb);
+
+int pg3gpu_get_stats(pg3gpu_ctx *ctx, pg3gpu_stats *stats);
+int pg3gpu_reset_stats(pg3gpu_ctx *ctx);
+
+/* Device pointers to the framebuffer accumulators (width*height*3 doubles
+ * each: sum and sum of squares), valid until destroy; for callers that keep
+ * results on the GPU. */
+int pg3gpu_device_framebuffer(pg3gpu_ctx *ctx, const double **sum_rgb, const double **sumsq_rgb);
+
+/* Text of the last error of this context (or of the last failed create when ctx is NULL). */
+const char *pg3gpu_last_error(const pg3gpu_ctx *ctx);
+const char *pg3gpu_status_string(int status);
+
+/* Library version, e.g. "pg3gpu 0.1 sm_103a". */
+const char *pg3gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PG3GPU_H */

@@ -1,0 +1,409 @@
+// C ABI of the hot path (include/pg3gpu.h): context life cycle, scene upload,
+// light-sampling tables, iteration scheduling and framebuffer readback.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pg3gpu.h"
+#include "pg3_host.h"
+#include "pg3_kernels.h"
+#include "pg3_scene_view.h"
+
+using namespace pg3;
+
+struct pg3gpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    pg3gpu_options opts{};
+    SceneView view{};
+    std::vector<void *> allocs;
+    uint32_t W = 0, H = 0;
+    double *dSum = nullptr, *dSumsq = nullptr;
+    float *dOut[3] = {nullptr, nullptr, nullptr};
+    uint64_t outCapacity = 0;            // paths per launch chunk
+    void *dWave = nullptr;               // wavefront queues
+    uint64_t waveCapacity = 0;
+    DevStats *dStats = nullptr;
+    unsigned int *dErr = nullptr;
+    uint64_t iterations = 0;
+    int megaGrid = 0, waveGrid = 0;
+    bool useWavefront = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    std::string lastError;
+};
+
+namespace {
+
+thread_local std::string g_createError;
+
+int fail(pg3gpu_ctx *ctx, int status, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->lastError = buf;
+    else g_createError = buf;
+    return status;
+}
+
+#define PG3_CUDA(ctx, call)                                                                          \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? PG3GPU_ERR_OUT_OF_MEMORY : PG3GPU_ERR_CUDA, \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                           \
+    } while (0)
+
+template <typename T>
+int devAlloc(pg3gpu_ctx *ctx, T **p, size_t count)
+{
+    void *q = nullptr;
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    PG3_CUDA(ctx, cudaMalloc(&q, bytes));
+    ctx->allocs.push_back(q);
+    *p = reinterpret_cast<T *>(q);
+    return PG3GPU_OK;
+}
+
+template <typename T>
+int upload(pg3gpu_ctx *ctx, T **p, const std::vector<T> &v)
+{
+    int st = devAlloc(ctx, p, v.size());
+    if (st) return st;
+    if (!v.empty()) PG3_CUDA(ctx, cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return PG3GPU_OK;
+}
+
+int ensureOutput(pg3gpu_ctx *ctx, uint64_t paths)
+{
+    if (paths <= ctx->outCapacity) return PG3GPU_OK;
+    for (auto &p : ctx->dOut) {
+        if (p) {
+            cudaFree(p);
+            ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), (void *)p), ctx->allocs.end());
+            p = nullptr;
+        }
+    }
+    for (auto &p : ctx->dOut) {
+        int st = devAlloc(ctx, &p, paths);
+        if (st) return st;
+    }
+    ctx->outCapacity = paths;
+    return PG3GPU_OK;
+}
+
+// Paths per launch chunk: whole sample passes, bounded by max_paths_in_flight.
+uint32_t passesPerChunk(const pg3gpu_ctx *ctx, uint32_t spp)
+{
+    const uint64_t npix = (uint64_t)ctx->W * ctx->H;
+    const uint64_t budget = ctx->opts.max_paths_in_flight ? ctx->opts.max_paths_in_flight : (1ull << 24);
+    uint64_t k = std::max<uint64_t>(1, budget / npix);
+    return (uint32_t)std::min<uint64_t>(k, spp);
+}
+
+int renderChunk(pg3gpu_ctx *ctx, bool naive, uint32_t sample0, uint32_t passes)
+{
+    const uint32_t npix = ctx->W * ctx->H;
+    const uint64_t paths = (uint64_t)passes * npix;
+    int st = ensureOutput(ctx, paths);
+    if (st) return st;
+    cudaError_t e;
+    if (ctx->useWavefront)
+        e = launchWavefront(ctx->view, naive, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
+                            ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->stream);
+    else
+        e = launchMegakernel(ctx->view, naive, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
+                             ctx->dStats, ctx->megaGrid, ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "path kernel launch: %s", cudaGetErrorString(e));
+    return PG3GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void pg3gpu_default_options(pg3gpu_options *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->algorithm = PG3GPU_ALG_PATH_TRACING;
+    o->min_path_length = 1;
+    o->max_path_length = 0;
+    o->rr_min_path_length = 0;
+    o->indirect_clipping = 0.f;
+    o->splitting_budget = 1;
+    o->em_sampler = PG3GPU_EM_CDF;
+    o->traversal = PG3GPU_TRAVERSAL_AUTO;
+    o->pipeline = PG3GPU_PIPELINE_AUTO;
+    o->steer_subdiv_level = 3;
+    o->seed = 1234;
+}
+
+const char *pg3gpu_status_string(int s)
+{
+    switch (s) {
+    case PG3GPU_OK: return "ok";
+    case PG3GPU_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case PG3GPU_ERR_UNSUPPORTED: return "unsupported";
+    case PG3GPU_ERR_CUDA: return "CUDA error";
+    case PG3GPU_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case PG3GPU_ERR_DEVICE_LIMIT: return "device limit reached";
+    default: return "unknown status";
+    }
+}
+
+const char *pg3gpu_version(void) { return "pg3gpu 0.1 sm_103a"; }
+
+const char *pg3gpu_last_error(const pg3gpu_ctx *ctx) { return ctx ? ctx->lastError.c_str() : g_createError.c_str(); }
+
+int pg3gpu_destroy(pg3gpu_ctx *ctx)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void *p : ctx->allocs) cudaFree(p);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    delete ctx;
+    return PG3GPU_OK;
+}
+
+int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, pg3gpu_ctx **out)
+{
+    if (!out) return fail(nullptr, PG3GPU_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (!scene || !opts) return fail(nullptr, PG3GPU_ERR_INVALID_ARGUMENT, "scene or options is NULL");
+
+    HostScene hs;
+    std::string err;
+    int st = prepareScene(*scene, *opts, hs, err);
+    if (st != PG3GPU_OK) return fail(nullptr, st, "%s", err.c_str());
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, PG3GPU_ERR_CUDA, "no CUDA device visible");
+    if (device < 0 || device >= ndev) return fail(nullptr, PG3GPU_ERR_INVALID_ARGUMENT, "device %d out of range", device);
+
+    pg3gpu_ctx *ctx = new (std::nothrow) pg3gpu_ctx;
+    if (!ctx) return fail(nullptr, PG3GPU_ERR_OUT_OF_MEMORY, "host allocation failed");
+    ctx->device = device;
+    ctx->opts = *opts;
+    ctx->W = scene->camera.width;
+    ctx->H = scene->camera.height;
+    auto bail = [&](int s) {
+        g_createError = ctx->lastError;
+        pg3gpu_destroy(ctx);
+        return s;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "cudaSetDevice failed"));
+
+    SceneView &v = ctx->view;
+    v = hs.view;   // camera, counts, options
+    if ((st = upload(ctx, (float4 **)&v.tri, hs.tri))) return bail(st);
+    if ((st = upload(ctx, (int **)&v.triMat, hs.triMat))) return bail(st);
+    if ((st = upload(ctx, (float4 **)&v.sph, hs.sph))) return bail(st);
+    if ((st = upload(ctx, (int **)&v.sphMat, hs.sphMat))) return bail(st);
+    if ((st = upload(ctx, (DevMaterial **)&v.mats, hs.mats))) return bail(st);
+    if ((st = upload(ctx, (int **)&v.mat2light, hs.mat2light))) return bail(st);
+    if ((st = upload(ctx, (DevAreaLight **)&v.lights, hs.lights))) return bail(st);
+    if ((st = upload(ctx, (float4 **)&v.em, hs.em))) return bail(st);
+    if ((st = upload(ctx, (float **)&v.emMarg, hs.emMarg))) return bail(st);
+    if ((st = upload(ctx, (float **)&v.emCond, hs.emCond))) return bail(st);
+    if ((st = devAlloc(ctx, &ctx->dErr, 1))) return bail(st);
+    if (cudaMemset(ctx->dErr, 0, sizeof(unsigned int)) != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "memset"));
+    v.errorFlag = ctx->dErr;
+
+    // acceleration structure
+    const uint32_t nprim = v.ntri + v.nsph;
+    if (nprim >= 2) {
+        BvhNode *nodes;
+        void *scratch;
+        if ((st = devAlloc(ctx, &nodes, nprim - 1))) return bail(st);
+        if ((st = devAlloc(ctx, (char **)&scratch, lbvhScratchBytes(nprim)))) return bail(st);
+        cudaError_t e = buildLbvh(v, nodes, scratch, nullptr, nullptr, nullptr);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "LBVH build: %s", cudaGetErrorString(e)));
+        v.bvh = nodes;
+        v.bvhRoot = 0;
+    }
+    const int trav = opts->traversal;
+    v.useBvh = (nprim >= 2) && (trav == PG3GPU_TRAVERSAL_BVH || (trav == PG3GPU_TRAVERSAL_AUTO && nprim > 32));
+
+    if ((st = devAlloc(ctx, &ctx->dSum, (size_t)ctx->W * ctx->H * 3))) return bail(st);
+    if ((st = devAlloc(ctx, &ctx->dSumsq, (size_t)ctx->W * ctx->H * 3))) return bail(st);
+    if ((st = devAlloc(ctx, &ctx->dStats, 1))) return bail(st);
+    if (cudaMemset(ctx->dSum, 0, sizeof(double) * ctx->W * ctx->H * 3) != cudaSuccess ||
+        cudaMemset(ctx->dSumsq, 0, sizeof(double) * ctx->W * ctx->H * 3) != cudaSuccess ||
+        cudaMemset(ctx->dStats, 0, sizeof(DevStats)) != cudaSuccess)
+        return bail(fail(ctx, PG3GPU_ERR_CUDA, "memset"));
+
+    int sms = 0, perSm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (megakernelOccupancy(opts->algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE, &perSm) != cudaSuccess || perSm < 1)
+        perSm = 1;
+    ctx->megaGrid = sms * perSm;
+    ctx->useWavefront = (opts->pipeline == PG3GPU_PIPELINE_WAVEFRONT);
+    if (ctx->useWavefront) {
+        ctx->waveCapacity = 1ull << 20;
+        void *w;
+        if ((st = devAlloc(ctx, (char **)&w, wavefrontBytes(ctx->waveCapacity)))) return bail(st);
+        ctx->dWave = w;
+        ctx->waveGrid = sms * 8;
+    }
+    if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
+        return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));
+    if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "setup sync"));
+    *out = ctx;
+    return PG3GPU_OK;
+}
+
+int pg3gpu_set_stream(pg3gpu_ctx *ctx, void *stream)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    ctx->stream = reinterpret_cast<cudaStream_t>(stream);
+    return PG3GPU_OK;
+}
+
+int pg3gpu_run_iteration(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    if (algorithm != PG3GPU_ALG_PATH_TRACING && algorithm != PG3GPU_ALG_PATH_TRACING_NAIVE)
+        return fail(ctx, PG3GPU_ERR_UNSUPPORTED, "algorithm %d is not a path tracer", (int)algorithm);
+    if (spp == 0) return PG3GPU_OK;
+    cudaSetDevice(ctx->device);
+    const bool naive = algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE;
+    const uint32_t npix = ctx->W * ctx->H;
+    const uint32_t per = passesPerChunk(ctx, spp);
+    PG3_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    for (uint32_t done = 0; done < spp; done += per) {
+        const uint32_t passes = std::min(per, spp - done);
+        int st = renderChunk(ctx, naive, iteration + done, passes);
+        if (st) return st;
+        cudaError_t e = launchAccumulate(npix, passes, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2], ctx->dSum,
+                                         ctx->dSumsq, ctx->stream);
+        if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "accumulate: %s", cudaGetErrorString(e));
+    }
+    PG3_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->timed = true;
+    ctx->iterations += spp;
+    return PG3GPU_OK;
+}
+
+int pg3gpu_synchronize(pg3gpu_ctx *ctx)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    PG3_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    unsigned int flag = 0;
+    PG3_CUDA(ctx, cudaMemcpy(&flag, ctx->dErr, sizeof flag, cudaMemcpyDeviceToHost));
+    if (flag) return fail(ctx, PG3GPU_ERR_DEVICE_LIMIT, "kernel limit flag 0x%x (1: BVH stack, 2: queue, 4: steerable descent)", flag);
+    return PG3GPU_OK;
+}
+
+int pg3gpu_render_samples(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp, float *out)
+{
+    if (!ctx || !out) return PG3GPU_ERR_INVALID_ARGUMENT;
+    if (algorithm != PG3GPU_ALG_PATH_TRACING && algorithm != PG3GPU_ALG_PATH_TRACING_NAIVE)
+        return fail(ctx, PG3GPU_ERR_UNSUPPORTED, "algorithm %d is not a path tracer", (int)algorithm);
+    cudaSetDevice(ctx->device);
+    const uint32_t npix = ctx->W * ctx->H;
+    const uint32_t per = passesPerChunk(ctx, spp);
+    std::vector<float> tmp[3];
+    for (uint32_t done = 0; done < spp; done += per) {
+        const uint32_t passes = std::min(per, spp - done);
+        int st = renderChunk(ctx, algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE, iteration + done, passes);
+        if (st) return st;
+        const size_t n = (size_t)passes * npix;
+        for (int c = 0; c < 3; ++c) {
+            tmp[c].resize(n);
+            PG3_CUDA(ctx, cudaMemcpyAsync(tmp[c].data(), ctx->dOut[c], n * sizeof(float), cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+        }
+        PG3_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        float *dst = out + (size_t)done * npix * 3;
+        for (size_t i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) dst[i * 3 + c] = tmp[c][i];
+    }
+    return pg3gpu_synchronize(ctx);
+}
+
+int pg3gpu_read_framebuffer(pg3gpu_ctx *ctx, double *mean, double *var, uint64_t *iters)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    int st = pg3gpu_synchronize(ctx);
+    if (st) return st;
+    const size_t n = (size_t)ctx->W * ctx->H * 3;
+    std::vector<double> s(n), q(var ? n : 0);
+    PG3_CUDA(ctx, cudaMemcpy(s.data(), ctx->dSum, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (var) PG3_CUDA(ctx, cudaMemcpy(q.data(), ctx->dSumsq, n * sizeof(double), cudaMemcpyDeviceToHost));
+    const double it = (double)ctx->iterations;
+    for (size_t i = 0; i < n; ++i) {
+        const double m = it > 0 ? s[i] / it : 0.0;   // GetFramebuffer scaling (src/renderer.hxx:255-262)
+        if (mean) mean[i] = m;
+        if (var) var[i] = it > 1 ? std::max(0.0, (q[i] - it * m * m) / (it - 1)) : 0.0;
+    }
+    if (iters) *iters = ctx->iterations;
+    return PG3GPU_OK;
+}
+
+int pg3gpu_clear_framebuffer(pg3gpu_ctx *ctx)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    const size_t n = (size_t)ctx->W * ctx->H * 3 * sizeof(double);
+    PG3_CUDA(ctx, cudaMemsetAsync(ctx->dSum, 0, n, ctx->stream));
+    PG3_CUDA(ctx, cudaMemsetAsync(ctx->dSumsq, 0, n, ctx->stream));
+    ctx->iterations = 0;
+    return PG3GPU_OK;
+}
+
+uint64_t pg3gpu_iterations(const pg3gpu_ctx *ctx) { return ctx ? ctx->iterations : 0; }
+
+int pg3gpu_get_stats(pg3gpu_ctx *ctx, pg3gpu_stats *out)
+{
+    if (!ctx || !out) return PG3GPU_ERR_INVALID_ARGUMENT;
+    int st = pg3gpu_synchronize(ctx);
+    if (st) return st;
+    DevStats d;
+    PG3_CUDA(ctx, cudaMemcpy(&d, ctx->dStats, sizeof d, cudaMemcpyDeviceToHost));
+    out->paths = d.paths;
+    out->extension_rays = d.extRays;
+    out->shadow_rays = d.shadowRays;
+    out->terminated_by_russian_roulette = d.byRR;
+    out->terminated_by_background = d.byBackground;
+    out->terminated_by_blocker = d.byBlocker;
+    out->terminated_by_max_limit = d.byMax;
+    out->terminated_by_safety_limit = d.bySafety;
+    float ms = 0.f;
+    if (ctx->timed && cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) out->last_iteration_ms = ms;
+    else out->last_iteration_ms = 0.0;
+    return PG3GPU_OK;
+}
+
+int pg3gpu_reset_stats(pg3gpu_ctx *ctx)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    PG3_CUDA(ctx, cudaMemsetAsync(ctx->dStats, 0, sizeof(DevStats), ctx->stream));
+    return PG3GPU_OK;
+}
+
+int pg3gpu_device_framebuffer(pg3gpu_ctx *ctx, const double **sum, const double **sumsq)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    if (sum) *sum = ctx->dSum;
+    if (sumsq) *sumsq = ctx->dSumsq;
+    return PG3GPU_OK;
+}
+
+}  // extern "C"

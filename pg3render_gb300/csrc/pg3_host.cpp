@@ -1,0 +1,247 @@
+// Host-side scene preparation for the device layout (see pg3_host.h).
+#include "pg3_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+namespace pg3 {
+
+namespace {
+
+struct V { float x, y, z; };
+V sub(V a, V b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+V crossv(V a, V b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+float dotv(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+float lenv(V a) { return std::sqrt(dotv(a, a)); }
+V scale(V a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+V divv(V a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+V normv(V a) { return divv(a, lenv(a)); }
+V ld(const float *p) { return {p[0], p[1], p[2]}; }
+float3 f3(V a) { return make_float3(a.x, a.y, a.z); }
+bool finite3(const float *p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+const float kPi = 3.14159265358979f;
+const float kTiny = 9.5367431640625E-7f;
+float lum(float r, float g, float b) { return 0.212671f * r + 0.715160f * g + 0.072169f * b; }
+
+// ComputeCdf (src/distribution.hxx:45-74): running sum of f/n, then divide by the total.
+void computeCdf(const float *f, uint32_t n, float *cdf, float &integral)
+{
+    cdf[0] = 0.f;
+    for (uint32_t i = 1; i < n + 1; ++i) cdf[i] = cdf[i - 1] + f[i - 1] / n;
+    integral = cdf[n];
+    if (integral == 0.f)
+        for (uint32_t i = 1; i < n + 1; ++i) cdf[i] = (float)i / n;
+    else
+        for (uint32_t i = 1; i < n + 1; ++i) cdf[i] /= integral;
+}
+
+}  // namespace
+
+void buildEmCdf(const float *rgb, uint32_t W, uint32_t H, std::vector<float> &marg, std::vector<float> &cond)
+{
+    auto L = [&](int x, int y) {
+        // NormalizeImgCoords (src/em_image.hxx:269-302)
+        int rx = x, ry = y;
+        if (y >= (int)H) { rx = x + (int)W / 2; ry = (int)H - 1; }
+        else if (y < 0) { rx = x + (int)W / 2; ry = 0; }
+        int m = rx % (int)W;
+        if (m < 0) m += (int)W;
+        const float *p = rgb + ((size_t)ry * W + (size_t)m) * 3;
+        return lum(p[0], p[1], p[2]);
+    };
+    std::vector<float> f((size_t)W);
+    cond.assign((size_t)H * (W + 1), 0.f);
+    std::vector<float> rowInt(H);
+    const float w0 = 1 / 24.f, w1 = 2 / 3.f;
+    for (uint32_t r = 0; r < H; ++r) {
+        const float s = std::sin(kPi * (r + 0.5f) / H);   // SinMidTheta (src/em_simple_spherical_sampler.hxx:186-199)
+        for (uint32_t c = 0; c < W; ++c) {
+            // tent-filter pixel integral (src/em_image.hxx:152-183, src/filter.hxx:37-60)
+            const int x = (int)c, y = (int)r;
+            const float l00 = L(x - 1, y - 1), l01 = L(x - 1, y), l02 = L(x - 1, y + 1);
+            const float l10 = L(x, y - 1), l11 = L(x, y), l12 = L(x, y + 1);
+            const float l20 = L(x + 1, y - 1), l21 = L(x + 1, y), l22 = L(x + 1, y + 1);
+            const float avg = l00 * w0 + l01 * w0 + l02 * w0 + l10 * w0 + l11 * w1 + l12 * w0 + l20 * w0 +
+                              l21 * w0 + l22 * w0;
+            f[c] = s * avg;
+        }
+        computeCdf(f.data(), W, &cond[(size_t)r * (W + 1)], rowInt[r]);
+    }
+    marg.assign(H + 1, 0.f);
+    float total;
+    computeCdf(rowInt.data(), H, marg.data(), total);
+}
+
+int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out, std::string &err)
+{
+    char buf[256];
+    auto bad = [&](int st, const char *msg) { err = msg; return st; };
+    const pg3gpu_camera &c = sc.camera;
+    if (c.width == 0 || c.height == 0 || (uint64_t)c.width * c.height > (1ull << 28))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "camera resolution must be positive and at most 2^28 pixels");
+    if (!finite3(c.position) || !finite3(c.forward) || !finite3(c.up) || !(c.hfov_deg > 0.f && c.hfov_deg < 180.f))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "camera parameters must be finite, 0 < hfov < 180");
+    if (o.algorithm != PG3GPU_ALG_PATH_TRACING && o.algorithm != PG3GPU_ALG_PATH_TRACING_NAIVE)
+        return bad(PG3GPU_ERR_UNSUPPORTED, "only the path-tracing algorithms (6, 7) are implemented");
+    if (o.min_path_length < 1) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "min_path_length must be >= 1");
+    // the reference rejects these combinations (src/config.hxx:1063-1077)
+    if (o.max_path_length == 0 && o.min_path_length != 1)
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "min path length != 1 with Russian roulette ending paths");
+    if (o.max_path_length != 0 && o.min_path_length > o.max_path_length)
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "min path length larger than max path length");
+    if (o.indirect_clipping != 0.f) return bad(PG3GPU_ERR_UNSUPPORTED, "indirect illumination clipping is not implemented");
+    if (o.splitting_budget != 1) return bad(PG3GPU_ERR_UNSUPPORTED, "splitting budget other than 1 is not implemented");
+    if (o.em_sampler != PG3GPU_EM_CDF && o.em_sampler != PG3GPU_EM_COSINE && o.em_sampler != PG3GPU_EM_STEERABLE)
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown environment-map sampler");
+    if (o.em_sampler == PG3GPU_EM_STEERABLE)
+        return bad(PG3GPU_ERR_UNSUPPORTED, "steerable sampler not available in this build");
+    if (sc.num_materials == 0 || !sc.materials) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "scene has no materials");
+    if ((sc.num_triangles && !sc.triangles) || (sc.num_spheres && !sc.spheres) ||
+        (sc.num_area_lights && !sc.area_lights))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "NULL array with a nonzero count");
+    if (sc.num_triangles + (uint64_t)sc.num_spheres > (1u << 30))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "too many primitives");
+
+    SceneView &v = out.view;
+    // camera: the reference's raster-to-world matrix (src/camera.hxx:13-59) sends raster
+    // (x, y) along forward + right * ndc_x * tan(hfov/2) - up * ndc_y * tan(vfov/2)
+    {
+        const V fwd = normv(ld(c.forward));
+        const V up = ld(c.up);
+        const V mfwd = scale(fwd, -1.f);
+        const V right = normv(crossv(up, mfwd));
+        const V upv = crossv(mfwd, right);
+        v.camPos = f3(ld(c.position));
+        v.camFwd = f3(fwd);
+        v.camRight = f3(right);
+        v.camUp = f3(upv);
+        v.tanX = std::tan(0.5f * c.hfov_deg * (2.f * kPi / 360.f));
+        v.tanY = v.tanX * (float)c.height / (float)c.width;
+        v.width = c.width;
+        v.height = c.height;
+    }
+
+    // materials (src/materials.hxx:262-266, 791-806, 996-1021)
+    out.mats.resize(sc.num_materials);
+    for (uint32_t i = 0; i < sc.num_materials; ++i) {
+        const pg3gpu_material &m = sc.materials[i];
+        DevMaterial d{};
+        d.kind = m.kind;
+        d.r = m.albedo[0]; d.g = m.albedo[1]; d.b = m.albedo[2];
+        d.alpha = std::min(std::max(m.alpha, 0.001f), 1.0f);
+        d.eta = 1.f; d.etaInv = 1.f;
+        if (m.kind == PG3GPU_MAT_LAMBERT) {
+            if (!finite3(m.albedo) || m.albedo[0] < 0.f || m.albedo[1] < 0.f || m.albedo[2] < 0.f)
+                return bad(PG3GPU_ERR_INVALID_ARGUMENT, "Lambert albedo must be finite and non-negative");
+            const float mx = std::max(d.r, std::max(d.g, d.b));
+            const float p = std::min(std::max(0.15f * lum(d.r, d.g, d.b) + 0.85f * mx, 0.f), 1.f);
+            d.rrProb = std::min(std::max(p, 0.0f), 0.997f);
+            d.zeroRefl = (d.r == 0.f && d.g == 0.f && d.b == 0.f) ? 1 : 0;
+        } else if (m.kind == PG3GPU_MAT_GGX_CONDUCTOR) {
+            d.eta = (std::fabs(m.ior_outer) < kTiny) ? 1.0f : m.ior / m.ior_outer;
+            d.absorb = m.absorb;
+            d.rrProb = 0.997f;
+        } else if (m.kind == PG3GPU_MAT_GGX_DIELECTRIC) {
+            if (std::fabs(m.ior_outer) >= kTiny) { d.eta = m.ior / m.ior_outer; d.etaInv = m.ior_outer / m.ior; }
+            d.rrProb = 0.997f;
+        } else {
+            std::snprintf(buf, sizeof buf, "material %u: unknown kind %d", i, m.kind);
+            err = buf;
+            return PG3GPU_ERR_INVALID_ARGUMENT;
+        }
+        if (!(m.alpha >= 0.f) && m.kind != PG3GPU_MAT_LAMBERT)
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "GGX roughness must be >= 0");
+        out.mats[i] = d;
+    }
+
+    // geometry
+    out.tri.resize((size_t)sc.num_triangles * 3);
+    out.triMat.resize(sc.num_triangles);
+    for (uint32_t i = 0; i < sc.num_triangles; ++i) {
+        const pg3gpu_triangle &t = sc.triangles[i];
+        if (t.material < 0 || (uint32_t)t.material >= sc.num_materials)
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "triangle material id out of range");
+        const V p0 = ld(t.p), p1 = ld(t.p + 3), p2 = ld(t.p + 6);
+        const V nrm = normv(crossv(sub(p1, p0), sub(p2, p0)));   // src/scene_graph.hxx:88-101
+        if (!(std::isfinite(nrm.x) && std::isfinite(nrm.y) && std::isfinite(nrm.z)))
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "degenerate or non-finite triangle");
+        out.tri[3 * i] = make_float4(p0.x, p0.y, p0.z, nrm.x);
+        out.tri[3 * i + 1] = make_float4(p1.x, p1.y, p1.z, nrm.y);
+        out.tri[3 * i + 2] = make_float4(p2.x, p2.y, p2.z, nrm.z);
+        out.triMat[i] = t.material;
+    }
+    out.sph.resize(sc.num_spheres);
+    out.sphMat.resize(sc.num_spheres);
+    for (uint32_t i = 0; i < sc.num_spheres; ++i) {
+        const pg3gpu_sphere &s = sc.spheres[i];
+        if (s.material < 0 || (uint32_t)s.material >= sc.num_materials)
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "sphere material id out of range");
+        if (!finite3(s.center) || !(s.radius > 0.f) || !std::isfinite(s.radius))
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "sphere needs a finite centre and a positive radius");
+        out.sph[i] = make_float4(s.center[0], s.center[1], s.center[2], s.radius);
+        out.sphMat[i] = s.material;
+    }
+    v.ntri = sc.num_triangles;
+    v.nsph = sc.num_spheres;
+
+    // lights: area lights keep their order, the background comes last (src/scene.hxx:948-953)
+    out.mat2light.assign(sc.num_materials, -1);
+    out.lights.resize(sc.num_area_lights);
+    for (uint32_t i = 0; i < sc.num_area_lights; ++i) {
+        const pg3gpu_area_light &a = sc.area_lights[i];
+        if (a.triangle >= sc.num_triangles) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "area light triangle out of range");
+        if (!finite3(a.radiance)) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "area light radiance must be finite");
+        const pg3gpu_triangle &t = sc.triangles[a.triangle];
+        const V p0 = ld(t.p), e1 = sub(ld(t.p + 3), p0), e2 = sub(ld(t.p + 6), p0);
+        const V n = crossv(e1, e2);
+        const float len = lenv(n);
+        const V nz = divv(n, len);   // src/lights.hxx:59-75
+        DevAreaLight L;
+        L.p0_invArea = make_float4(p0.x, p0.y, p0.z, 2.f / len);
+        L.e1_r = make_float4(e1.x, e1.y, e1.z, a.radiance[0]);
+        L.e2_g = make_float4(e2.x, e2.y, e2.z, a.radiance[1]);
+        L.n_b = make_float4(nz.x, nz.y, nz.z, a.radiance[2]);
+        out.lights[i] = L;
+        if (out.mat2light[t.material] >= 0)
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "two area lights share one emitting material");
+        out.mat2light[t.material] = (int)i;
+    }
+    v.nArea = sc.num_area_lights;
+    v.bgKind = sc.background;
+    v.lightCount = v.nArea + (sc.background != PG3GPU_BG_NONE ? 1 : 0);
+    v.bgLightId = (sc.background != PG3GPU_BG_NONE) ? (int)v.nArea : -1;
+    v.bgConst = make_float3(sc.background_radiance[0], sc.background_radiance[1], sc.background_radiance[2]);
+    if (sc.background != PG3GPU_BG_NONE && sc.num_area_lights > 0)
+        return bad(PG3GPU_ERR_UNSUPPORTED,
+                   "a background light together with area lights needs the environment contribution estimate, "
+                   "which is not implemented");
+    if (sc.background == PG3GPU_BG_ENVMAP) {
+        if (!sc.env_map || sc.env_width < 2 || sc.env_height < 2 || (uint64_t)sc.env_width * sc.env_height > (1ull << 26))
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "environment map needs data and 2 <= size <= 2^26 pixels");
+        const size_t np = (size_t)sc.env_width * sc.env_height;
+        out.em.resize(np);
+        for (size_t i = 0; i < np; ++i) {
+            const float *p = sc.env_map + 3 * i;
+            if (!finite3(p) || p[0] < 0.f || p[1] < 0.f || p[2] < 0.f)
+                return bad(PG3GPU_ERR_INVALID_ARGUMENT, "environment map texels must be finite and non-negative");
+            out.em[i] = make_float4(p[0], p[1], p[2], 0.f);
+        }
+        buildEmCdf(sc.env_map, sc.env_width, sc.env_height, out.emMarg, out.emCond);
+        v.emW = sc.env_width;
+        v.emH = sc.env_height;
+    } else if (sc.background != PG3GPU_BG_NONE && sc.background != PG3GPU_BG_CONSTANT) {
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown background kind");
+    }
+    v.emSampler = o.em_sampler;
+    v.algorithm = o.algorithm;
+    v.minPL = o.min_path_length;
+    v.maxPL = o.max_path_length;
+    v.rrMinPL = o.rr_min_path_length;
+    v.seedLo = (uint32_t)o.seed;
+    v.seedHi = (uint32_t)(o.seed >> 32);
+    return PG3GPU_OK;
+}
+
+}  // namespace pg3

@@ -1,0 +1,36 @@
+// Host-side scene preparation: validation, camera basis, material records,
+// light table and the environment-map sampling tables, in device layout.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pg3gpu.h"
+#include "pg3_scene_view.h"
+
+namespace pg3 {
+
+struct HostScene {
+    SceneView view{};                    // counts, camera, options (device pointers filled later)
+    std::vector<float4> tri;
+    std::vector<int> triMat;
+    std::vector<float4> sph;
+    std::vector<int> sphMat;
+    std::vector<DevMaterial> mats;
+    std::vector<int> mat2light;
+    std::vector<DevAreaLight> lights;
+    std::vector<float4> em;
+    std::vector<float> emMarg, emCond;
+};
+
+// Returns PG3GPU_OK or an error status with a message in err.
+int prepareScene(const pg3gpu_scene &scene, const pg3gpu_options &opts, HostScene &out, std::string &err);
+
+// Environment-map CDF tables of the reference's spherical sampler
+// (src/em_simple_spherical_sampler.hxx:117-152, src/distribution.hxx:45-74, 484-501):
+// marg has H+1 entries, cond H rows of W+1 entries.
+void buildEmCdf(const float *rgb, uint32_t W, uint32_t H, std::vector<float> &marg, std::vector<float> &cond);
+
+}  // namespace pg3

@@ -1,0 +1,34 @@
+// Host-callable launchers of the device kernels (one translation unit each).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pg3_scene_view.h"
+
+namespace pg3 {
+
+constexpr int kMegaBlock = 128;
+
+// pg3_megakernel.cu
+cudaError_t launchMegakernel(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
+                             float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,
+                             cudaStream_t stream);
+cudaError_t megakernelOccupancy(bool naive, int *blocksPerSm);
+cudaError_t launchAccumulate(uint32_t npix, uint32_t passes, const float *r, const float *g, const float *b,
+                             double *sum, double *sumsq, cudaStream_t stream);
+
+// pg3_lbvh.cu
+size_t lbvhScratchBytes(uint32_t numPrims);
+cudaError_t buildLbvh(const SceneView &S, BvhNode *nodes, void *scratch, uint32_t *sortedCodesOut,
+                      uint32_t *sortedIdsOut, cudaStream_t stream);
+
+// pg3_wavefront.cu
+struct WavefrontBuffers;
+size_t wavefrontBytes(uint64_t capacity);
+cudaError_t launchWavefront(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
+                            float *outR, float *outG, float *outB, DevStats *stats, void *scratch,
+                            uint64_t capacity, int gridBlocks, cudaStream_t stream);
+
+}  // namespace pg3

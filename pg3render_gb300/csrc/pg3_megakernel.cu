@@ -1,0 +1,98 @@
+// Megakernel pipeline: one thread carries one camera path from the camera to
+// its last vertex, then writes its radiance to the per-sample buffer.
+//
+// Launch shape: a persistent grid (SM count x resident blocks per SM) striding
+// over path indices; consecutive threads take consecutive pixels of the same
+// sample pass, so neighbouring lanes start with nearly identical primary rays.
+#include "pg3_estimator.cuh"
+#include "pg3_kernels.h"
+
+namespace pg3 {
+
+PG3_DI void flushCounters(DevStats *st, const PathCounters &c, uint32_t paths)
+{
+    const unsigned mask = __activemask();
+    const uint32_t vals[8] = {paths, c.ext, c.shadow, c.rr, c.bg, c.blocker, c.maxl, c.safety};
+    unsigned long long *dst = &st->paths;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const uint32_t s = __reduce_add_sync(mask, vals[i]);
+        if ((threadIdx.x & 31) == (__ffs(mask) - 1) && s) atomicAdd(dst + i, (unsigned long long)s);
+    }
+}
+
+template <bool kNaive>
+__global__ void __launch_bounds__(kMegaBlock) megakernel(const __grid_constant__ SceneView S, uint32_t sample0,
+                                                         uint64_t numPaths, uint32_t npix, float *__restrict__ outR,
+                                                         float *__restrict__ outG, float *__restrict__ outB,
+                                                         DevStats *stats)
+{
+    PathCounters pc;
+    uint32_t done = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < numPaths; i += stride) {
+        const uint32_t pixel = (uint32_t)(i % npix);
+        const uint32_t sample = sample0 + (uint32_t)(i / npix);
+        const float3 L = kNaive ? tracePathNaive(S, pixel, sample, pc) : tracePath(S, pixel, sample, pc);
+        outR[i] = L.x;
+        outG[i] = L.y;
+        outB[i] = L.z;
+        ++done;
+    }
+    flushCounters(stats, pc, done);
+}
+
+// Adds `passes` samples per pixel from the per-sample buffer into the fp64
+// framebuffer accumulators (sum and sum of squares). Samples are summed in fp32
+// in groups of 32 and the group sums in fp64, which keeps the fp64 work at 1/32.
+__global__ void __launch_bounds__(256) accumulateKernel(uint32_t npix, uint32_t passes, const float *__restrict__ inR,
+                                                         const float *__restrict__ inG, const float *__restrict__ inB,
+                                                         double *__restrict__ sum, double *__restrict__ sumsq)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    double s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+    for (uint32_t k0 = 0; k0 < passes; k0 += 32) {
+        float fs[3] = {0, 0, 0}, fq[3] = {0, 0, 0};
+        const uint32_t k1 = min(passes, k0 + 32);
+        for (uint32_t k = k0; k < k1; ++k) {
+            const size_t idx = (size_t)k * npix + p;
+            const float v[3] = {inR[idx], inG[idx], inB[idx]};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { fs[c] += v[c]; fq[c] += v[c] * v[c]; }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { s[c] += fs[c]; q[c] += fq[c]; }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        sum[(size_t)p * 3 + c] += s[c];
+        sumsq[(size_t)p * 3 + c] += q[c];
+    }
+}
+
+cudaError_t launchMegakernel(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
+                             float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,
+                             cudaStream_t stream)
+{
+    if (naive)
+        megakernel<true><<<gridBlocks, kMegaBlock, 0, stream>>>(S, sample0, numPaths, npix, outR, outG, outB, stats);
+    else
+        megakernel<false><<<gridBlocks, kMegaBlock, 0, stream>>>(S, sample0, numPaths, npix, outR, outG, outB, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t megakernelOccupancy(bool naive, int *blocksPerSm)
+{
+    return naive ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, megakernel<true>, kMegaBlock, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, megakernel<false>, kMegaBlock, 0);
+}
+
+cudaError_t launchAccumulate(uint32_t npix, uint32_t passes, const float *r, const float *g, const float *b,
+                             double *sum, double *sumsq, cudaStream_t stream)
+{
+    accumulateKernel<<<(npix + 255) / 256, 256, 0, stream>>>(npix, passes, r, g, b, sum, sumsq);
+    return cudaGetLastError();
+}
+
+}  // namespace pg3

@@ -1,0 +1,118 @@
+// Device-side scene layout shared by the host setup code and the kernels.
+//
+// Everything a kernel reads lives in HBM in structure-of-arrays form and is
+// passed to kernels by value in one SceneView (kernel-parameter space), so a
+// launch needs no extra indirection. Geometry is stored the way the closest-
+// hit loop consumes it: three float4 per triangle (vertex xyz + one normal
+// component in w), one float4 per sphere (centre, radius).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pg3 {
+
+enum : int { kMatLambert = 0, kMatGgxConductor = 1, kMatGgxDielectric = 2 };
+enum : int { kBgNone = 0, kBgConstant = 1, kBgEnvMap = 2 };
+enum : int { kEmCdf = 0, kEmCosine = 1, kEmSteerable = 2 };
+
+struct DevMaterial {          // 48 bytes
+    int kind;
+    float r, g, b;            // Lambert reflectance
+    float alpha;              // GGX roughness (already clamped)
+    float eta, etaInv;        // inner/outer, outer/inner
+    float absorb;             // conductor k
+    float rrProb;             // Russian-roulette continuation probability (clamped to 0.997)
+    int zeroRefl;             // Lambert with zero reflectance: paths end here (lights)
+    int pad0, pad1;
+};
+
+struct DevAreaLight {         // 64 bytes; radiance rides in the w lanes
+    float4 p0_invArea;        // p0.xyz, 1/area
+    float4 e1_r;              // edge p1 - p0, radiance r
+    float4 e2_g;              // edge p2 - p0, radiance g
+    float4 n_b;               // frame normal xyz, radiance b
+};
+
+// Linear BVH node (Karras 2012 layout, children as signed ids: >= 0 inner node,
+// < 0 leaf ~primitive slot); boxes of both children stored in the parent so a
+// traversal step is one 64-byte read.
+struct BvhNode {
+    float4 lo_l;              // left child box min xyz, left child id (as int bits)
+    float4 hi_l;              // left child box max xyz, unused
+    float4 lo_r;              // right child box min xyz, right child id (as int bits)
+    float4 hi_r;              // right child box max xyz, unused
+};
+
+// Steerable sampler tables (filled by the host build; see steerable.cpp).
+struct SteerView {
+    const float4 *vdir;       // per vertex: unit direction xyz, unused
+    const float *vsh;         // per vertex: 9 SH-weighted coefficients (luminance basis values)
+    const int4 *tri;          // per leaf triangle: vertex ids (x, y, z), unused
+    const float *nodeW;       // per tree node: 9 summed coefficients
+    const int *nodeChild;     // per tree node: 6 child ids (>= 0 node, < 0 ~leaf triangle, INT_MIN none)
+    uint32_t numNodes, numTris;
+    int root;
+};
+
+struct SceneView {
+    // camera (pinhole equivalent of the reference's raster-to-world matrix)
+    float3 camPos, camFwd, camRight, camUp;
+    float tanX, tanY;
+    uint32_t width, height;
+
+    // geometry
+    const float4 *tri;        // 3 per triangle
+    const int *triMat;
+    const float4 *sph;
+    const int *sphMat;
+    uint32_t ntri, nsph;
+
+    // acceleration structure (null when the list loop is used)
+    const BvhNode *bvh;
+    uint32_t bvhRoot;         // root node id (valid when nprims > 1)
+    int useBvh;
+
+    // materials and lights
+    const DevMaterial *mats;
+    const int *mat2light;     // material id -> light id or -1
+    uint32_t nmat;
+    const DevAreaLight *lights;
+    uint32_t nArea;
+    uint32_t lightCount;      // area lights + background
+    int bgKind;
+    int bgLightId;
+    float3 bgConst;
+
+    // environment map (lat-long, float4 texels) and its samplers
+    const float4 *em;
+    uint32_t emW, emH;
+    const float *emMarg;      // marginal CDF over rows (emH + 1)
+    const float *emCond;      // conditional CDFs, emH rows of (emW + 1)
+    int emSampler;
+    SteerView steer;
+
+    // options
+    int algorithm;
+    uint32_t minPL, maxPL, rrMinPL;
+    uint32_t seedLo, seedHi;
+
+    // device error word (bounded loops set bits instead of trapping)
+    unsigned int *errorFlag;
+};
+
+// Per-launch counters (PathTerminationReason histogram + ray totals).
+struct DevStats {
+    unsigned long long paths;
+    unsigned long long extRays;
+    unsigned long long shadowRays;
+    unsigned long long byRR;
+    unsigned long long byBackground;
+    unsigned long long byBlocker;
+    unsigned long long byMax;
+    unsigned long long bySafety;
+};
+
+enum : unsigned int { kErrTraversalStack = 1u, kErrQueueOverflow = 2u, kErrSteerDescent = 4u };
+
+}  // namespace pg3

@@ -1,0 +1,157 @@
+"""Host-side mirror of the reference's renderer interface over the C ABI.
+
+``Config`` carries the options of the reference's ``Config`` that the path
+tracer reads (src/config.hxx:1100-1137); ``GpuPathTracer`` behaves like a
+``PathTracer`` (src/path_tracer.hxx:5-41) deriving from ``AbstractRenderer``
+(src/renderer.hxx:232-278): ``RunIteration`` renders one (or ``spp``)
+iterations, ``GetFramebuffer`` returns the accumulated image divided by the
+iteration count, ``WasUsed`` tells whether any iteration ran. Errors the
+reference reports with PG3_FATAL_ERROR raise :class:`Pg3Error` here.
+"""
+import ctypes
+import dataclasses
+
+import numpy as np
+
+from . import _lib
+from ._lib import (ALG_PATH_TRACING, ALG_PATH_TRACING_NAIVE, EM_CDF, EM_COSINE, EM_STEERABLE,  # noqa: F401
+                   PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT, TRAVERSAL_AUTO, TRAVERSAL_BVH,
+                   TRAVERSAL_LIST, Pg3Error)
+
+# Algorithm enum of src/config.hxx:23-34
+kEyeLight, kNormalVisualiser, kDirectIllumBsdfSampling, kDirectIllumLightSamplingAll, \
+    kDirectIllumLightSamplingSingle, kDirectIllumMis, kPathTracingNaive, kPathTracing = range(8)
+
+
+@dataclasses.dataclass
+class Config:
+    scene: object = None                 # pg3render_gb300.scene.Scene
+    algorithm: int = kPathTracing        # mAlgorithm
+    iterations: int = 1                  # mIterations
+    base_seed: int = 1234                # mBaseSeed
+    min_path_length: int = 1             # mMinPathLength
+    max_path_length: int = 0             # mMaxPathLength (0: Russian roulette)
+    indirect_illum_clipping: float = 0.0  # mIndirectIllumClipping (only 0 implemented)
+    splitting_budget: int = 1            # mSplittingBudget (only 1 implemented)
+    em_sampler: int = EM_CDF             # compile-time PG3_USE_ENVMAP_* in the reference
+    rr_min_path_length: int = 0          # extension: roulette from this length on with a max length set
+    traversal: int = TRAVERSAL_AUTO
+    pipeline: int = PIPELINE_AUTO
+    steer_subdiv_level: int = 3
+    max_paths_in_flight: int = 0
+
+    def options(self, seed=None):
+        o = _lib.Options()
+        _lib.load().pg3gpu_default_options(ctypes.byref(o))
+        o.algorithm = self.algorithm
+        o.min_path_length = self.min_path_length
+        o.max_path_length = self.max_path_length
+        o.rr_min_path_length = self.rr_min_path_length
+        o.indirect_clipping = self.indirect_illum_clipping
+        o.splitting_budget = self.splitting_budget
+        o.em_sampler = self.em_sampler
+        o.traversal = self.traversal
+        o.pipeline = self.pipeline
+        o.steer_subdiv_level = self.steer_subdiv_level
+        o.seed = self.base_seed if seed is None else seed
+        o.max_paths_in_flight = self.max_paths_in_flight
+        return o
+
+
+class GpuPathTracer:
+    """One GPU renderer context (the reference creates one renderer per thread;
+    here one context renders whole iterations on the device)."""
+
+    def __init__(self, config: Config, seed=None, device=0, stream=None):
+        self.config = config
+        self._L = _lib.load()
+        self._desc = _lib.scene_desc(config.scene)
+        self._opts = config.options(seed)
+        h = ctypes.c_void_p()
+        _lib.check(self._L.pg3gpu_create(ctypes.byref(self._desc), ctypes.byref(self._opts), device, ctypes.byref(h)))
+        self._ctx = h
+        self.width = config.scene.camera.width
+        self.height = config.scene.camera.height
+        if stream is not None:
+            self.set_stream(stream)
+
+    # -- reference-named entry points ------------------------------------------------
+    def RunIteration(self, algorithm, iteration, spp=1):   # noqa: N802
+        _lib.check(self._L.pg3gpu_run_iteration(self._ctx, algorithm, iteration, spp), self._ctx)
+
+    def GetFramebuffer(self):   # noqa: N802
+        return self.framebuffer()[0]
+
+    def WasUsed(self):   # noqa: N802
+        return self.iterations > 0
+
+    # -- pythonic helpers --------------------------------------------------------------
+    run_iteration = RunIteration
+
+    @property
+    def iterations(self):
+        return int(self._L.pg3gpu_iterations(self._ctx))
+
+    def set_stream(self, stream):
+        ptr = stream if isinstance(stream, int) else getattr(stream, "cuda_stream", stream)
+        _lib.check(self._L.pg3gpu_set_stream(self._ctx, ctypes.c_void_p(ptr)), self._ctx)
+
+    def synchronize(self):
+        _lib.check(self._L.pg3gpu_synchronize(self._ctx), self._ctx)
+
+    def framebuffer(self, with_variance=False):
+        n = self.width * self.height * 3
+        mean = np.zeros(n, np.float64)
+        var = np.zeros(n, np.float64) if with_variance else None
+        it = ctypes.c_uint64()
+        _lib.check(self._L.pg3gpu_read_framebuffer(
+            self._ctx, mean.ctypes.data_as(ctypes.c_void_p),
+            var.ctypes.data_as(ctypes.c_void_p) if var is not None else None, ctypes.byref(it)), self._ctx)
+        shape = (self.height, self.width, 3)
+        return mean.reshape(shape), (var.reshape(shape) if var is not None else None), int(it.value)
+
+    def clear(self):
+        _lib.check(self._L.pg3gpu_clear_framebuffer(self._ctx), self._ctx)
+
+    def render_samples(self, algorithm, iteration, spp):
+        out = np.zeros((spp, self.height, self.width, 3), np.float32)
+        _lib.check(self._L.pg3gpu_render_samples(self._ctx, algorithm, iteration, spp,
+                                                  out.ctypes.data_as(ctypes.c_void_p)), self._ctx)
+        return out
+
+    def stats(self):
+        s = _lib.Stats()
+        _lib.check(self._L.pg3gpu_get_stats(self._ctx, ctypes.byref(s)), self._ctx)
+        return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+
+    def reset_stats(self):
+        _lib.check(self._L.pg3gpu_reset_stats(self._ctx), self._ctx)
+
+    def device_framebuffer(self):
+        a, b = ctypes.c_void_p(), ctypes.c_void_p()
+        _lib.check(self._L.pg3gpu_device_framebuffer(self._ctx, ctypes.byref(a), ctypes.byref(b)), self._ctx)
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.pg3gpu_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def render(config: Config, spp=None, seed=None, device=0):
+    """Convenience: renders config.iterations (or spp) samples and returns the mean image."""
+    with GpuPathTracer(config, seed=seed, device=device) as r:
+        r.RunIteration(config.algorithm, 0, spp or config.iterations)
+        return r.GetFramebuffer()

@@ -1,0 +1,62 @@
+#!/usr/bin/env python3
+"""Generates the golden images in tests/golden/ from the reference renderer's
+own code (oracle/_ref/pg3ref_* built by oracle/build_ref.py from the reference
+sources). Run here, where the reference checkout exists; the fixtures are
+committed so that tests on other machines need neither the reference nor its
+build.
+
+Each fixture ``<name>.npz`` holds
+  scene_text   the scene in the oracle/harness text format (EM path placeholder)
+  env_map      float32 [H, W, 3] or empty
+  mean         float64 [h, w, 3]  mean over K*N reference iterations
+  var_mean     float64 [h, w, 3]  variance of that mean (var of one renderer's mean / K)
+  spp          K*N
+and the options the scene was rendered with.
+"""
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from pg3render_gb300 import scene as S  # noqa: E402
+
+CASES = {
+    # name: (builder, max_path_length, em_sampler, algorithm, renderers, iterations)
+    "cornell_area_32": (lambda: S.cornell_box(32, 32), 8, "cdf", "pt", 64, 128),
+    "cornell_area_32_naive": (lambda: S.cornell_box(32, 32), 8, "cdf", "ptn", 64, 128),
+    "cornell_area_32_rr": (lambda: S.cornell_box(32, 32), 0, "cdf", "pt", 64, 128),
+    "cornell_env_32_cdf": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cdf", "pt", 64, 128),
+    "cornell_env_32_cos": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cosine", "pt", 64, 128),
+}
+
+EM_TOKEN = "@EM@"
+
+
+def make(name):
+    build, maxpl, sampler, alg, K, N = CASES[name]
+    scene = build()
+    with tempfile.TemporaryDirectory() as td:
+        em_path = os.path.join(td, "em.bin")
+        if scene.env_map is not None:
+            scene.write_env_map(em_path)
+        text = scene.to_text(em_path=em_path, algorithm=alg, max_path_length=maxpl)
+        r = O.reference_render(text, renderers=K, iters=N, seed=4321, em_sampler=sampler)
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        scene_text=np.array(text.replace(em_path, EM_TOKEN)),
+        env_map=(scene.env_map if scene.env_map is not None else np.zeros((0, 0, 3), np.float32)),
+        mean=r["mean"], var_mean=r["var_of_renderer_mean"] / K, spp=np.array(K * N),
+        max_path_length=np.array(maxpl), em_sampler=np.array(sampler), algorithm=np.array(alg))
+    print(name, "done", r["timing"])
+
+
+if __name__ == "__main__":
+    for n in (sys.argv[1:] or CASES):
+        make(n)

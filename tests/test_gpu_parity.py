@@ -1,0 +1,125 @@
+"""Parity of the CUDA path with the oracle and with the reference (GPU tests).
+
+* path by path: the CUDA kernels and the C++ oracle draw the same Philox
+  numbers, so each sample's radiance must agree up to float rounding (a few
+  paths may take another branch after a rounding difference);
+* against the reference: golden images rendered by the reference's own code
+  (tests/golden) must agree per pixel, |z| <= 4 on >= 99.9% of pixel channels.
+"""
+import numpy as np
+import pytest
+
+import pg3render_gb300 as P
+from pg3render_gb300 import scene as S
+
+from _util import load_golden, scene_from_golden, z_ok, zscores
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr",
+                "cornell_env_32_cdf", "cornell_env_32_cos"]
+SAMPLERS = {"cdf": P.renderer.EM_CDF, "cosine": P.renderer.EM_COSINE}
+
+# Path-by-path tolerance: per sample and channel |gpu - oracle| <= 1e-3 * max(1, |oracle|)
+# for at least 99% of the samples (the rest may have taken another branch).
+REL_TOL = 1e-3
+MIN_MATCH = 0.99
+
+
+def _cfg(scene, maxpl, alg=P.renderer.kPathTracing, sampler=P.renderer.EM_CDF, **kw):
+    return P.Config(scene=scene, algorithm=alg, max_path_length=maxpl, em_sampler=sampler, **kw)
+
+
+def _oracle_samples(scene, text, spp, seed, sampler=0, rr=0):
+    import oracle as O
+    o = O.render(text, scene.camera.width, scene.camera.height, seed=seed, spp=spp, em_sampler=sampler,
+                 rr_min_path_length=rr, per_sample=True)
+    return o["samples"]
+
+
+def _match_fraction(g, o):
+    ok = np.abs(g - o) <= REL_TOL * np.maximum(1.0, np.abs(o))
+    return float(ok.mean())
+
+
+@pytest.mark.parametrize("case", ["area", "area_naive", "env_cdf", "env_cos"])
+def test_path_by_path_vs_oracle(case, tmp_path):
+    if case.startswith("area"):
+        scene = S.cornell_box(24, 24)
+        maxpl, sampler = 8, 0
+    else:
+        scene = S.cornell_env(24, 24, 64, 32)
+        maxpl, sampler = 12, (0 if case == "env_cdf" else 1)
+    alg = P.renderer.kPathTracingNaive if case.endswith("naive") else P.renderer.kPathTracing
+    em = str(tmp_path / "em.bin")
+    if scene.env_map is not None:
+        scene.write_env_map(em)
+    text = scene.to_text(em_path=em, algorithm="ptn" if alg == 6 else "pt", max_path_length=maxpl)
+    seed = 77
+    with P.GpuPathTracer(_cfg(scene, maxpl, alg, sampler), seed=seed) as r:
+        g = r.render_samples(alg, 0, 8)
+    o = _oracle_samples(scene, text, 8, seed, sampler)
+    frac = _match_fraction(g, o)
+    assert frac >= MIN_MATCH, "only %.4f of samples match the oracle" % frac
+    # the sample means agree much tighter than the per-pixel noise
+    assert np.allclose(g.mean(axis=(0, 1, 2)), o.mean(axis=(0, 1, 2)), rtol=2e-2)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_against_reference_golden(name):
+    d, text, td = load_golden(name)
+    scene = scene_from_golden(d)
+    alg = P.renderer.kPathTracingNaive if str(d["algorithm"]) == "ptn" else P.renderer.kPathTracing
+    cfg = _cfg(scene, int(d["max_path_length"]), alg, SAMPLERS[str(d["em_sampler"])])
+    spp = 8192
+    with P.GpuPathTracer(cfg, seed=2024) as r:
+        r.RunIteration(alg, 0, spp)
+        mean, var, n = r.framebuffer(with_variance=True)
+        assert n == spp and r.WasUsed()
+    z = zscores(mean, var / spp, d["mean"], d["var_mean"])
+    frac, zm, zs = z_ok(z)
+    assert frac >= 0.999, "%s: only %.4f of |z| <= 4 (mean z %.3f, std %.3f)" % (name, frac, zm, zs)
+    assert abs(zm) < 0.25 and 0.7 < zs < 1.3, "%s: z distribution off (mean %.3f, std %.3f)" % (name, zm, zs)
+
+
+def test_bvh_and_list_traversal_identical():
+    scene = S.cornell_box(24, 24)
+    outs = []
+    for trav in (P.renderer.TRAVERSAL_LIST, P.renderer.TRAVERSAL_BVH):
+        with P.GpuPathTracer(_cfg(scene, 8, traversal=trav), seed=5) as r:
+            outs.append(r.render_samples(P.renderer.kPathTracing, 0, 4))
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_iterations_accumulate_like_get_framebuffer():
+    scene = S.cornell_box(16, 16)
+    with P.GpuPathTracer(_cfg(scene, 8), seed=11) as r:
+        assert not r.WasUsed()
+        samples = r.render_samples(P.renderer.kPathTracing, 0, 6)
+        r.RunIteration(P.renderer.kPathTracing, 0, 2)
+        r.RunIteration(P.renderer.kPathTracing, 2, 4)
+        mean = r.GetFramebuffer()
+        assert r.iterations == 6
+    assert np.allclose(mean, samples.astype(np.float64).mean(axis=0), rtol=1e-5, atol=1e-6)
+
+
+def test_stats_counts():
+    scene = S.cornell_box(16, 16)
+    with P.GpuPathTracer(_cfg(scene, 8), seed=3) as r:
+        r.RunIteration(P.renderer.kPathTracing, 0, 4)
+        st = r.stats()
+    assert st["paths"] == 16 * 16 * 4
+    assert st["extension_rays"] >= st["paths"]
+    ended = (st["terminated_by_background"] + st["terminated_by_blocker"] + st["terminated_by_max_limit"]
+             + st["terminated_by_russian_roulette"])
+    assert ended <= st["paths"] and ended > 0
+    assert st["terminated_by_max_limit"] > 0   # a closed box keeps many paths to the limit
+
+
+def test_chunked_launches_match_single_launch():
+    scene = S.cornell_box(16, 16)
+    outs = []
+    for cap in (0, 16 * 16):   # default chunking vs one sample pass per launch
+        with P.GpuPathTracer(_cfg(scene, 8, max_paths_in_flight=cap), seed=9) as r:
+            outs.append(r.render_samples(P.renderer.kPathTracing, 3, 5))
+    assert np.array_equal(outs[0], outs[1])
