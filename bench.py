@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""Headline benchmark: Msamples/s of the NEE+MIS path tracer on the
+environment-map Cornell box (512x512, 256 spp, max path length 12, Russian
+roulette after 3 bounces, synthetic 1024x512 sky), one JSON line on stdout.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+A step renders the whole workload once (512*512*256 = 67,108,864 camera paths).
+* value    device time (CUDA events on the library's stream) of K steps, inputs
+           resident in HBM, L2 flushed between steps (a 256 MiB memset outside
+           the timed events);
+* e2e      the same metric through the C ABI as a user calls it with host
+           buffers: create (scene + environment map host->device), render,
+           read the framebuffer (device->host), destroy -- per step;
+* roofline algorithmic bytes of the path kernel per launch (per segment 360 B,
+           per path 72 B start + 36 B end, the wavefront record sizes) over its
+           event-timed launch duration, against the measured HBM copy peak;
+* cpu_baseline the reference's own CPU renderer (oracle/_ref, built from the
+           reference sources) on all host cores over a bounded sample.
+--impl reference times that CPU renderer alone as the main line.
+With N > 1 (torchrun) every rank renders its own sample range of the same
+workload (weak scaling, no collective on the data path).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Msamples/s at matched rel-MSE vs CPU"
+UNIT = "Msamples/s"
+WIDTH = HEIGHT = 512
+SPP = 256
+MAX_PATH = 12
+RR_FROM = 4            # Russian roulette from path length 4, i.e. after 3 bounces
+EM_W, EM_H = 1024, 512
+# per-unit algorithmic bytes of the wavefront record layout (ray 32, hit 16, state 40, shadow 48)
+BYTES_PER_SEGMENT = 360
+BYTES_PER_PATH = 72 + 36
+# DRAM bytes per path-kernel launch measured by ncu on the same workload
+# (profiles/megakernel_cornell_env.md); None until captured for the current kernel.
+NCU_TRAFFIC_PER_PATH = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--sampler", default="auto", choices=["auto", "steerable", "cdf", "cosine"])
+    ap.add_argument("--pipeline", default="auto", choices=["auto", "megakernel", "wavefront"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    # smaller cases of the same workload (profiling captures); the headline uses the defaults
+    ap.add_argument("--width", type=int, default=512)
+    ap.add_argument("--spp", type=int, default=256)
+    ap.add_argument("--cpu-iters", type=int, default=12)
+    a = ap.parse_args()
+    global WIDTH, HEIGHT, SPP
+    WIDTH = HEIGHT = a.width
+    SPP = a.spp
+    return a
+
+
+def build_scene():
+    from pg3render_gb300 import scene as S
+    return S.cornell_env(WIDTH, HEIGHT, EM_W, EM_H, em_seed=7)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(scene, sampler, threads=None, iters=1):
+    """The reference's own CPU renderer (oracle/_ref) on the same scene, all host cores,
+    `threads` renderers x `iters` iterations at 512x512; falls back to the oracle port."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    threads = threads or os.cpu_count() or 1
+    ref_sampler = {"steerable": "steerable", "cdf": "cdf", "cosine": "cosine"}[sampler]
+    with tempfile.TemporaryDirectory() as td:
+        em = os.path.join(td, "em.bin")
+        scene.write_env_map(em)
+        text = scene.to_text(em_path=em, max_path_length=MAX_PATH)
+        if O.reference_binary(ref_sampler):
+            extra = ["--em-params", "5", "3", "3"] if ref_sampler == "steerable" else []
+            r = O.reference_render(text, renderers=threads, iters=iters, threads=threads, seed=1,
+                                   em_sampler=ref_sampler, time_only=True, extra=extra)
+            t = r["timing"]
+            return {"value": t["msamples_per_s"], "unit": UNIT, "cores": t["threads"], "kind": "reference",
+                    "sample": "%d renderers x %d iteration(s) of the %dx%d scene (%.1f M paths, %.1f s), max path "
+                              "length %d without roulette (the reference applies roulette only without a length "
+                              "limit), %s sampler" % (threads, iters, WIDTH, HEIGHT, t["samples"] / 1e6,
+                                                      t["seconds"], MAX_PATH, ref_sampler)}
+        # oracle port (C++ restatement) -- CDF / cosine only
+        t0 = time.perf_counter()
+        spp = max(1, iters * threads // 8)
+        O.render(text, WIDTH, HEIGHT, seed=1, spp=spp, em_sampler=0 if sampler == "cdf" else 1,
+                 rr_min_path_length=RR_FROM, threads=threads)
+        dt = time.perf_counter() - t0
+        return {"value": WIDTH * HEIGHT * spp / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": "%d spp of the %dx%d scene" % (spp, WIDTH, HEIGHT)}
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    import pg3render_gb300 as P
+    from pg3render_gb300 import _lib
+    from pg3render_gb300 import renderer as R
+
+    torch.cuda.set_device(local_rank)
+    scene = build_scene()
+    sampler = args.sampler
+    if sampler == "auto":
+        sampler = "steerable" if steerable_available() else "cdf"
+    em_sampler = {"steerable": R.EM_STEERABLE, "cdf": R.EM_CDF, "cosine": R.EM_COSINE}[sampler]
+    pipeline = {"auto": R.PIPELINE_AUTO, "megakernel": R.PIPELINE_MEGAKERNEL,
+                "wavefront": R.PIPELINE_WAVEFRONT}[args.pipeline]
+    cfg = P.Config(scene=scene, algorithm=R.kPathTracing, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM,
+                   em_sampler=em_sampler, pipeline=pipeline, base_seed=1234)
+    npix = WIDTH * HEIGHT
+    paths_per_step = npix * SPP
+    sample_base = rank * (1 << 24)
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    r = P.GpuPathTracer(cfg, device=local_rank)
+    for w in range(args.warmup):
+        r.RunIteration(R.kPathTracing, sample_base + w * SPP, SPP)
+    r.synchronize()
+    r.reset_stats()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            flush.zero_()                                  # L2 flush, outside the events
+            starts[k].record()
+            r.RunIteration(R.kPathTracing, sample_base + (args.warmup + k) * SPP, SPP)
+            stops[k].record()
+        torch.cuda.synchronize()
+    r.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
+    total_s = sum(step_ms) / 1e3
+    st = r.stats()
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        total_s = float(t.item())
+    value = world * args.steps * paths_per_step / total_s / 1e6
+
+    # roofline of the path kernel
+    launches = max(1, st["path_kernel_launches"])
+    launch_ms = st["path_kernel_ms"] / launches
+    alg_bytes = (BYTES_PER_SEGMENT * st["extension_rays"] + BYTES_PER_PATH * st["paths"]) / launches
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    traffic = (NCU_TRAFFIC_PER_PATH * st["paths"] / launches) if NCU_TRAFFIC_PER_PATH else None
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "megakernel" if args.pipeline != "wavefront" else "wavefront",
+                "launch_ms": round(launch_ms, 4), "algorithmic_bytes_per_launch": int(alg_bytes),
+                "segments_per_path": round(st["extension_rays"] / max(1, st["paths"]), 4),
+                "shadow_rays_per_path": round(st["shadow_rays"] / max(1, st["paths"]), 4)}
+    gpu_launches = int(st["kernel_launches"])
+    r.close()
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 5))
+    if e2e_steps == 0:
+        e2e = None
+    desc_bytes = (scene.env_map.nbytes + 40 * len(scene.triangles) + 20 * len(scene.spheres)
+                  + 32 * len(scene.materials) + 16 * len(scene.area_lights))
+    d2h = npix * 3 * 8
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    img = None
+    for k in range(e2e_steps):
+        with P.GpuPathTracer(cfg, device=local_rank) as rr:
+            rr.RunIteration(R.kPathTracing, sample_base + k * SPP, SPP)
+            img = rr.GetFramebuffer()
+    torch.cuda.synchronize()
+    e2e_s = max(time.perf_counter() - t0, 1e-9)
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = None if e2e_steps == 0 else {"value": round(world * e2e_steps * paths_per_step / e2e_s / 1e6, 3), "unit": UNIT,
+           "h2d_bytes_per_step": int(desc_bytes), "d2h_bytes_per_step": int(d2h),
+           "steps": e2e_steps, "image_mean": [round(float(x), 5) for x in img.mean(axis=(0, 1))]}
+    if e2e_steps == 0:
+        e2e = None
+
+    if rank != 0:
+        return None
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_s * 1e3 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "cornell_env_%dx%d_%dspp_maxpl12_rr3_em1024x512_%s" % (WIDTH, HEIGHT, SPP, sampler),
+                   "width": WIDTH, "height": HEIGHT, "spp": SPP, "max_path_length": MAX_PATH,
+                   "rr_min_path_length": RR_FROM, "env_map": [EM_W, EM_H], "em_sampler": sampler,
+                   "pipeline": args.pipeline, "paths_per_step": paths_per_step,
+                   "l2": "flushed between steps (256 MiB memset outside the timed events)",
+                   "parallelism": "replicas over sample ranges" if world > 1 else "single GPU"},
+        "e2e": e2e, "roofline": roofline, "gpu_launches": gpu_launches,
+        "step_ms": [round(x, 3) for x in step_ms],
+    }
+    line["clocks"] = clk.summary()
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(scene, sampler, iters=args.cpu_iters)
+    return line
+
+
+def steerable_available():
+    try:
+        from pg3render_gb300 import _lib
+        return bool(getattr(_lib.load(), "pg3gpu_steerable_available", lambda: 0)())
+    except Exception:
+        return False
+
+
+# ----------------------------------------------------------------------------- reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    scene = build_scene()
+    sampler = args.sampler if args.sampler != "auto" else "steerable"
+    threads = os.cpu_count() or 1
+    for _ in range(max(0, args.warmup)):
+        cpu_baseline(scene, sampler, threads=threads)
+    vals, secs = [], []
+    last = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        last = cpu_baseline(scene, sampler, threads=threads)
+        secs.append(time.perf_counter() - t0)
+        vals.append(last["value"])
+    value = statistics.mean(vals)
+    cb = dict(last)
+    cb["value"] = round(value, 4)
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.mean(secs), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "cornell_env_%dx%d_%dspp_maxpl12_rr3_em1024x512_%s" % (WIDTH, HEIGHT, SPP, sampler),
+                       "width": WIDTH, "height": HEIGHT, "em_sampler": sampler,
+                       "step": "bounded sample: one iteration per host thread"},
+            "cpu_baseline": cb,
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        if world > 1:
+            import torch
+            torch.cuda.set_device(local_rank)
+            torch.distributed.init_process_group("nccl")
+        line = run_gpu(args, rank, world, local_rank)
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -137,6 +137,10 @@ typedef struct pg3gpu_stats {
     uint64_t terminated_by_max_limit;
     uint64_t terminated_by_safety_limit;
     double last_iteration_ms;        /* device time of the last pg3gpu_run_iteration */
+    double path_kernel_ms;           /* summed device time of path-kernel launches since reset
+                                        (CUDA events on the context's stream) */
+    uint64_t path_kernel_launches;   /* path-kernel launches since reset */
+    uint64_t kernel_launches;        /* all kernel launches of this library since reset */
 } pg3gpu_stats;
 
 typedef struct pg3gpu_ctx pg3gpu_ctx;

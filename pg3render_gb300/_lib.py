@@ -70,7 +70,8 @@ class Stats(ctypes.Structure):
                 ("shadow_rays", ctypes.c_uint64), ("terminated_by_russian_roulette", ctypes.c_uint64),
                 ("terminated_by_background", ctypes.c_uint64), ("terminated_by_blocker", ctypes.c_uint64),
                 ("terminated_by_max_limit", ctypes.c_uint64), ("terminated_by_safety_limit", ctypes.c_uint64),
-                ("last_iteration_ms", ctypes.c_double)]
+                ("last_iteration_ms", ctypes.c_double), ("path_kernel_ms", ctypes.c_double),
+                ("path_kernel_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
 
 
 # every exported symbol, with its ctypes signature (checked against include/pg3gpu.h by the tests)

@@ -37,6 +37,13 @@ struct pg3gpu_ctx {
     bool useWavefront = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
+    // per-launch timing of the path kernel: event pairs recorded around each launch,
+    // folded into kernelMs when the stream is synchronised
+    static constexpr int kTimerSlots = 64;
+    cudaEvent_t tStart[kTimerSlots] = {}, tStop[kTimerSlots] = {};
+    int pendingTimers = 0;
+    double kernelMs = 0.0;
+    uint64_t kernelLaunches = 0, allLaunches = 0;
     std::string lastError;
 };
 
@@ -111,12 +118,28 @@ uint32_t passesPerChunk(const pg3gpu_ctx *ctx, uint32_t spp)
     return (uint32_t)std::min<uint64_t>(k, spp);
 }
 
+// Adds the elapsed times of all recorded path-kernel launches (stream must be idle).
+void foldTimers(pg3gpu_ctx *ctx)
+{
+    for (int i = 0; i < ctx->pendingTimers; ++i) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ctx->tStart[i], ctx->tStop[i]) == cudaSuccess) ctx->kernelMs += ms;
+    }
+    ctx->pendingTimers = 0;
+}
+
 int renderChunk(pg3gpu_ctx *ctx, bool naive, uint32_t sample0, uint32_t passes)
 {
     const uint32_t npix = ctx->W * ctx->H;
     const uint64_t paths = (uint64_t)passes * npix;
     int st = ensureOutput(ctx, paths);
     if (st) return st;
+    if (ctx->pendingTimers == pg3gpu_ctx::kTimerSlots) {
+        cudaStreamSynchronize(ctx->stream);
+        foldTimers(ctx);
+    }
+    const int slot = ctx->pendingTimers++;
+    cudaEventRecord(ctx->tStart[slot], ctx->stream);
     cudaError_t e;
     if (ctx->useWavefront)
         e = launchWavefront(ctx->view, naive, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
@@ -125,6 +148,9 @@ int renderChunk(pg3gpu_ctx *ctx, bool naive, uint32_t sample0, uint32_t passes)
         e = launchMegakernel(ctx->view, naive, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
                              ctx->dStats, ctx->megaGrid, ctx->stream);
     if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "path kernel launch: %s", cudaGetErrorString(e));
+    cudaEventRecord(ctx->tStop[slot], ctx->stream);
+    ctx->kernelLaunches += 1;
+    ctx->allLaunches += ctx->useWavefront ? 0 : 1;
     return PG3GPU_OK;
 }
 
@@ -174,6 +200,10 @@ int pg3gpu_destroy(pg3gpu_ctx *ctx)
     for (void *p : ctx->allocs) cudaFree(p);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (int i = 0; i < pg3gpu_ctx::kTimerSlots; ++i) {
+        if (ctx->tStart[i]) cudaEventDestroy(ctx->tStart[i]);
+        if (ctx->tStop[i]) cudaEventDestroy(ctx->tStop[i]);
+    }
     delete ctx;
     return PG3GPU_OK;
 }
@@ -262,6 +292,9 @@ int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int dev
     }
     if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
         return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));
+    for (int i = 0; i < pg3gpu_ctx::kTimerSlots; ++i)
+        if (cudaEventCreate(&ctx->tStart[i]) != cudaSuccess || cudaEventCreate(&ctx->tStop[i]) != cudaSuccess)
+            return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));
     if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "setup sync"));
     *out = ctx;
     return PG3GPU_OK;
@@ -292,6 +325,7 @@ int pg3gpu_run_iteration(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration,
         cudaError_t e = launchAccumulate(npix, passes, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2], ctx->dSum,
                                          ctx->dSumsq, ctx->stream);
         if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "accumulate: %s", cudaGetErrorString(e));
+        ctx->allLaunches += 1;
     }
     PG3_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->timed = true;
@@ -304,6 +338,7 @@ int pg3gpu_synchronize(pg3gpu_ctx *ctx)
     if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     PG3_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    foldTimers(ctx);
     unsigned int flag = 0;
     PG3_CUDA(ctx, cudaMemcpy(&flag, ctx->dErr, sizeof flag, cudaMemcpyDeviceToHost));
     if (flag) return fail(ctx, PG3GPU_ERR_DEVICE_LIMIT, "kernel limit flag 0x%x (1: BVH stack, 2: queue, 4: steerable descent)", flag);
@@ -387,6 +422,9 @@ int pg3gpu_get_stats(pg3gpu_ctx *ctx, pg3gpu_stats *out)
     float ms = 0.f;
     if (ctx->timed && cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) out->last_iteration_ms = ms;
     else out->last_iteration_ms = 0.0;
+    out->path_kernel_ms = ctx->kernelMs;
+    out->path_kernel_launches = ctx->kernelLaunches;
+    out->kernel_launches = ctx->allLaunches;
     return PG3GPU_OK;
 }
 
@@ -395,6 +433,11 @@ int pg3gpu_reset_stats(pg3gpu_ctx *ctx)
     if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     PG3_CUDA(ctx, cudaMemsetAsync(ctx->dStats, 0, sizeof(DevStats), ctx->stream));
+    PG3_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    foldTimers(ctx);
+    ctx->kernelMs = 0.0;
+    ctx->kernelLaunches = 0;
+    ctx->allLaunches = 0;
     return PG3GPU_OK;
 }
 
