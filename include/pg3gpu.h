@@ -195,6 +195,28 @@ int pg3gpu_reset_stats(pg3gpu_ctx *ctx);
  * results on the GPU. */
 int pg3gpu_device_framebuffer(pg3gpu_ctx *ctx, const double **sum_rgb, const double **sumsq_rgb);
 
+/* Allocation-free rendering. No counterpart in the reference.
+ * For callers that may not allocate device memory once they are running: a frame
+ * loop captured into a CUDA graph (cudaMalloc cannot be captured), or an engine whose
+ * device memory belongs to its own allocator after start-up. Renders samples
+ * `iteration` .. iteration+spp-1 of the context's scene exactly like
+ * pg3gpu_run_iteration, but adds them to the caller's device arrays sum_rgb and
+ * sumsq_rgb (width*height*3 doubles each; sum and sum of squares; never cleared by
+ * this call) instead of the context's framebuffer. The per-sample radiance lives in
+ * a scratch area compiled into the library: PG3GPU_NOALLOC_MAX_PATHS paths (12 MiB),
+ * held by every GPU that loads the library until the process exits. The call
+ * allocates nothing (no cudaMalloc, cudaFree or allocating library routine); images
+ * of more than PG3GPU_NOALLOC_MAX_PATHS pixels are rejected with
+ * PG3GPU_ERR_INVALID_ARGUMENT. The first call on a device looks up the scratch
+ * area's device address: make that first call before any stream capture. All calls
+ * share the one scratch area and it keeps the last call's contents (nothing in it
+ * needs to start at zero): calls that overlap on the GPU -- on other streams or from
+ * other host threads -- race, so the caller must serialise them. Asynchronous, on
+ * the context's stream, like pg3gpu_run_iteration. */
+#define PG3GPU_NOALLOC_MAX_PATHS (1u << 20)
+int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp,
+                                 double *sum_rgb, double *sumsq_rgb);
+
 /* Text of the last error of this context (or of the last failed create when ctx is NULL). */
 const char *pg3gpu_last_error(const pg3gpu_ctx *ctx);
 const char *pg3gpu_status_string(int status);

@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -450,3 +451,74 @@ int pg3gpu_device_framebuffer(pg3gpu_ctx *ctx, const double **sum, const double 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// Rendering without device allocations (no counterpart in the reference).
+//
+// For callers that may not allocate device memory once they are running -- a frame loop
+// captured into a CUDA graph (cudaMalloc cannot be captured), or an engine whose device
+// memory belongs to its own allocator after start-up. The per-sample radiance of a launch
+// chunk lives in this file-scope array instead of a cudaMalloc'd buffer; every GPU that
+// loads the library holds it (12 MiB) until the process exits.
+// ------------------------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t kNoAllocMaxPaths = PG3GPU_NOALLOC_MAX_PATHS;
+static __device__ __align__(256) float g_noallocRadiance[3 * (size_t)kNoAllocMaxPaths];
+
+constexpr int kNoAllocMaxDevices = 64;
+float *g_noallocAddress[kNoAllocMaxDevices] = {};
+std::mutex g_noallocMutex;
+
+// Device address of the scratch array on ctx's device. In host code the array's name is a
+// host-side stand-in, not a device address, so it is looked up once per device with that
+// device current (the caller has made it current).
+int noallocScratch(pg3gpu_ctx *ctx, float **out)
+{
+    if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
+        return fail(ctx, PG3GPU_ERR_UNSUPPORTED, "device %d: no scratch slot", ctx->device);
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocAddress[ctx->device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocRadiance);
+        if (e != cudaSuccess || !p)
+            return fail(ctx, PG3GPU_ERR_CUDA, "cudaGetSymbolAddress of the scratch area: %s", cudaGetErrorString(e));
+        g_noallocAddress[ctx->device] = static_cast<float *>(p);
+    }
+    *out = g_noallocAddress[ctx->device];
+    return PG3GPU_OK;
+}
+
+}  // namespace
+
+extern "C" int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp,
+                                            double *sum_rgb, double *sumsq_rgb)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    if (!sum_rgb || !sumsq_rgb) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "sum_rgb and sumsq_rgb are required");
+    if (algorithm != PG3GPU_ALG_PATH_TRACING && algorithm != PG3GPU_ALG_PATH_TRACING_NAIVE)
+        return fail(ctx, PG3GPU_ERR_UNSUPPORTED, "algorithm %d is not a path tracer", (int)algorithm);
+    const uint32_t npix = ctx->W * ctx->H;
+    if (npix > kNoAllocMaxPaths)
+        return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT,
+                    "image of %u pixels exceeds the %u-path scratch area of pg3gpu_run_iteration_noalloc", npix,
+                    kNoAllocMaxPaths);
+    if (spp == 0) return PG3GPU_OK;
+    PG3_CUDA(ctx, cudaSetDevice(ctx->device));
+    float *scratch = nullptr;
+    int st = noallocScratch(ctx, &scratch);
+    if (st) return st;
+    // Every scratch element the accumulation reads is written by the path kernel of the same
+    // chunk first, so nothing in the (shared, persistent) scratch has to start at zero.
+    float *r = scratch, *g = scratch + kNoAllocMaxPaths, *b = scratch + 2 * (size_t)kNoAllocMaxPaths;
+    const bool naive = algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE;
+    const uint32_t per = std::min(spp, kNoAllocMaxPaths / npix);
+    for (uint32_t done = 0; done < spp; done += per) {
+        const uint32_t passes = std::min(per, spp - done);
+        cudaError_t e = launchMegakernel(ctx->view, naive, iteration + done, (uint64_t)passes * npix, npix, r, g, b,
+                                         ctx->dStats, ctx->megaGrid, ctx->stream);
+        if (e == cudaSuccess) e = launchAccumulate(npix, passes, r, g, b, sum_rgb, sumsq_rgb, ctx->stream);
+        if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "allocation-free launch: %s", cudaGetErrorString(e));
+    }
+    return PG3GPU_OK;
+}
