@@ -142,16 +142,18 @@ int renderChunk(pg3gpu_ctx *ctx, bool naive, uint32_t sample0, uint32_t passes)
     const int slot = ctx->pendingTimers++;
     cudaEventRecord(ctx->tStart[slot], ctx->stream);
     cudaError_t e;
-    if (ctx->useWavefront)
+    uint64_t launches = 1;
+    if (ctx->useWavefront && !naive) {   // the BSDF-only tracer always runs as a megakernel
+        launches = 0;
         e = launchWavefront(ctx->view, naive, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
-                            ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->stream);
-    else
+                            ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->stream, &launches);
+    } else
         e = launchMegakernel(ctx->view, naive, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
                              ctx->dStats, ctx->megaGrid, ctx->stream);
     if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "path kernel launch: %s", cudaGetErrorString(e));
     cudaEventRecord(ctx->tStop[slot], ctx->stream);
     ctx->kernelLaunches += 1;
-    ctx->allLaunches += ctx->useWavefront ? 0 : 1;
+    ctx->allLaunches += launches;
     return PG3GPU_OK;
 }
 
@@ -283,13 +285,16 @@ int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int dev
     if (megakernelOccupancy(opts->algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE, &perSm) != cudaSuccess || perSm < 1)
         perSm = 1;
     ctx->megaGrid = sms * perSm;
-    ctx->useWavefront = (opts->pipeline == PG3GPU_PIPELINE_WAVEFRONT);
+    // the wavefront pipeline is the default for the NEE path tracer (3x the megakernel on the
+    // benchmark scenes); the BSDF-only tracer always runs as a megakernel
+    ctx->useWavefront = (opts->pipeline == PG3GPU_PIPELINE_WAVEFRONT || opts->pipeline == PG3GPU_PIPELINE_AUTO);
     if (ctx->useWavefront) {
-        ctx->waveCapacity = 1ull << 20;
+        const uint64_t npix = (uint64_t)ctx->W * ctx->H;
+        ctx->waveCapacity = std::min<uint64_t>(1ull << 22, std::max<uint64_t>(1ull << 16, npix * 16));
         void *w;
         if ((st = devAlloc(ctx, (char **)&w, wavefrontBytes(ctx->waveCapacity)))) return bail(st);
         ctx->dWave = w;
-        ctx->waveGrid = sms * 8;
+        ctx->waveGrid = sms * 4;
     }
     if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
         return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));

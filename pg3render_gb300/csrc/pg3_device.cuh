@@ -344,16 +344,17 @@ PG3_DI float dielPdf(const DevMaterial &mt, const DielCtx &c)
     return vn * J * (c.refl ? c.F : (1.f - c.F));
 }
 
-// EvalBsdf + GetOptData(kOptSamplingProbs): :277-283 (Lambert), :809-817 (conductor),
-// :1023-1031 with InitEvalContext :1123-1160 (dielectric)
-PG3_DI void evalBsdf(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
+// EvalBsdf + GetOptData(kOptSamplingProbs) per material kind: :277-283 (Lambert),
+// :809-817 (conductor), :1023-1031 with InitEvalContext :1123-1160 (dielectric)
+template <int K>
+PG3_DI void evalBsdfK(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
 {
     r.wil = wil;
     r.compProb = 1.f;
-    if (m.kind == kMatLambert) {
+    if (K == kMatLambert) {
         r.att = (wil.z <= 0.f || wol.z <= 0.f) ? f3(0.f) : make_float3(m.r, m.g, m.b) * kPiInvF;
         r.pdfW = cosHemispherePdf(wil.z);
-    } else if (m.kind == kMatGgxConductor) {
+    } else if (K == kMatGgxConductor) {
         const float3 h = halfwayReflection(wil, wol);
         const float D = ggxD(h, m.alpha);
         const float F = fresnelConductor(dot(h, wol), m.eta, m.absorb);
@@ -375,15 +376,22 @@ PG3_DI void evalBsdf(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
         r.pdfW = dielPdf(m, c);
     }
 }
+PG3_DI void evalBsdf(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
+{
+    if (m.kind == kMatLambert) evalBsdfK<kMatLambert>(m, wil, wol, r);
+    else if (m.kind == kMatGgxConductor) evalBsdfK<kMatGgxConductor>(m, wil, wol, r);
+    else evalBsdfK<kMatGgxDielectric>(m, wil, wol, r);
+}
 
-// SampleBsdf: :285-292 (Lambert), :819-851 (conductor), :1033-1100 (dielectric)
-PG3_DI void sampleBsdf(const DevMaterial &m, float3 wol, float u0, float u1, float u2, BsdfRec &r)
+// SampleBsdf per material kind: :285-292 (Lambert), :819-851 (conductor), :1033-1100 (dielectric)
+template <int K>
+PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, float u2, BsdfRec &r)
 {
     r.compProb = 1.f;
-    if (m.kind == kMatLambert) {
+    if (K == kMatLambert) {
         r.wil = sampleCosHemisphere(u0, u1, r.pdfW);
         r.att = (r.wil.z <= 0.f || wol.z <= 0.f) ? f3(0.f) : make_float3(m.r, m.g, m.b) * kPiInvF;
-    } else if (m.kind == kMatGgxConductor) {
+    } else if (K == kMatGgxConductor) {
         const float3 h = sampleGgxVisibleNormals(wol, m.alpha, u0, u1);
         const float D = ggxD(h, m.alpha);
         bool above;
@@ -416,6 +424,12 @@ PG3_DI void sampleBsdf(const DevMaterial &m, float3 wol, float u0, float u1, flo
         r.pdfW = dielPdf(m, c);
         r.att = (!above || cosAbs < 0.0f) ? f3(0.f) : dielEval(m, c);
     }
+}
+PG3_DI void sampleBsdf(const DevMaterial &m, float3 wol, float u0, float u1, float u2, BsdfRec &r)
+{
+    if (m.kind == kMatLambert) sampleBsdfK<kMatLambert>(m, wol, u0, u1, u2, r);
+    else if (m.kind == kMatGgxConductor) sampleBsdfK<kMatGgxConductor>(m, wol, u0, u1, u2, r);
+    else sampleBsdfK<kMatGgxDielectric>(m, wol, u0, u1, u2, r);
 }
 
 // ------------------------------------------------------------------------------------------

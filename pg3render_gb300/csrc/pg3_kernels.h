@@ -25,10 +25,9 @@ cudaError_t buildLbvh(const SceneView &S, BvhNode *nodes, void *scratch, uint32_
                       uint32_t *sortedIdsOut, cudaStream_t stream);
 
 // pg3_wavefront.cu
-struct WavefrontBuffers;
 size_t wavefrontBytes(uint64_t capacity);
 cudaError_t launchWavefront(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch,
-                            uint64_t capacity, int gridBlocks, cudaStream_t stream);
+                            uint64_t capacity, int gridBlocks, cudaStream_t stream, uint64_t *launches);
 
 }  // namespace pg3

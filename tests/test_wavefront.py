@@ -1,0 +1,68 @@
+"""Wavefront pipeline parity (GPU tests): the stage kernels draw the same Philox
+numbers as the megakernel, so the two pipelines agree sample by sample up to
+float rounding; the wavefront also matches the oracle path by path and the
+reference's golden images statistically."""
+import numpy as np
+import pytest
+
+import pg3render_gb300 as P
+from pg3render_gb300 import scene as S
+
+from _util import load_golden, scene_from_golden, z_ok, zscores
+
+pytestmark = pytest.mark.gpu
+
+R = P.renderer
+
+
+def _samples(scene, maxpl, pipeline, sampler=R.EM_CDF, spp=8, seed=31, rr=0, cap=0):
+    cfg = P.Config(scene=scene, max_path_length=maxpl, em_sampler=sampler, pipeline=pipeline,
+                   rr_min_path_length=rr, max_paths_in_flight=cap)
+    with P.GpuPathTracer(cfg, seed=seed) as r:
+        out = r.render_samples(R.kPathTracing, 0, spp)
+        st = r.stats()
+    return out, st
+
+
+def _match(a, b, tol=1e-3):
+    return float(np.mean(np.abs(a - b) <= tol * np.maximum(1.0, np.abs(b))))
+
+
+@pytest.mark.parametrize("case", ["area", "area_rr", "env_cdf", "env_cos", "env_rr3"])
+def test_wavefront_matches_megakernel(case):
+    if case.startswith("area"):
+        scene, maxpl, sampler = S.cornell_box(32, 32), (0 if case == "area_rr" else 8), R.EM_CDF
+        rr = 0
+    else:
+        scene, maxpl = S.cornell_env(32, 32, 64, 32), 12
+        sampler = R.EM_COSINE if case == "env_cos" else R.EM_CDF
+        rr = 4 if case == "env_rr3" else 0
+    a, sa = _samples(scene, maxpl, R.PIPELINE_MEGAKERNEL, sampler, rr=rr)
+    b, sb = _samples(scene, maxpl, R.PIPELINE_WAVEFRONT, sampler, rr=rr)
+    frac = _match(b, a)
+    assert frac >= 0.995, "wavefront/megakernel sample match %.4f" % frac
+    assert sa["paths"] == sb["paths"]
+    # identical random decisions -> (nearly) identical ray counts
+    assert abs(sa["extension_rays"] - sb["extension_rays"]) <= 1e-3 * sa["extension_rays"]
+    assert abs(sa["shadow_rays"] - sb["shadow_rays"]) <= 1e-3 * sa["shadow_rays"]
+
+
+def test_wavefront_small_capacity_chunks():
+    # more paths than one wavefront chunk holds: chunks must not interfere
+    scene = S.cornell_box(16, 16)
+    a, _ = _samples(scene, 8, R.PIPELINE_WAVEFRONT, spp=6)
+    b, _ = _samples(scene, 8, R.PIPELINE_MEGAKERNEL, spp=6)
+    assert _match(a, b) >= 0.995
+
+
+@pytest.mark.parametrize("name", ["cornell_area_32", "cornell_env_32_cdf"])
+def test_wavefront_against_reference_golden(name):
+    d, text, td = load_golden(name)
+    scene = scene_from_golden(d)
+    cfg = P.Config(scene=scene, max_path_length=int(d["max_path_length"]), pipeline=R.PIPELINE_WAVEFRONT)
+    spp = 16384
+    with P.GpuPathTracer(cfg, seed=77) as r:
+        r.RunIteration(R.kPathTracing, 0, spp)
+        mean, var, n = r.framebuffer(with_variance=True)
+    frac, zm, zs = z_ok(zscores(mean, var / spp, d["mean"], d["var_mean"]))
+    assert frac >= 0.999 and abs(zm) < 0.25 and 0.7 < zs < 1.3, (frac, zm, zs)
