@@ -185,7 +185,7 @@ def run_gpu(args, rank, world, local_rank):
     scene = build_scene()
     sampler = args.sampler
     if sampler == "auto":
-        sampler = "steerable" if steerable_available() else "cdf"
+        sampler = "steerable"   # the workload's light sampler (icosahedron subdivided to 1280 triangles)
     em_sampler = {"steerable": R.EM_STEERABLE, "cdf": R.EM_CDF, "cosine": R.EM_COSINE}[sampler]
     pipeline = {"auto": R.PIPELINE_AUTO, "megakernel": R.PIPELINE_MEGAKERNEL,
                 "wavefront": R.PIPELINE_WAVEFRONT}[args.pipeline]
@@ -233,7 +233,7 @@ def run_gpu(args, rank, world, local_rank):
     traffic = (NCU_TRAFFIC_PER_PATH * st["paths"] / launches) if NCU_TRAFFIC_PER_PATH else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "megakernel" if args.pipeline != "wavefront" else "wavefront",
+                "kernel": "megakernel" if args.pipeline == "megakernel" else "wavefront (all stage kernels of a chunk)",
                 "launch_ms": round(launch_ms, 4), "algorithmic_bytes_per_launch": int(alg_bytes),
                 "segments_per_path": round(st["extension_rays"] / max(1, st["paths"]), 4),
                 "shadow_rays_per_path": round(st["shadow_rays"] / max(1, st["paths"]), 4)}
@@ -285,14 +285,6 @@ def run_gpu(args, rank, world, local_rank):
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(scene, sampler, iters=args.cpu_iters)
     return line
-
-
-def steerable_available():
-    try:
-        from pg3render_gb300 import _lib
-        return bool(getattr(_lib.load(), "pg3gpu_steerable_available", lambda: 0)())
-    except Exception:
-        return False
 
 
 # ----------------------------------------------------------------------------- reference arm

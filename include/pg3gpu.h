@@ -122,8 +122,13 @@ typedef struct pg3gpu_options {
     uint32_t steer_subdiv_level;     /* steerable sampler: icosahedron subdivision level (3 -> 1280 triangles) */
     uint64_t seed;                   /* mBaseSeed: keys every random stream */
     uint32_t max_paths_in_flight;    /* 0 = automatic; upper bound on paths per launch chunk */
-    uint32_t reserved[5];
+    int32_t ggx_sampler;             /* PG3GPU_GGX_*: visible-normal sampling of the GGX materials */
+    uint32_t reserved[4];
 } pg3gpu_options;
+
+/* GGX visible-normal sampling: exact (Heitz 2018, default) or the reference's routine with its
+ * rational fit of the slope CDF (src/microfacet.hxx:610-729), which is approximate in its tails. */
+enum { PG3GPU_GGX_VNDF_EXACT = 0, PG3GPU_GGX_VNDF_REFERENCE_FIT = 1 };
 
 /* Path statistics: counts of the reference's PathTerminationReason
  * (src/renderer.hxx:11-28) plus traced-ray totals. */
@@ -194,6 +199,25 @@ int pg3gpu_reset_stats(pg3gpu_ctx *ctx);
  * each: sum and sum of squares), valid until destroy; for callers that keep
  * results on the GPU. */
 int pg3gpu_device_framebuffer(pg3gpu_ctx *ctx, const double **sum_rgb, const double **sumsq_rgb);
+
+/* Sampler probes (test entry points, no counterpart in the reference): run one
+ * sampler of the path kernels n times, one sample per thread, on host arrays.
+ * pg3gpu_probe_bsdf samples material `material` for outgoing local directions wol
+ * (n x 3) and returns the incoming directions, the sampled pdf (pdfW * compProb),
+ * the pdf the evaluation path gives for the same pair, and both attenuations
+ * (src/materials.hxx SampleBsdf / EvalBsdf). pg3gpu_probe_light samples light
+ * `light` (area light id, or the background's id = number of area lights) from
+ * surface points/normals as next-event estimation does and returns direction,
+ * sampled pdf, evaluated pdf (the emitter-hit MIS path) and radiance * cos.
+ * The *_pdf variants evaluate the pdf of given directions only. */
+int pg3gpu_probe_bsdf(pg3gpu_ctx *ctx, int32_t material, uint32_t n, const float *wol, uint32_t seed, float *wil,
+                      float *pdf_sampled, float *pdf_eval, float *att_sampled, float *att_eval);
+int pg3gpu_probe_bsdf_pdf(pg3gpu_ctx *ctx, int32_t material, uint32_t n, const float *wol, const float *wil,
+                          float *pdf, float *att_max);   /* att_max (may be NULL): max channel of the BSDF value */
+int pg3gpu_probe_light(pg3gpu_ctx *ctx, int32_t light, uint32_t n, const float *points, const float *normals,
+                       uint32_t seed, float *dirs, float *pdf_sampled, float *pdf_eval, float *radiance_cos);
+int pg3gpu_probe_light_pdf(pg3gpu_ctx *ctx, int32_t light, uint32_t n, const float *points, const float *normals,
+                           const float *dirs, float *pdf);
 
 /* Allocation-free rendering. No counterpart in the reference.
  * For callers that may not allocate device memory once they are running: a frame

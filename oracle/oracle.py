@@ -48,8 +48,10 @@ def _ptr(a):
 
 
 def render(scene_text, width, height, seed=1234, sample0=0, spp=1, em_sampler=EM_CDF,
-           rr_min_path_length=0, threads=0, per_sample=False):
-    """Returns dict(sum=[H,W,3] f64, sumsq=[H,W,3] f64, samples=[spp,H,W,3] f32 or None)."""
+           rr_min_path_length=0, threads=0, per_sample=False, ggx_exact=True):
+    """Returns dict(sum=[H,W,3] f64, sumsq=[H,W,3] f64, samples=[spp,H,W,3] f32 or None).
+    ggx_exact selects the exact visible-normal sampler (False: the reference's fitted routine)."""
+    lib().pg3o_set_ggx_exact(1 if ggx_exact else 0)
     npix = width * height
     s = np.zeros((npix, 3), np.float64)
     s2 = np.zeros((npix, 3), np.float64)

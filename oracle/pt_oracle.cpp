@@ -368,6 +368,28 @@ static V3 SampleGgxVisibleNormals(V3 wo, float a, float u0, float u1)
     const float inv = 1.0f / Len(V3(x, y, 1.0f));
     return V3(-x * inv, -y * inv, inv);
 }
+// Exact visible-normal sampling, Heitz, "Sampling the GGX Distribution of Visible Normals"
+// (JCGT 2018): same density as SampleGgxVisibleNormals above, without its rational fit.
+static V3 SampleGgxVndfExact(V3 wo, float a, float u0, float u1)
+{
+    const V3 vh = Normalize(V3(a * wo.x, a * wo.y, std::max(wo.z, 0.0f)));
+    const float lensq = vh.x * vh.x + vh.y * vh.y;
+    const V3 t1 = lensq > 0.f ? V3(-vh.y, vh.x, 0.f) / std::sqrt(lensq) : V3(1.f, 0.f, 0.f);
+    const V3 t2 = Cross(vh, t1);
+    const float r = std::sqrt(u0);
+    const float phi = 2.f * kPiF * u1;
+    const float p1 = r * std::cos(phi);
+    const float s = 0.5f * (1.f + vh.z);
+    const float p2 = (1.f - s) * std::sqrt(std::max(0.f, 1.f - p1 * p1)) + s * (r * std::sin(phi));
+    const V3 nh = t1 * p1 + t2 * p2 + vh * std::sqrt(std::max(0.f, 1.f - p1 * p1 - p2 * p2));
+    return Normalize(V3(a * nh.x, a * nh.y, std::max(1e-6f, nh.z)));
+}
+static bool g_vndfExact = true;   // false: the reference's fitted routine
+static V3 SampleVndf(V3 wo, float a, float u0, float u1)
+{
+    return g_vndfExact ? SampleGgxVndfExact(wo, a, u0, u1) : SampleGgxVisibleNormals(wo, a, u0, u1);
+}
+
 // src/microfacet.hxx:732-756
 static inline float GgxPdfVisibleNormals(V3 wo, V3 h, float D, float a)
 {
@@ -518,7 +540,7 @@ struct Material {
         } else if (kind == kGgxConductor) {
             CondCtx c;
             c.wol = r.wol;
-            c.m = SampleGgxVisibleNormals(c.wol, alpha, u[0], u[1]);
+            c.m = SampleVndf(c.wol, alpha, u[0], u[1]);
             c.D = DistributionGgx(c.m, alpha);
             bool above;
             c.wil = Reflect(above, c.wol, c.m);
@@ -535,7 +557,7 @@ struct Material {
             c.wo = r.wol * s;
             c.etaS = c.below ? etaInv : eta;
             c.etaInvS = c.below ? eta : etaInv;
-            c.m = SampleGgxVisibleNormals(c.wo, alpha, u[0], u[1]);
+            c.m = SampleVndf(c.wo, alpha, u[0], u[1]);
             c.D = DistributionGgx(c.m, alpha);
             c.F = FresnelDielectric(Dot(c.m, c.wo), c.etaS);
             bool above;
@@ -1232,6 +1254,9 @@ int pg3o_render(const char *scene_text, uint64_t seed, uint32_t sample0, uint32_
 }
 
 // Philox4x32-10 block for the known-answer test.
+// GGX visible-normal sampling for all later calls: 1 exact (default), 0 the reference's fit.
+void pg3o_set_ggx_exact(int exact) { pg3o::g_vndfExact = exact != 0; }
+
 void pg3o_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
 {
     uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
@@ -1264,3 +1289,57 @@ int pg3o_em_cdf(const char *em_path, float *marg, float *cond)
 }
 
 }  // extern "C"
+
+extern "C" {
+// BSDF sampler probe: material (kind 0/1/2 with alpha, eta=n/n_out, k), n samples for one wol;
+// u[3n] uniforms; outputs wil[3n], pdf_sampled[n], pdf_eval[n], att_sampled[n] (grey), att_eval[n].
+void pg3o_probe_bsdf(int kind, float alpha, float n_in, float n_out, float k, const float *wol, int n,
+                     const float *u, float *wil, float *pdfS, float *pdfE, float *attS, float *attE)
+{
+    using namespace pg3o;
+    Material m = kind == kLambert ? Material::Lambert(V3(0.5f))
+               : kind == kGgxConductor ? Material::Conductor(alpha, n_in, n_out, k)
+                                       : Material::Dielectric(alpha, n_in, n_out);
+    const V3 wo(wol[0], wol[1], wol[2]);
+    for (int i = 0; i < n; ++i) {
+        MatRecord s;
+        s.wol = wo;
+        m.Sample(u + 3 * i, s);
+        MatRecord e;
+        e.wil = s.wil;
+        e.wol = wo;
+        m.Eval(e);
+        wil[3 * i] = s.wil.x; wil[3 * i + 1] = s.wil.y; wil[3 * i + 2] = s.wil.z;
+        pdfS[i] = s.pdfW * s.compProb;
+        pdfE[i] = e.pdfW * e.compProb;
+        attS[i] = s.attenuation.x;
+        attE[i] = e.attenuation.x;
+    }
+}
+void pg3o_bsdf_pdf(int kind, float alpha, float n_in, float n_out, float k, const float *wol, int n,
+                   const float *wil, float *pdf, float *att)
+{
+    using namespace pg3o;
+    Material m = kind == kLambert ? Material::Lambert(V3(0.5f))
+               : kind == kGgxConductor ? Material::Conductor(alpha, n_in, n_out, k)
+                                       : Material::Dielectric(alpha, n_in, n_out);
+    for (int i = 0; i < n; ++i) {
+        MatRecord e;
+        e.wil = V3(wil[3 * i], wil[3 * i + 1], wil[3 * i + 2]);
+        e.wol = V3(wol[0], wol[1], wol[2]);
+        m.Eval(e);
+        pdf[i] = e.pdfW * e.compProb;
+        if (att) att[i] = e.attenuation.x;
+    }
+}
+}
+
+extern "C" void pg3o_probe_vndf(const float *wol, float alpha, int n, const float *u, float *m)
+{
+    using namespace pg3o;
+    const V3 wo(wol[0], wol[1], wol[2]);
+    for (int i = 0; i < n; ++i) {
+        const V3 h = SampleGgxVisibleNormals(wo, alpha, u[2 * i], u[2 * i + 1]);
+        m[3 * i] = h.x; m[3 * i + 1] = h.y; m[3 * i + 2] = h.z;
+    }
+}

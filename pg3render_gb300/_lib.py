@@ -19,6 +19,7 @@ BG_NONE, BG_CONSTANT, BG_ENVMAP = 0, 1, 2
 EM_CDF, EM_COSINE, EM_STEERABLE = 0, 1, 2
 TRAVERSAL_AUTO, TRAVERSAL_LIST, TRAVERSAL_BVH = 0, 1, 2
 PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT = 0, 1, 2
+GGX_VNDF_EXACT, GGX_VNDF_REFERENCE_FIT = 0, 1
 
 c_float3 = ctypes.c_float * 3
 
@@ -62,7 +63,8 @@ class Options(ctypes.Structure):
                 ("indirect_clipping", ctypes.c_float), ("splitting_budget", ctypes.c_uint32),
                 ("em_sampler", ctypes.c_int32), ("traversal", ctypes.c_int32), ("pipeline", ctypes.c_int32),
                 ("steer_subdiv_level", ctypes.c_uint32), ("seed", ctypes.c_uint64),
-                ("max_paths_in_flight", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 5)]
+                ("max_paths_in_flight", ctypes.c_uint32), ("ggx_sampler", ctypes.c_int32),
+                ("reserved", ctypes.c_uint32 * 4)]
 
 
 class Stats(ctypes.Structure):
@@ -93,6 +95,12 @@ SIGNATURES = {
     "pg3gpu_reset_stats": (ctypes.c_int, [ctypes.c_void_p]),
     "pg3gpu_device_framebuffer": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
                                                  ctypes.POINTER(ctypes.c_void_p)]),
+    "pg3gpu_probe_bsdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_void_p,
+                                         ctypes.c_uint32] + [ctypes.c_void_p] * 5),
+    "pg3gpu_probe_bsdf_pdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
+    "pg3gpu_probe_light": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
+    "pg3gpu_probe_light_pdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
     "pg3gpu_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "pg3gpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "pg3gpu_version": (ctypes.c_char_p, []),

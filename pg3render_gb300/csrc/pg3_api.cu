@@ -26,6 +26,7 @@ struct pg3gpu_ctx {
     SceneView view{};
     std::vector<void *> allocs;
     uint32_t W = 0, H = 0;
+    uint32_t nmat = 0;
     double *dSum = nullptr, *dSumsq = nullptr;
     float *dOut[3] = {nullptr, nullptr, nullptr};
     uint64_t outCapacity = 0;            // paths per launch chunk
@@ -233,6 +234,7 @@ int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int dev
     ctx->opts = *opts;
     ctx->W = scene->camera.width;
     ctx->H = scene->camera.height;
+    ctx->nmat = scene->num_materials;
     auto bail = [&](int s) {
         g_createError = ctx->lastError;
         pg3gpu_destroy(ctx);
@@ -252,6 +254,17 @@ int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int dev
     if ((st = upload(ctx, (float4 **)&v.em, hs.em))) return bail(st);
     if ((st = upload(ctx, (float **)&v.emMarg, hs.emMarg))) return bail(st);
     if ((st = upload(ctx, (float **)&v.emCond, hs.emCond))) return bail(st);
+    if (hs.hasSteer) {
+        SteerView &sv = v.steer;
+        if ((st = upload(ctx, (float4 **)&sv.vdir, hs.steer.vdir))) return bail(st);
+        if ((st = upload(ctx, (float **)&sv.vw, hs.steer.vw))) return bail(st);
+        if ((st = upload(ctx, (int4 **)&sv.tri, hs.steer.tri))) return bail(st);
+        if ((st = upload(ctx, (float **)&sv.nodeW, hs.steer.nodeW))) return bail(st);
+        if ((st = upload(ctx, (int **)&sv.nodeChild, hs.steer.nodeChild))) return bail(st);
+        sv.level = hs.steer.level;
+        for (size_t l = 0; l < hs.steer.levelOffset.size() && l < 10; ++l) sv.levelOff[l] = hs.steer.levelOffset[l];
+        sv.root = hs.steer.root;
+    }
     if ((st = devAlloc(ctx, &ctx->dErr, 1))) return bail(st);
     if (cudaMemset(ctx->dErr, 0, sizeof(unsigned int)) != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "memset"));
     v.errorFlag = ctx->dErr;
@@ -525,5 +538,113 @@ extern "C" int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, 
         if (e == cudaSuccess) e = launchAccumulate(npix, passes, r, g, b, sum_rgb, sumsq_rgb, ctx->stream);
         if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "allocation-free launch: %s", cudaGetErrorString(e));
     }
+    return PG3GPU_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Sampler probes (test entry points; host arrays in and out, temporary device buffers)
+// ------------------------------------------------------------------------------------------
+namespace {
+
+struct DevTemp {
+    std::vector<void *> ptrs;
+    ~DevTemp() { for (void *p : ptrs) cudaFree(p); }
+    float *in(const float *h, size_t n, cudaError_t &e)
+    {
+        void *p = nullptr;
+        if (e == cudaSuccess) e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(float));
+        if (e == cudaSuccess) { ptrs.push_back(p); if (h) e = cudaMemcpy(p, h, n * sizeof(float), cudaMemcpyHostToDevice); }
+        return (float *)p;
+    }
+};
+
+int probeChecks(pg3gpu_ctx *ctx, uint32_t n)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    if (n == 0 || n > (1u << 26)) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "probe count must be in 1..2^26");
+    cudaSetDevice(ctx->device);
+    return PG3GPU_OK;
+}
+
+}  // namespace
+
+extern "C" int pg3gpu_probe_bsdf(pg3gpu_ctx *ctx, int32_t material, uint32_t n, const float *wol, uint32_t seed,
+                                 float *wil, float *pdf_sampled, float *pdf_eval, float *att_sampled, float *att_eval)
+{
+    int st = probeChecks(ctx, n);
+    if (st) return st;
+    if (material < 0 || (uint32_t)material >= ctx->nmat) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "material id");
+    if (!wol || !wil || !pdf_sampled || !pdf_eval || !att_sampled || !att_eval)
+        return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "NULL probe array");
+    cudaError_t e = cudaSuccess;
+    DevTemp t;
+    float *dWo = t.in(wol, 3 * (size_t)n, e), *dWi = t.in(nullptr, 3 * (size_t)n, e);
+    float *dPs = t.in(nullptr, n, e), *dPe = t.in(nullptr, n, e);
+    float *dAs = t.in(nullptr, 3 * (size_t)n, e), *dAe = t.in(nullptr, 3 * (size_t)n, e);
+    if (e == cudaSuccess) e = launchProbeBsdf(ctx->view, material, n, dWo, seed, dWi, dPs, dPe, dAs, dAe, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(wil, dWi, 12 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(pdf_sampled, dPs, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(pdf_eval, dPe, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(att_sampled, dAs, 12 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(att_eval, dAe, 12 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "bsdf probe: %s", cudaGetErrorString(e));
+    return PG3GPU_OK;
+}
+
+extern "C" int pg3gpu_probe_bsdf_pdf(pg3gpu_ctx *ctx, int32_t material, uint32_t n, const float *wol, const float *wil,
+                                     float *pdf, float *att)
+{
+    int st = probeChecks(ctx, n);
+    if (st) return st;
+    if (material < 0 || (uint32_t)material >= ctx->nmat) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "material id");
+    if (!wol || !wil || !pdf) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "NULL probe array");
+    cudaError_t e = cudaSuccess;
+    DevTemp t;
+    float *dWo = t.in(wol, 3 * (size_t)n, e), *dWi = t.in(wil, 3 * (size_t)n, e), *dP = t.in(nullptr, n, e);
+    float *dA = att ? t.in(nullptr, n, e) : nullptr;
+    if (e == cudaSuccess) e = launchProbeBsdfPdf(ctx->view, material, n, dWo, dWi, dP, dA, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(pdf, dP, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && att) e = cudaMemcpy(att, dA, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "bsdf pdf probe: %s", cudaGetErrorString(e));
+    return PG3GPU_OK;
+}
+
+extern "C" int pg3gpu_probe_light(pg3gpu_ctx *ctx, int32_t light, uint32_t n, const float *points,
+                                  const float *normals, uint32_t seed, float *dirs, float *pdf_sampled,
+                                  float *pdf_eval, float *radiance_cos)
+{
+    int st = probeChecks(ctx, n);
+    if (st) return st;
+    if (light < 0 || (uint32_t)light >= ctx->view.lightCount) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "light id");
+    if (!points || !normals || !dirs || !pdf_sampled || !pdf_eval || !radiance_cos)
+        return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "NULL probe array");
+    cudaError_t e = cudaSuccess;
+    DevTemp t;
+    float *dP = t.in(points, 3 * (size_t)n, e), *dN = t.in(normals, 3 * (size_t)n, e);
+    float *dD = t.in(nullptr, 3 * (size_t)n, e), *dPs = t.in(nullptr, n, e), *dPe = t.in(nullptr, n, e);
+    float *dR = t.in(nullptr, 3 * (size_t)n, e);
+    if (e == cudaSuccess) e = launchProbeLight(ctx->view, light, n, dP, dN, seed, dD, dPs, dPe, dR, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(dirs, dD, 12 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(pdf_sampled, dPs, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(pdf_eval, dPe, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(radiance_cos, dR, 12 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "light probe: %s", cudaGetErrorString(e));
+    return pg3gpu_synchronize(ctx);
+}
+
+extern "C" int pg3gpu_probe_light_pdf(pg3gpu_ctx *ctx, int32_t light, uint32_t n, const float *points,
+                                      const float *normals, const float *dirs, float *pdf)
+{
+    int st = probeChecks(ctx, n);
+    if (st) return st;
+    if (light < 0 || (uint32_t)light >= ctx->view.lightCount) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "light id");
+    if (!points || !normals || !dirs || !pdf) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "NULL probe array");
+    cudaError_t e = cudaSuccess;
+    DevTemp t;
+    float *dP = t.in(points, 3 * (size_t)n, e), *dN = t.in(normals, 3 * (size_t)n, e);
+    float *dD = t.in(dirs, 3 * (size_t)n, e), *dO = t.in(nullptr, n, e);
+    if (e == cudaSuccess) e = launchProbeLightPdf(ctx->view, light, n, dP, dN, dD, dO, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(pdf, dO, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "light pdf probe: %s", cudaGetErrorString(e));
     return PG3GPU_OK;
 }

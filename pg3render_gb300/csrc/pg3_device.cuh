@@ -285,6 +285,29 @@ PG3_DI float3 sampleGgxVisibleNormals(float3 wo, float a, float u0, float u1)   
     const float inv = 1.0f / sqrtf(x * x + y * y + 1.0f);
     return make_float3(-x * inv, -y * inv, inv);
 }
+// Exact visible-normal sampling (Heitz, "Sampling the GGX Distribution of Visible Normals",
+// JCGT 7(4), 2018): the same density D_wo(m) as the routine above, without its rational fit
+// of the slope CDF (whose tails over-produce sideways-tilted normals by up to 2x).
+PG3_DI float3 sampleGgxVndfExact(float3 wo, float a, float u0, float u1)
+{
+    const float3 vh = normalize(make_float3(a * wo.x, a * wo.y, fmaxf(wo.z, 0.0f)));
+    const float lensq = vh.x * vh.x + vh.y * vh.y;
+    const float3 t1 = lensq > 0.f ? make_float3(-vh.y, vh.x, 0.f) * rsqrtf(lensq) : make_float3(1.f, 0.f, 0.f);
+    const float3 t2 = cross(vh, t1);
+    const float r = sqrtf(u0);
+    float sp, cp;
+    sincosf(2.f * kPiF * u1, &sp, &cp);
+    const float p1 = r * cp;
+    const float s = 0.5f * (1.f + vh.z);
+    const float p2 = (1.f - s) * sqrtf(fmaxf(0.f, 1.f - p1 * p1)) + s * (r * sp);
+    const float3 nh = t1 * p1 + t2 * p2 + vh * sqrtf(fmaxf(0.f, 1.f - p1 * p1 - p2 * p2));
+    return normalize(make_float3(a * nh.x, a * nh.y, fmaxf(1e-6f, nh.z)));
+}
+PG3_DI float3 sampleGgxVndf(float3 wo, float a, float u0, float u1, bool exact)
+{
+    return exact ? sampleGgxVndfExact(wo, a, u0, u1) : sampleGgxVisibleNormals(wo, a, u0, u1);
+}
+
 PG3_DI float ggxPdfVisibleNormals(float3 wo, float3 h, float D, float a)          // :732-756
 {
     if (h.z <= 0.f) return 0.0f;
@@ -392,7 +415,7 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         r.wil = sampleCosHemisphere(u0, u1, r.pdfW);
         r.att = (r.wil.z <= 0.f || wol.z <= 0.f) ? f3(0.f) : make_float3(m.r, m.g, m.b) * kPiInvF;
     } else if (K == kMatGgxConductor) {
-        const float3 h = sampleGgxVisibleNormals(wol, m.alpha, u0, u1);
+        const float3 h = sampleGgxVndf(wol, m.alpha, u0, u1, m.vndfExact != 0);
         const float D = ggxD(h, m.alpha);
         bool above;
         r.wil = reflect(above, wol, h);
@@ -406,7 +429,7 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         c.wo = wol * s;
         c.etaS = below ? m.etaInv : m.eta;
         c.etaInvS = below ? m.eta : m.etaInv;
-        c.m = sampleGgxVisibleNormals(c.wo, m.alpha, u0, u1);
+        c.m = sampleGgxVndf(c.wo, m.alpha, u0, u1, m.vndfExact != 0);
         c.D = ggxD(c.m, m.alpha);
         c.F = fresnelDielectric(dot(c.m, c.wo), c.etaS);
         bool above;

@@ -16,6 +16,7 @@
 #pragma once
 
 #include "pg3_device.cuh"
+#include "pg3_steer.cuh"
 #include "pg3_traverse.cuh"
 
 namespace pg3 {
@@ -77,18 +78,24 @@ PG3_DI float3 bgEmission(const SceneView &S, float3 dir, bool wantPdf, const Fra
 {
     if (S.bgKind == kBgEnvMap) {
         const float3 L = emEvaluateDir(S, dir);
-        if (wantPdf) pdf = (S.emSampler == kEmCdf) ? emCdfPdf(S, dir) : cosSpherePdfFront(toLocal(pf, dir));
+        if (wantPdf)
+            pdf = (S.emSampler == kEmCdf) ? emCdfPdf(S, dir)
+                  : (S.emSampler == kEmSteerable) ? steerPdf(S.steer, dir, pf.z) : cosSpherePdfFront(toLocal(pf, dir));
         return L;
     }
     if (wantPdf) pdf = cosSpherePdfFront(toLocal(pf, dir));
     return S.bgConst;
 }
 // BackgroundLight::SampleIllumination (src/lights.hxx:424-445)
-PG3_DI void bgSample(const SceneView &S, const Frame &f, float u0, float u1, float3 &wig, float &pdfW,
+PG3_DI void bgSample(const SceneView &S, const Frame &f, float u0, float u1, float u2, float3 &wig, float &pdfW,
                      float3 &radCos)
 {
     if (S.bgKind == kBgEnvMap && S.emSampler == kEmCdf) {
         emCdfSample(S, f.z, u0, u1, wig, pdfW, radCos);
+        return;
+    }
+    if (S.bgKind == kBgEnvMap && S.emSampler == kEmSteerable) {
+        steerSample(S, f.z, u0, u1, u2, wig, pdfW, radCos);
         return;
     }
     const float3 wil = sampleCosHemisphere(u0, u1, pdfW);   // cosine sampler, front side only
@@ -179,7 +186,7 @@ PG3_DI float3 tracePath(const SceneView &S, uint32_t pixel, uint32_t sample, Pat
                 float3 wig, smp;
                 float dist, pdfW;
                 if (lid == S.bgLightId) {
-                    bgSample(S, frame, ra.b, ra.c, wig, pdfW, smp);
+                    bgSample(S, frame, ra.b, ra.c, ra.d, wig, pdfW, smp);
                     dist = kFloatMax;
                 } else {
                     areaSample(S.lights[lid], pt, n, ra.b, ra.c, wig, dist, smp, pdfW);

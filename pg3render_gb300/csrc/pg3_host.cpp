@@ -95,8 +95,6 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
     if (o.splitting_budget != 1) return bad(PG3GPU_ERR_UNSUPPORTED, "splitting budget other than 1 is not implemented");
     if (o.em_sampler != PG3GPU_EM_CDF && o.em_sampler != PG3GPU_EM_COSINE && o.em_sampler != PG3GPU_EM_STEERABLE)
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown environment-map sampler");
-    if (o.em_sampler == PG3GPU_EM_STEERABLE)
-        return bad(PG3GPU_ERR_UNSUPPORTED, "steerable sampler not available in this build");
     if (sc.num_materials == 0 || !sc.materials) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "scene has no materials");
     if ((sc.num_triangles && !sc.triangles) || (sc.num_spheres && !sc.spheres) ||
         (sc.num_area_lights && !sc.area_lights))
@@ -153,6 +151,7 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         }
         if (!(m.alpha >= 0.f) && m.kind != PG3GPU_MAT_LAMBERT)
             return bad(PG3GPU_ERR_INVALID_ARGUMENT, "GGX roughness must be >= 0");
+        d.vndfExact = (o.ggx_sampler == PG3GPU_GGX_VNDF_REFERENCE_FIT) ? 0 : 1;
         out.mats[i] = d;
     }
 
@@ -231,6 +230,11 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         buildEmCdf(sc.env_map, sc.env_width, sc.env_height, out.emMarg, out.emCond);
         v.emW = sc.env_width;
         v.emH = sc.env_height;
+        if (o.em_sampler == PG3GPU_EM_STEERABLE) {
+            if (!buildSteerable(sc.env_map, sc.env_width, sc.env_height, o.steer_subdiv_level, out.steer, err))
+                return PG3GPU_ERR_INVALID_ARGUMENT;
+            out.hasSteer = true;
+        }
     } else if (sc.background != PG3GPU_BG_NONE && sc.background != PG3GPU_BG_CONSTANT) {
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown background kind");
     }

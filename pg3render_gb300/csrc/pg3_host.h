@@ -9,6 +9,7 @@
 
 #include "../../include/pg3gpu.h"
 #include "pg3_scene_view.h"
+#include "pg3_steerable.h"
 
 namespace pg3 {
 
@@ -23,6 +24,8 @@ struct HostScene {
     std::vector<DevAreaLight> lights;
     std::vector<float4> em;
     std::vector<float> emMarg, emCond;
+    SteerableHost steer;
+    bool hasSteer = false;
 };
 
 // Returns PG3GPU_OK or an error status with a message in err.

@@ -30,4 +30,14 @@ cudaError_t launchWavefront(const SceneView &S, bool naive, uint32_t sample0, ui
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch,
                             uint64_t capacity, int gridBlocks, cudaStream_t stream, uint64_t *launches);
 
+// pg3_probe.cu (sampler probes for tests)
+cudaError_t launchProbeBsdf(const SceneView &S, int mat, uint32_t n, const float *wol, uint32_t seed, float *wil,
+                            float *pdfS, float *pdfE, float *attS, float *attE, cudaStream_t st);
+cudaError_t launchProbeBsdfPdf(const SceneView &S, int mat, uint32_t n, const float *wol, const float *wil, float *pdf,
+                               float *att, cudaStream_t st);
+cudaError_t launchProbeLight(const SceneView &S, int light, uint32_t n, const float *pts, const float *nrms,
+                             uint32_t seed, float *dirs, float *pdfS, float *pdfE, float *rad, cudaStream_t st);
+cudaError_t launchProbeLightPdf(const SceneView &S, int light, uint32_t n, const float *pts, const float *nrms,
+                                const float *dirs, float *pdf, cudaStream_t st);
+
 }  // namespace pg3

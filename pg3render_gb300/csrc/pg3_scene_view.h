@@ -24,7 +24,8 @@ struct DevMaterial {          // 48 bytes
     float absorb;             // conductor k
     float rrProb;             // Russian-roulette continuation probability (clamped to 0.997)
     int zeroRefl;             // Lambert with zero reflectance: paths end here (lights)
-    int pad0, pad1;
+    int vndfExact;            // GGX: exact visible-normal sampling (1) or the reference's fitted routine (0)
+    int pad1;
 };
 
 struct DevAreaLight {         // 64 bytes; radiance rides in the w lanes
@@ -44,14 +45,15 @@ struct BvhNode {
     float4 hi_r;              // right child box max xyz, unused
 };
 
-// Steerable sampler tables (filled by the host build; see steerable.cpp).
+// Steerable sampler tables (host build in pg3_steerable.cpp, sampling in pg3_steer.cuh).
 struct SteerView {
-    const float4 *vdir;       // per vertex: unit direction xyz, unused
-    const float *vsh;         // per vertex: 9 SH-weighted coefficients (luminance basis values)
-    const int4 *tri;          // per leaf triangle: vertex ids (x, y, z), unused
-    const float *nodeW;       // per tree node: 9 summed coefficients
-    const int *nodeChild;     // per tree node: 6 child ids (>= 0 node, < 0 ~leaf triangle, INT_MIN none)
-    uint32_t numNodes, numTris;
+    const float4 *vdir;       // per vertex: unit direction xyz
+    const float *vw;          // per vertex: 9 SH basis values scaled by the map's luminance
+    const int4 *tri;          // vertex ids of the triangles of every subdivision level
+    const float *nodeW;       // per 6-ary tree node: 6 children x 9 summed weights
+    const int *nodeChild;     // per node: 6 child ids (>= 0 node, < 0 ~leaf, INT_MIN none)
+    uint32_t level;           // leaf subdivision level
+    uint32_t levelOff[10];    // first entry of each level in `tri`
     int root;
 };
 

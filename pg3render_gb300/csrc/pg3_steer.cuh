@@ -1,0 +1,190 @@
+// Steerable environment-map sampling on the device (tables from pg3_steerable.cpp).
+//
+// Target density (solid angle), for a surface normal n with clamped-cosine SH
+// coefficients c(n) (src/em_steerable_sampler.hxx:657-688, with the reference's
+// +0.15 compensation that keeps the approximation positive everywhere):
+//   base(w) = g_T(p) / Z(n) * r^3 / d_T
+// where T is the leaf triangle containing w, p the point where w meets T's plane
+// (distance d_T from the origin, r = |p|), g_T the linear interpolation over T of
+// the vertex values (vertex weight . c), and Z(n) the sum of all leaf integrals.
+// Sampling draws T from the 6-ary tree (src/em_steerable_sampler.hxx:3798-3875),
+// then p with density proportional to g_T on the planar triangle, then w = p/|p|;
+// its pdf is exactly base(w). Directions below the horizon are mirrored through
+// the origin as in the reference (:2196-2208), so the returned pdf is
+// base(w) + base(-w) for both sampled and evaluated directions.
+#pragma once
+
+#include <climits>
+
+#include "pg3_device.cuh"
+
+namespace pg3 {
+
+PG3_DI void steerCoeffs(float3 n, float c[9])
+{
+    const float c1 = .429043f, c2 = .511644f, c3 = .743125f, c4 = .886227f, c5 = .247708f;
+    c[0] = c4 + 0.15f;
+    c[1] = 2.f * c2 * n.y;
+    c[2] = 2.f * c2 * n.z;
+    c[3] = 2.f * c2 * n.x;
+    c[4] = 2.f * c1 * n.x * n.y;
+    c[5] = 2.f * c1 * n.y * n.z;
+    c[6] = c3 * n.z * n.z - c5;
+    c[7] = 2.f * c1 * n.x * n.z;
+    c[8] = c1 * (n.x * n.x - n.y * n.y);
+}
+
+PG3_DI float dot9(const float *__restrict__ w, const float c[9])
+{
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) s += __ldg(&w[k]) * c[k];
+    return s;
+}
+
+// Whole-sphere integral Z(n): the root node's children.
+PG3_DI float steerTotal(const SteerView &T, const float c[9])
+{
+    float z = 0.f;
+    for (int i = 0; i < 6; ++i)
+        if (__ldg(&T.nodeChild[T.root * 6 + i]) != INT_MIN) z += fmaxf(dot9(&T.nodeW[(T.root * 6 + i) * 9], c), 0.f);
+    return z;
+}
+
+PG3_DI float3 vdir(const SteerView &T, int v) { return xyz(__ldg(&T.vdir[v])); }
+
+// g_T at a planar point with barycentrics b, and the solid-angle Jacobian r^3 / d_T.
+PG3_DI float steerLeafPdf(const SteerView &T, int4 tri, float b0, float b1, float b2, const float c[9], float Z)
+{
+    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
+    const float v0 = fmaxf(dot9(&T.vw[tri.x * 9], c), 0.f);
+    const float v1 = fmaxf(dot9(&T.vw[tri.y * 9], c), 0.f);
+    const float v2 = fmaxf(dot9(&T.vw[tri.z * 9], c), 0.f);
+    const float g = fmaxf(b0 * v0 + b1 * v1 + b2 * v2, 0.f);
+    const float3 p = A * b0 + B * b1 + C * b2;
+    const float3 nT = normalize(cross(B - A, C - A));
+    const float d = dot(nT, A);
+    const float r = length(p);
+    return (Z > 0.f) ? g / Z * (r * r * r / d) : 0.f;
+}
+
+// Leaf (level-L triangle) containing direction w, through the subdivision hierarchy.
+PG3_DI int steerLocate(const SteerView &T, float3 w)
+{
+    int best = 0;
+    float bestMin = -1e30f;
+    for (int f = 0; f < 20; ++f) {
+        const int4 t = __ldg(&T.tri[f]);
+        const float3 a = vdir(T, t.x), b = vdir(T, t.y), c = vdir(T, t.z);
+        const float m = fminf(fminf(dot(w, cross(a, b)), dot(w, cross(b, c))), dot(w, cross(c, a)));
+        if (m > bestMin) { bestMin = m; best = f; }
+    }
+    int local = best;
+    for (uint32_t l = 0; l < T.level; ++l) {
+        const int4 mid = __ldg(&T.tri[T.levelOff[l + 1] + 4 * local + 3]);   // (ab, bc, ca)
+        const float3 ab = vdir(T, mid.x), bc = vdir(T, mid.y), ca = vdir(T, mid.z);
+        int child = 3;
+        if (dot(w, cross(ab, ca)) >= 0.f) child = 0;
+        else if (dot(w, cross(bc, ab)) >= 0.f) child = 1;
+        else if (dot(w, cross(ca, bc)) >= 0.f) child = 2;
+        local = 4 * local + child;
+    }
+    return local;
+}
+
+// base(w) for any direction.
+PG3_DI float steerBasePdf(const SteerView &T, float3 w, const float c[9], float Z)
+{
+    const int leaf = steerLocate(T, w);
+    const int4 tri = __ldg(&T.tri[T.levelOff[T.level] + leaf]);
+    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
+    const float3 n = cross(B - A, C - A);
+    const float dw = dot(n, w);
+    if (!(dw > 0.f)) return 0.f;
+    const float3 p = w * (dot(n, A) / dw);        // w meets the leaf's plane
+    const float nn = dot(n, n);
+    const float b0 = dot(cross(B - p, C - p), n) / nn;
+    const float b1 = dot(cross(C - p, A - p), n) / nn;
+    return steerLeafPdf(T, tri, b0, b1, 1.f - b0 - b1, c, Z);
+}
+
+// Pdf of the mirrored-hemisphere sampler for a direction above the surface (front side).
+PG3_DI float steerPdf(const SteerView &T, float3 w, float3 n)
+{
+    if (dot(w, n) < 0.f) return 0.f;
+    float c[9];
+    steerCoeffs(n, c);
+    const float Z = steerTotal(T, c);
+    if (!(Z > 0.f)) return 0.f;
+    return steerBasePdf(T, w, c, Z) + steerBasePdf(T, -w, c, Z);
+}
+
+// Samples a direction in the upper hemisphere of n. Returns false when the map is black.
+PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float u2, float3 &wig, float &pdf,
+                        float3 &radCos)
+{
+    const SteerView &T = S.steer;
+    float c[9];
+    steerCoeffs(n, c);
+    const float Z = steerTotal(T, c);
+    if (!(Z > 0.f)) { pdf = 0.f; radCos = f3(0.f); wig = n; return false; }
+    // tree descent with the rescaled uniform (src/em_steerable_sampler.hxx:3798-3875)
+    int node = T.root;
+    float u = u0;
+    int leaf = -1;
+    for (int depth = 0; depth < 32; ++depth) {
+        float val[6], cum = 0.f;
+        int ids[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            ids[i] = __ldg(&T.nodeChild[node * 6 + i]);
+            val[i] = (ids[i] != INT_MIN) ? fmaxf(dot9(&T.nodeW[(node * 6 + i) * 9], c), 0.f) : 0.f;
+            cum += val[i];
+        }
+        // children occupy the first slots; the first one whose running sum exceeds t wins,
+        // rounding past the end falls back to the last child
+        const float t = u * 0.999999f * cum;
+        float lo = 0.f;
+        int pick = -1, last = -1;
+        for (int i = 0; i < 6 && ids[i] != INT_MIN; ++i) {
+            last = i;
+            if (t < lo + val[i]) { pick = i; break; }
+            lo += val[i];
+        }
+        if (last < 0) { atomicOr(S.errorFlag, kErrSteerDescent); return false; }
+        if (pick < 0) { pick = last; lo -= val[last]; }
+        u = fminf((t - lo) / fmaxf(val[pick], 1e-30f), 1.f);
+        const int id = ids[pick];
+        if (id < 0) { leaf = ~id; break; }
+        node = id;
+    }
+    if (leaf < 0) { atomicOr(S.errorFlag, kErrSteerDescent); return false; }
+
+    // exact sample of the linear density on the planar triangle: pick corner i with
+    // probability v_i / sum, then barycentric b_i from its marginal 6b(1-b) (inverse of
+    // 3b^2 - 2b^3), the other two uniformly along the remaining segment
+    const int4 tri = __ldg(&T.tri[T.levelOff[T.level] + leaf]);
+    const float v0 = fmaxf(dot9(&T.vw[tri.x * 9], c), 0.f);
+    const float v1 = fmaxf(dot9(&T.vw[tri.y * 9], c), 0.f);
+    const float v2 = fmaxf(dot9(&T.vw[tri.z * 9], c), 0.f);
+    const float vs = v0 + v1 + v2;
+    const float ts = u * vs;
+    const int corner = (vs > 0.f) ? ((ts < v0) ? 0 : ((ts < v0 + v1) ? 1 : 2)) : min((int)(u * 3.f), 2);
+    const float bi = 0.5f - sinf(asinf(clampf(1.f - 2.f * u1, -1.f, 1.f)) * (1.f / 3.f));
+    const float rest = 1.f - bi;
+    const float bj = rest * u2, bk = rest - bj;
+    float b0, b1, b2;
+    if (corner == 0) { b0 = bi; b1 = bj; b2 = bk; }
+    else if (corner == 1) { b1 = bi; b2 = bj; b0 = bk; }
+    else { b2 = bi; b0 = bj; b1 = bk; }
+    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
+    const float3 w0 = normalize(A * b0 + B * b1 + C * b2);
+    pdf = steerLeafPdf(T, tri, b0, b1, b2, c, Z) + steerBasePdf(T, -w0, c, Z);
+    float cosIn = dot(w0, n);
+    wig = w0;
+    if (cosIn < 0.f) { wig = -w0; cosIn = -cosIn; }
+    radCos = emEvaluateDir(S, wig) * cosIn;
+    return true;
+}
+
+}  // namespace pg3

@@ -1,0 +1,189 @@
+// Host-side build of the steerable sampler tables (see pg3_steerable.h).
+#include "pg3_steerable.h"
+
+#include <climits>
+#include <cmath>
+#include <map>
+#include <utility>
+
+namespace pg3 {
+
+namespace {
+
+struct D3 { double x, y, z; };
+D3 sub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+D3 add(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+D3 crs(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+double dt(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+D3 nrm(D3 a) { const double l = std::sqrt(dt(a, a)); return {a.x / l, a.y / l, a.z / l}; }
+
+const float kPi = 3.14159265358979f;
+
+// Bilinear (tent) lookup of the lat-long map, as the kernels do (src/em_image.hxx:95-143).
+float emLuminanceAt(const float *rgb, uint32_t W, uint32_t H, float dx, float dy, float dz)
+{
+    const float phi = -std::atan2(dy, dx);
+    const float theta = std::acos(std::fmin(std::fmax(dz, -1.f), 1.f));
+    const float u = std::fmin(std::fmax(0.5f + phi * 0.5f * (1.f / kPi), 0.f), 1.f);
+    const float v = std::fmin(std::fmax(theta * (1.f / kPi), 0.f), 1.f);
+    const float xf = u * (float)W, yf = v * (float)H;
+    const int cx = (int)(xf + 0.5f), cy = (int)(yf + 0.5f);
+    const int x0 = cx - 1, y0 = cy - 1;
+    const float xl = xf - ((float)x0 + 0.5f), yl = yf - ((float)y0 + 0.5f);
+    auto wrap = [&](int x, int y, int &ox, int &oy) {
+        int rx = x, ry = y;
+        if (y >= (int)H) { rx = x + (int)W / 2; ry = (int)H - 1; }
+        else if (y < 0) { rx = x + (int)W / 2; ry = 0; }
+        int m = rx % (int)W;
+        if (m < 0) m += (int)W;
+        ox = m; oy = ry;
+    };
+    auto lum = [&](int x, int y) {
+        const float *p = rgb + ((size_t)y * W + (size_t)x) * 3;
+        return 0.212671f * p[0] + 0.715160f * p[1] + 0.072169f * p[2];
+    };
+    int ax, ay, bx, by;
+    wrap(x0, y0, ax, ay);
+    wrap(cx, cy, bx, by);
+    const float top = (1.f - xl) * lum(ax, ay) + xl * lum(bx, ay);
+    const float bot = (1.f - xl) * lum(ax, by) + xl * lum(bx, by);
+    return (1.f - yl) * top + yl * bot;
+}
+
+// 9 real SH basis values (Ramamoorthi & Hanrahan 2001), scaled by s.
+void shBasis(double x, double y, double z, double s, float *o)
+{
+    o[0] = (float)(s * 0.282095);
+    o[1] = (float)(s * 0.488603 * y);
+    o[2] = (float)(s * 0.488603 * z);
+    o[3] = (float)(s * 0.488603 * x);
+    o[4] = (float)(s * 1.092548 * x * y);
+    o[5] = (float)(s * 1.092548 * y * z);
+    o[6] = (float)(s * 0.315392 * (3.0 * z * z - 1.0));
+    o[7] = (float)(s * 1.092548 * x * z);
+    o[8] = (float)(s * 0.546274 * (x * x - y * y));
+}
+
+}  // namespace
+
+bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, SteerableHost &out, std::string &err)
+{
+    if (level > 7) { err = "steerable subdivision level must be <= 7"; return false; }
+    out = SteerableHost();
+    out.level = level;
+
+    // icosahedron: the 12 cyclic permutations of (0, +-1, +-t), normalised
+    const double t = (1.0 + std::sqrt(5.0)) / 2.0;
+    std::vector<D3> v;
+    for (int s1 = -1; s1 <= 1; s1 += 2)
+        for (int s2 = -1; s2 <= 1; s2 += 2) {
+            v.push_back(nrm({0.0, (double)s1, s2 * t}));
+            v.push_back(nrm({(double)s1, s2 * t, 0.0}));
+            v.push_back(nrm({s2 * t, 0.0, (double)s1}));
+        }
+    double emin = 1e9;
+    for (size_t i = 0; i < v.size(); ++i)
+        for (size_t j = i + 1; j < v.size(); ++j) emin = std::fmin(emin, std::sqrt(dt(sub(v[i], v[j]), sub(v[i], v[j]))));
+    auto adjacent = [&](size_t i, size_t j) { return std::sqrt(dt(sub(v[i], v[j]), sub(v[i], v[j]))) < emin * 1.001; };
+    std::vector<int4> level0;
+    for (size_t i = 0; i < v.size(); ++i)
+        for (size_t j = i + 1; j < v.size(); ++j)
+            for (size_t k = j + 1; k < v.size(); ++k)
+                if (adjacent(i, j) && adjacent(j, k) && adjacent(i, k)) {
+                    const D3 n = crs(sub(v[j], v[i]), sub(v[k], v[i]));
+                    const bool ccw = dt(n, add(add(v[i], v[j]), v[k])) > 0;   // outward facing
+                    level0.push_back(make_int4((int)i, ccw ? (int)j : (int)k, ccw ? (int)k : (int)j, 0));
+                }
+    if (level0.size() != 20) { err = "icosahedron construction failed"; return false; }
+
+    // 4-way subdivision, children (A,ab,ca), (ab,B,bc), (ca,bc,C), (ab,bc,ca)
+    std::map<std::pair<int, int>, int> mid;
+    auto midpoint = [&](int a, int b) {
+        const auto key = std::make_pair(std::min(a, b), std::max(a, b));
+        auto it = mid.find(key);
+        if (it != mid.end()) return it->second;
+        v.push_back(nrm(add(v[a], v[b])));
+        const int id = (int)v.size() - 1;
+        mid[key] = id;
+        return id;
+    };
+    out.tri = level0;
+    out.levelOffset.push_back(0);
+    std::vector<int4> cur = level0;
+    for (uint32_t l = 0; l < level; ++l) {
+        std::vector<int4> next;
+        next.reserve(cur.size() * 4);
+        for (const int4 &T : cur) {
+            const int ab = midpoint(T.x, T.y), bc = midpoint(T.y, T.z), ca = midpoint(T.z, T.x);
+            next.push_back(make_int4(T.x, ab, ca, 0));
+            next.push_back(make_int4(ab, T.y, bc, 0));
+            next.push_back(make_int4(ca, bc, T.z, 0));
+            next.push_back(make_int4(ab, bc, ca, 0));
+        }
+        out.levelOffset.push_back((uint32_t)out.tri.size());
+        out.tri.insert(out.tri.end(), next.begin(), next.end());
+        cur.swap(next);
+    }
+    out.levelOffset.push_back((uint32_t)out.tri.size());
+
+    // vertex weights: SH basis scaled by the map's luminance in the vertex direction
+    const size_t nv = v.size();
+    out.vdir.resize(nv);
+    out.vw.resize(nv * 9);
+    for (size_t i = 0; i < nv; ++i) {
+        out.vdir[i] = make_float4((float)v[i].x, (float)v[i].y, (float)v[i].z, 0.f);
+        const float L = emLuminanceAt(rgb, W, H, (float)v[i].x, (float)v[i].y, (float)v[i].z);
+        shBasis(v[i].x, v[i].y, v[i].z, (double)L, &out.vw[i * 9]);
+    }
+
+    // leaf weights: planar area x mean vertex weight (src/em_steerable_sampler.hxx:1277-1296)
+    const uint32_t nLeaf = (uint32_t)cur.size();
+    std::vector<float> leafW((size_t)nLeaf * 9);
+    for (uint32_t i = 0; i < nLeaf; ++i) {
+        const int4 T = cur[i];
+        const D3 a = {out.vdir[T.x].x, out.vdir[T.x].y, out.vdir[T.x].z};
+        const D3 b = {out.vdir[T.y].x, out.vdir[T.y].y, out.vdir[T.y].z};
+        const D3 c = {out.vdir[T.z].x, out.vdir[T.z].y, out.vdir[T.z].z};
+        const D3 cr = crs(sub(b, a), sub(c, a));
+        const double area = 0.5 * std::sqrt(dt(cr, cr));
+        for (int k = 0; k < 9; ++k)
+            leafW[(size_t)i * 9 + k] = (float)(area * ((double)out.vw[T.x * 9 + k] + out.vw[T.y * 9 + k] +
+                                                       out.vw[T.z * 9 + k]) / 3.0);
+    }
+
+    // 6-ary tree, bottom-up over consecutive nodes (src/em_steerable_sampler.hxx:3755-3793)
+    struct Item { int id; float w[9]; };
+    std::vector<Item> layer(nLeaf);
+    for (uint32_t i = 0; i < nLeaf; ++i) {
+        layer[i].id = ~(int)i;
+        for (int k = 0; k < 9; ++k) layer[i].w[k] = leafW[(size_t)i * 9 + k];
+    }
+    do {
+        std::vector<Item> up;
+        for (size_t s = 0; s < layer.size(); s += 6) {
+            const int node = (int)(out.nodeChild.size() / 6);
+            Item parent;
+            parent.id = node;
+            for (int k = 0; k < 9; ++k) parent.w[k] = 0.f;
+            for (size_t c = 0; c < 6; ++c) {
+                if (s + c < layer.size()) {
+                    const Item &ch = layer[s + c];
+                    out.nodeChild.push_back(ch.id);
+                    for (int k = 0; k < 9; ++k) {
+                        out.nodeW.push_back(ch.w[k]);
+                        parent.w[k] += ch.w[k];
+                    }
+                } else {
+                    out.nodeChild.push_back(INT_MIN);
+                    for (int k = 0; k < 9; ++k) out.nodeW.push_back(0.f);
+                }
+            }
+            up.push_back(parent);
+        }
+        layer.swap(up);
+    } while (layer.size() > 1);
+    out.root = layer[0].id;
+    return true;
+}
+
+}  // namespace pg3

@@ -1,0 +1,47 @@
+// Steerable environment-map sampler (Subr & Arvo 2007, as structured by the
+// reference's EnvironmentMapSteerableSampler, src/em_steerable_sampler.hxx),
+// host-side build in device layout.
+//
+// Triangulation: the unit icosahedron (src/geom.hxx:291-346) subdivided 4-way
+// `level` times with edge midpoints pushed to the sphere -- the reference's
+// refinement with minimum = maximum subdivision level (level 3: 1280 triangles).
+// Each vertex carries its 9 SH basis values scaled by the environment map's
+// luminance in its direction (src/em_steerable_sampler.hxx:181-202, 3084-3095);
+// each leaf triangle the planar area times its mean vertex weight (:1277-1296).
+// A 6-ary tree is built bottom-up over the leaves in subdivision order
+// (:3755-3793).
+//
+// Corrections over the reference (whose sampled and evaluated pdfs disagree):
+// * the density is the linear interpolation of the vertex values on the planar
+//   triangle, and the reported solid-angle pdf includes the planar-to-sphere
+//   Jacobian r^2 / cos;
+// * the in-triangle sampler is exact (a mixture of the three corner-weighted
+//   densities, each sampled by inverting its cubic marginal);
+// * pdf evaluation locates a direction's leaf through the subdivision hierarchy
+//   (20 faces, then one of 4 children per level) instead of reading the
+//   environment map, so evaluated pdf == sampled pdf.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace pg3 {
+
+struct SteerableHost {
+    uint32_t level = 0;
+    std::vector<float4> vdir;          // vertex directions
+    std::vector<float> vw;             // 9 weights per vertex
+    std::vector<int4> tri;             // vertex ids of every triangle of every level (level 0 first)
+    std::vector<uint32_t> levelOffset; // first triangle of each level in `tri` (level+1 entries + end)
+    std::vector<float> nodeW;          // 6 x 9 child weights per tree node
+    std::vector<int> nodeChild;        // 6 child ids per node: >= 0 node, < 0 ~leaf, INT32_MIN none
+    int root = 0;
+};
+
+// rgb: env_height rows of env_width RGB float texels (row 0 at theta = 0).
+bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, SteerableHost &out, std::string &err);
+
+}  // namespace pg3

@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kWaveBlock) shadeKernel(const __grid_constant_
                             float3 wig, smp;
                             float dist, pdfW;
                             if (lid == S.bgLightId) {
-                                bgSample(S, frame, ra.b, ra.c, wig, pdfW, smp);
+                                bgSample(S, frame, ra.b, ra.c, ra.d, wig, pdfW, smp);
                                 dist = kFloatMax;
                             } else {
                                 areaSample(S.lights[lid], pt, nrm, ra.b, ra.c, wig, dist, smp, pdfW);

@@ -39,6 +39,7 @@ class Config:
     pipeline: int = PIPELINE_AUTO
     steer_subdiv_level: int = 3
     max_paths_in_flight: int = 0
+    ggx_sampler: int = 0                 # GGX_VNDF_EXACT; GGX_VNDF_REFERENCE_FIT = the reference's routine
 
     def options(self, seed=None):
         o = _lib.Options()
@@ -55,6 +56,7 @@ class Config:
         o.steer_subdiv_level = self.steer_subdiv_level
         o.seed = self.base_seed if seed is None else seed
         o.max_paths_in_flight = self.max_paths_in_flight
+        o.ggx_sampler = self.ggx_sampler
         return o
 
 
@@ -126,6 +128,48 @@ class GpuPathTracer:
 
     def reset_stats(self):
         _lib.check(self._L.pg3gpu_reset_stats(self._ctx), self._ctx)
+
+    # -- sampler probes (tests) --------------------------------------------------------
+    def probe_bsdf(self, material, wol, seed=0):
+        wol = np.ascontiguousarray(wol, np.float32)
+        n = len(wol)
+        wil, ps, pe = np.zeros((n, 3), np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32)
+        a_s, a_e = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)   # noqa: E731
+        _lib.check(self._L.pg3gpu_probe_bsdf(self._ctx, material, n, p(wol), seed, p(wil), p(ps), p(pe), p(a_s),
+                                             p(a_e)), self._ctx)
+        return dict(wil=wil, pdf_sampled=ps, pdf_eval=pe, att_sampled=a_s, att_eval=a_e)
+
+    def probe_bsdf_pdf(self, material, wol, wil, with_att=False):
+        wol = np.ascontiguousarray(wol, np.float32)
+        wil = np.ascontiguousarray(wil, np.float32)
+        out = np.zeros(len(wol), np.float32)
+        att = np.zeros(len(wol), np.float32)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)   # noqa: E731
+        _lib.check(self._L.pg3gpu_probe_bsdf_pdf(self._ctx, material, len(wol), p(wol), p(wil), p(out), p(att)),
+                   self._ctx)
+        return (out, att) if with_att else out
+
+    def probe_light(self, light, points, normals, seed=0):
+        pts = np.ascontiguousarray(points, np.float32)
+        nrm = np.ascontiguousarray(normals, np.float32)
+        n = len(pts)
+        d, ps, pe, rc = np.zeros((n, 3), np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32), \
+            np.zeros((n, 3), np.float32)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)   # noqa: E731
+        _lib.check(self._L.pg3gpu_probe_light(self._ctx, light, n, p(pts), p(nrm), seed, p(d), p(ps), p(pe), p(rc)),
+                   self._ctx)
+        return dict(dirs=d, pdf_sampled=ps, pdf_eval=pe, radiance_cos=rc)
+
+    def probe_light_pdf(self, light, points, normals, dirs):
+        pts = np.ascontiguousarray(points, np.float32)
+        nrm = np.ascontiguousarray(normals, np.float32)
+        dd = np.ascontiguousarray(dirs, np.float32)
+        out = np.zeros(len(pts), np.float32)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)   # noqa: E731
+        _lib.check(self._L.pg3gpu_probe_light_pdf(self._ctx, light, len(pts), p(pts), p(nrm), p(dd), p(out)),
+                   self._ctx)
+        return out
 
     def device_framebuffer(self):
         a, b = ctypes.c_void_p(), ctypes.c_void_p()

@@ -48,3 +48,77 @@ def scene_from_golden(d):
     if s.env_map is not None:
         s.env_map = d["env_map"]
     return s
+
+
+# ----------------------------------------------------------------------------- chi-square
+def sphere_bins(nz, nphi):
+    """Equal-area bins over the sphere: uniform in z = cos(theta) and phi."""
+    return np.linspace(-1.0, 1.0, nz + 1), np.linspace(-np.pi, np.pi, nphi + 1)
+
+
+def histogram_dirs(d, nz, nphi):
+    ze, pe = sphere_bins(nz, nphi)
+    z = np.clip(d[:, 2], -1.0, 1.0)
+    phi = np.arctan2(d[:, 1], d[:, 0])
+    h, _, _ = np.histogram2d(z, phi, bins=[ze, pe])
+    return h
+
+
+def expected_counts(pdf_fn, n, nz, nphi, k=6):
+    """N * integral of pdf over each bin by a k x k midpoint rule (pdf_fn: dirs[m,3] -> pdf[m])."""
+    ze, pe = sphere_bins(nz, nphi)
+    dz, dp = 2.0 / nz, 2 * np.pi / nphi
+    sz = (np.arange(nz * k) + 0.5) * (dz / k) - 1.0
+    sp = (np.arange(nphi * k) + 0.5) * (dp / k) - np.pi
+    Z, PH = np.meshgrid(sz, sp, indexing="ij")
+    r = np.sqrt(np.maximum(0.0, 1.0 - Z * Z))
+    dirs = np.stack([r * np.cos(PH), r * np.sin(PH), Z], -1).reshape(-1, 3).astype(np.float32)
+    pdf = pdf_fn(dirs).astype(np.float64).reshape(nz * k, nphi * k)
+    cell = (dz / k) * (dp / k)
+    return n * pdf.reshape(nz, k, nphi, k).sum(axis=(1, 3)) * cell
+
+
+def chi2_test(observed, expected, min_expected=5.0):
+    """Pearson chi-square with low-expectation bins pooled; returns (p_value, chi2, dof)."""
+    from scipy import stats
+    o = observed.ravel().astype(np.float64)
+    e = expected.ravel().astype(np.float64)
+    keep = e >= min_expected
+    o_pool, e_pool = o[~keep].sum(), e[~keep].sum()
+    oo, ee = list(o[keep]), list(e[keep])
+    if e_pool >= min_expected:
+        oo.append(o_pool)
+        ee.append(e_pool)
+    oo, ee = np.array(oo), np.array(ee)
+    ee *= oo.sum() / ee.sum()      # compare shapes (quadrature normalisation error removed)
+    chi2 = float(((oo - ee) ** 2 / ee).sum())
+    dof = len(oo) - 1
+    return float(stats.chi2.sf(chi2, dof)), chi2, dof
+
+
+def em_pixel_probs(em):
+    """Per-pixel probability of the reference's CDF environment sampler: tent-filtered pixel
+    luminance x sin(theta_mid), normalised (src/em_simple_spherical_sampler.hxx:117-152,
+    src/em_image.hxx:152-183 with the wrap rules of :269-302), restated in numpy."""
+    em = np.asarray(em, np.float64)
+    H, W, _ = em.shape
+    lum = 0.212671 * em[..., 0] + 0.715160 * em[..., 1] + 0.072169 * em[..., 2]
+
+    def at(dx, dy):
+        ys = np.arange(H)[:, None] + dy
+        xs = np.arange(W)[None, :] + dx + np.where((ys < 0) | (ys >= H), W // 2, 0)
+        ys = np.clip(ys, 0, H - 1)
+        return lum[np.broadcast_to(ys, (H, W)), np.mod(xs, W)]
+
+    tent = sum(at(dx, dy) * (2 / 3 if dx == 0 and dy == 0 else 1 / 24) for dx in (-1, 0, 1) for dy in (-1, 0, 1))
+    f = tent * np.sin(np.pi * (np.arange(H) + 0.5) / H)[:, None]
+    return f / f.sum()
+
+
+def dirs_to_pixels(d, W, H):
+    """Lat-long pixel of each direction (src/geom.hxx:77-95)."""
+    phi = -np.arctan2(d[:, 1], d[:, 0])
+    th = np.arccos(np.clip(d[:, 2], -1, 1))
+    u = np.clip(0.5 + phi / (2 * np.pi), 0, 1)
+    v = np.clip(th / np.pi, 0, 1)
+    return np.minimum((v * H).astype(int), H - 1), np.minimum((u * W).astype(int), W - 1)

@@ -92,3 +92,16 @@ def test_reference_harness_runs_and_is_seeded():
     a = O.reference_render(text, renderers=2, iters=1, seed=3)
     b = O.reference_render(text, renderers=2, iters=1, seed=3)
     assert np.array_equal(a["mean"], b["mean"]) and a["mean"].mean() > 0
+
+
+def test_em_pixel_probabilities_match_cdf_tables(tmp_path):
+    # the numpy restatement the GPU chi-square test uses equals the oracle's CDF tables
+    from pg3render_gb300 import scene as S
+    from _util import em_pixel_probs
+    em = S.synthetic_sky(64, 32, seed=5)
+    p = str(tmp_path / "em.bin")
+    S.write_env_map(p, em)
+    marg, cond = O.em_cdf(p, 64, 32)
+    probs = np.diff(marg)[:, None] * np.diff(cond, axis=1)
+    # float32 running sums: a few ulp of 1.0 in each CDF entry
+    assert np.allclose(probs, em_pixel_probs(em), rtol=1e-3, atol=2e-7)
