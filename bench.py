@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--width", type=int, default=512)
     ap.add_argument("--spp", type=int, default=256)
     ap.add_argument("--cpu-iters", type=int, default=12)
+    ap.add_argument("--paths-in-flight", type=int, default=0, help="wavefront chunk size (0: automatic)")
     a = ap.parse_args()
     global WIDTH, HEIGHT, SPP
     WIDTH = HEIGHT = a.width
@@ -190,7 +191,8 @@ def run_gpu(args, rank, world, local_rank):
     pipeline = {"auto": R.PIPELINE_AUTO, "megakernel": R.PIPELINE_MEGAKERNEL,
                 "wavefront": R.PIPELINE_WAVEFRONT}[args.pipeline]
     cfg = P.Config(scene=scene, algorithm=R.kPathTracing, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM,
-                   em_sampler=em_sampler, pipeline=pipeline, base_seed=1234)
+                   em_sampler=em_sampler, pipeline=pipeline, base_seed=1234,
+                   max_paths_in_flight=args.paths_in_flight)
     npix = WIDTH * HEIGHT
     paths_per_step = npix * SPP
     sample_base = rank * (1 << 24)

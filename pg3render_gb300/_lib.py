@@ -114,7 +114,7 @@ def load(path=None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("PG3GPU_LIBRARY") or LIB_PATH
     if not os.path.exists(path):
         raise RuntimeError("pg3gpu: CUDA library not built (%s); run __graft_entry__.build()" % path)
     L = ctypes.CDLL(path)

@@ -33,15 +33,18 @@ def _deps():
     return max(os.path.getmtime(f) for f in files)
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps():
-        return LIB
+def build(force=False, verbose=False, extra_flags=(), out_dir=None):
+    """Compiles into out_dir (default pg3render_gb300/_build) and returns the library path."""
+    bdir = out_dir or BUILD
+    lib = os.path.join(bdir, "libpg3gpu.so")
+    os.makedirs(bdir, exist_ok=True)
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= _deps():
+        return lib
     nvcc = _nvcc()
     objs = []
 
     def compile_one(src):
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(bdir, src + ".o")
         cmd = [nvcc] + ARCH + NVCC_FLAGS + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
             cmd = [nvcc] + NVCC_FLAGS + ["-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
@@ -54,13 +57,13 @@ def build(force=False, verbose=False, extra_flags=()):
 
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr[-8000:])
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

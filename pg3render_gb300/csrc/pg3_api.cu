@@ -261,6 +261,8 @@ int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int dev
         if ((st = upload(ctx, (int4 **)&sv.tri, hs.steer.tri))) return bail(st);
         if ((st = upload(ctx, (float **)&sv.nodeW, hs.steer.nodeW))) return bail(st);
         if ((st = upload(ctx, (int **)&sv.nodeChild, hs.steer.nodeChild))) return bail(st);
+        if ((st = upload(ctx, (float4 **)&sv.leafPlane, hs.steer.leafPlane))) return bail(st);
+        if ((st = upload(ctx, (int4 **)&sv.faceCells, hs.steer.faceCells))) return bail(st);
         sv.level = hs.steer.level;
         for (size_t l = 0; l < hs.steer.levelOffset.size() && l < 10; ++l) sv.levelOff[l] = hs.steer.levelOffset[l];
         sv.root = hs.steer.root;
@@ -303,7 +305,8 @@ int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int dev
     ctx->useWavefront = (opts->pipeline == PG3GPU_PIPELINE_WAVEFRONT || opts->pipeline == PG3GPU_PIPELINE_AUTO);
     if (ctx->useWavefront) {
         const uint64_t npix = (uint64_t)ctx->W * ctx->H;
-        ctx->waveCapacity = std::min<uint64_t>(1ull << 22, std::max<uint64_t>(1ull << 16, npix * 16));
+        const uint64_t cap = opts->max_paths_in_flight ? opts->max_paths_in_flight : (1ull << 22);
+        ctx->waveCapacity = std::min<uint64_t>(cap, std::max<uint64_t>(1ull << 16, npix * 16));
         void *w;
         if ((st = devAlloc(ctx, (char **)&w, wavefrontBytes(ctx->waveCapacity)))) return bail(st);
         ctx->dWave = w;

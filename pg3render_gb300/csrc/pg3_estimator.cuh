@@ -74,27 +74,33 @@ PG3_DI float pickProb(const SceneView &S, float3 pt, float3 n, float sum, int id
 
 // Background emission and its light-sampling pdf for MIS (src/lights.hxx:379-407,
 // src/em.hxx:87-121).
+// EMK selects the environment-map sampler at compile time (-1: read it from the scene), so a
+// specialised kernel carries only the sampler it uses.
+template <int EMK = -1>
 PG3_DI float3 bgEmission(const SceneView &S, float3 dir, bool wantPdf, const Frame &pf, float &pdf)
 {
+    const int em = (EMK >= 0) ? EMK : S.emSampler;
     if (S.bgKind == kBgEnvMap) {
         const float3 L = emEvaluateDir(S, dir);
         if (wantPdf)
-            pdf = (S.emSampler == kEmCdf) ? emCdfPdf(S, dir)
-                  : (S.emSampler == kEmSteerable) ? steerPdf(S.steer, dir, pf.z) : cosSpherePdfFront(toLocal(pf, dir));
+            pdf = (em == kEmCdf) ? emCdfPdf(S, dir)
+                  : (em == kEmSteerable) ? steerPdf(S.steer, dir, pf.z) : cosSpherePdfFront(toLocal(pf, dir));
         return L;
     }
     if (wantPdf) pdf = cosSpherePdfFront(toLocal(pf, dir));
     return S.bgConst;
 }
 // BackgroundLight::SampleIllumination (src/lights.hxx:424-445)
+template <int EMK = -1>
 PG3_DI void bgSample(const SceneView &S, const Frame &f, float u0, float u1, float u2, float3 &wig, float &pdfW,
                      float3 &radCos)
 {
-    if (S.bgKind == kBgEnvMap && S.emSampler == kEmCdf) {
+    const int em = (EMK >= 0) ? EMK : S.emSampler;
+    if (S.bgKind == kBgEnvMap && em == kEmCdf) {
         emCdfSample(S, f.z, u0, u1, wig, pdfW, radCos);
         return;
     }
-    if (S.bgKind == kBgEnvMap && S.emSampler == kEmSteerable) {
+    if (S.bgKind == kBgEnvMap && em == kEmSteerable) {
         steerSample(S, f.z, u0, u1, u2, wig, pdfW, radCos);
         return;
     }

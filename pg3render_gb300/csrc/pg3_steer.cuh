@@ -20,6 +20,8 @@
 
 namespace pg3 {
 
+constexpr int kSteerCellsDev = 8;   // must equal kSteerCells of the host build
+
 PG3_DI void steerCoeffs(float3 n, float c[9])
 {
     const float c1 = .429043f, c2 = .511644f, c3 = .743125f, c4 = .886227f, c5 = .247708f;
@@ -52,32 +54,52 @@ PG3_DI float steerTotal(const SteerView &T, const float c[9])
 }
 
 PG3_DI float3 vdir(const SteerView &T, int v) { return xyz(__ldg(&T.vdir[v])); }
+PG3_DI float vval(const SteerView &T, int v, const float c[9]) { return fmaxf(dot9(&T.vw[v * 9], c), 0.f); }
 
-// g_T at a planar point with barycentrics b, and the solid-angle Jacobian r^3 / d_T.
-PG3_DI float steerLeafPdf(const SteerView &T, int4 tri, float b0, float b1, float b2, const float c[9], float Z)
+// base density of the point p = b0 A + b1 B + b2 C of leaf `leaf` (vertex values v).
+PG3_DI float steerLeafPdf(const SteerView &T, int leaf, float3 p, float g, float Z)
 {
-    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
-    const float v0 = fmaxf(dot9(&T.vw[tri.x * 9], c), 0.f);
-    const float v1 = fmaxf(dot9(&T.vw[tri.y * 9], c), 0.f);
-    const float v2 = fmaxf(dot9(&T.vw[tri.z * 9], c), 0.f);
-    const float g = fmaxf(b0 * v0 + b1 * v1 + b2 * v2, 0.f);
-    const float3 p = A * b0 + B * b1 + C * b2;
-    const float3 nT = normalize(cross(B - A, C - A));
-    const float d = dot(nT, A);
+    const float d = __ldg(&T.leafPlane[leaf].w);
     const float r = length(p);
-    return (Z > 0.f) ? g / Z * (r * r * r / d) : 0.f;
+    return (Z > 0.f) ? fmaxf(g, 0.f) / Z * (r * r * r / d) : 0.f;
 }
 
-// Leaf (level-L triangle) containing direction w, through the subdivision hierarchy.
+PG3_DI float faceMinEdge(const SteerView &T, int f, float3 w)
+{
+    const int4 t = __ldg(&T.tri[f]);
+    const float3 a = vdir(T, t.x), b = vdir(T, t.y), c = vdir(T, t.z);
+    return fminf(fminf(dot(w, cross(a, b)), dot(w, cross(b, c))), dot(w, cross(c, a)));
+}
+
+// Leaf (level-L triangle) containing direction w: a cube-map cell gives at most four
+// candidate icosahedron faces (all 20 are scanned if none contains w), then one of
+// four children per subdivision level by three great-circle tests.
 PG3_DI int steerLocate(const SteerView &T, float3 w)
 {
-    int best = 0;
+    const float ax = fabsf(w.x), ay = fabsf(w.y), az = fabsf(w.z);
+    int a;
+    float wa, wb, wc;
+    if (ax >= ay && ax >= az) { a = 0; wa = w.x; wb = w.y; wc = w.z; }
+    else if (ay >= az) { a = 1; wa = w.y; wb = w.z; wc = w.x; }
+    else { a = 2; wa = w.z; wb = w.x; wc = w.y; }
+    const int face = 2 * a + (wa < 0.f ? 1 : 0);
+    const float inv = 1.f / fabsf(wa);
+    const int iu = min(max((int)((wb * inv + 1.f) * (0.5f * kSteerCellsDev)), 0), kSteerCellsDev - 1);
+    const int iv = min(max((int)((wc * inv + 1.f) * (0.5f * kSteerCellsDev)), 0), kSteerCellsDev - 1);
+    const int cell = (face * kSteerCellsDev + iv) * kSteerCellsDev + iu;
+    const int4 ca = __ldg(&T.faceCells[2 * cell]), cb = __ldg(&T.faceCells[2 * cell + 1]);
+    const int cs[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+    int best = cs[0] >= 0 ? cs[0] : 0;
     float bestMin = -1e30f;
-    for (int f = 0; f < 20; ++f) {
-        const int4 t = __ldg(&T.tri[f]);
-        const float3 a = vdir(T, t.x), b = vdir(T, t.y), c = vdir(T, t.z);
-        const float m = fminf(fminf(dot(w, cross(a, b)), dot(w, cross(b, c))), dot(w, cross(c, a)));
-        if (m > bestMin) { bestMin = m; best = f; }
+    for (int i = 0; i < 8 && cs[i] >= 0; ++i) {
+        const float m = faceMinEdge(T, cs[i], w);
+        if (m > bestMin) { bestMin = m; best = cs[i]; }
+    }
+    if (bestMin < -1e-6f) {
+        for (int f = 0; f < 20; ++f) {
+            const float m = faceMinEdge(T, f, w);
+            if (m > bestMin) { bestMin = m; best = f; }
+        }
     }
     int local = best;
     for (uint32_t l = 0; l < T.level; ++l) {
@@ -97,15 +119,19 @@ PG3_DI float steerBasePdf(const SteerView &T, float3 w, const float c[9], float 
 {
     const int leaf = steerLocate(T, w);
     const int4 tri = __ldg(&T.tri[T.levelOff[T.level] + leaf]);
-    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
-    const float3 n = cross(B - A, C - A);
-    const float dw = dot(n, w);
+    const float4 pl = __ldg(&T.leafPlane[leaf]);
+    const float3 nT = xyz(pl);
+    const float dw = dot(nT, w);
     if (!(dw > 0.f)) return 0.f;
-    const float3 p = w * (dot(n, A) / dw);        // w meets the leaf's plane
+    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
+    const float3 p = w * (pl.w / dw);            // w meets the leaf's plane
+    const float3 n = cross(B - A, C - A);
     const float nn = dot(n, n);
     const float b0 = dot(cross(B - p, C - p), n) / nn;
     const float b1 = dot(cross(C - p, A - p), n) / nn;
-    return steerLeafPdf(T, tri, b0, b1, 1.f - b0 - b1, c, Z);
+    const float b2 = 1.f - b0 - b1;
+    const float g = b0 * vval(T, tri.x, c) + b1 * vval(T, tri.y, c) + b2 * vval(T, tri.z, c);
+    return steerLeafPdf(T, leaf, p, g, Z);
 }
 
 // Pdf of the mirrored-hemisphere sampler for a direction above the surface (front side).
@@ -164,9 +190,7 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     // probability v_i / sum, then barycentric b_i from its marginal 6b(1-b) (inverse of
     // 3b^2 - 2b^3), the other two uniformly along the remaining segment
     const int4 tri = __ldg(&T.tri[T.levelOff[T.level] + leaf]);
-    const float v0 = fmaxf(dot9(&T.vw[tri.x * 9], c), 0.f);
-    const float v1 = fmaxf(dot9(&T.vw[tri.y * 9], c), 0.f);
-    const float v2 = fmaxf(dot9(&T.vw[tri.z * 9], c), 0.f);
+    const float v0 = vval(T, tri.x, c), v1 = vval(T, tri.y, c), v2 = vval(T, tri.z, c);
     const float vs = v0 + v1 + v2;
     const float ts = u * vs;
     const int corner = (vs > 0.f) ? ((ts < v0) ? 0 : ((ts < v0 + v1) ? 1 : 2)) : min((int)(u * 3.f), 2);
@@ -177,9 +201,9 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     if (corner == 0) { b0 = bi; b1 = bj; b2 = bk; }
     else if (corner == 1) { b1 = bi; b2 = bj; b0 = bk; }
     else { b2 = bi; b0 = bj; b1 = bk; }
-    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
-    const float3 w0 = normalize(A * b0 + B * b1 + C * b2);
-    pdf = steerLeafPdf(T, tri, b0, b1, b2, c, Z) + steerBasePdf(T, -w0, c, Z);
+    const float3 p = vdir(T, tri.x) * b0 + vdir(T, tri.y) * b1 + vdir(T, tri.z) * b2;
+    const float3 w0 = normalize(p);
+    pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) + steerBasePdf(T, -w0, c, Z);
     float cosIn = dot(w0, n);
     wig = w0;
     if (cosIn < 0.f) { wig = -w0; cosIn = -cosIn; }

@@ -136,9 +136,11 @@ bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, St
         shBasis(v[i].x, v[i].y, v[i].z, (double)L, &out.vw[i * 9]);
     }
 
-    // leaf weights: planar area x mean vertex weight (src/em_steerable_sampler.hxx:1277-1296)
+    // leaf weights: planar area x mean vertex weight (src/em_steerable_sampler.hxx:1277-1296),
+    // and each leaf's plane (unit normal, distance) for the solid-angle Jacobian
     const uint32_t nLeaf = (uint32_t)cur.size();
     std::vector<float> leafW((size_t)nLeaf * 9);
+    out.leafPlane.resize(nLeaf);
     for (uint32_t i = 0; i < nLeaf; ++i) {
         const int4 T = cur[i];
         const D3 a = {out.vdir[T.x].x, out.vdir[T.x].y, out.vdir[T.x].z};
@@ -146,6 +148,8 @@ bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, St
         const D3 c = {out.vdir[T.z].x, out.vdir[T.z].y, out.vdir[T.z].z};
         const D3 cr = crs(sub(b, a), sub(c, a));
         const double area = 0.5 * std::sqrt(dt(cr, cr));
+        const D3 nT = nrm(cr);
+        out.leafPlane[i] = make_float4((float)nT.x, (float)nT.y, (float)nT.z, (float)dt(nT, a));
         for (int k = 0; k < 9; ++k)
             leafW[(size_t)i * 9 + k] = (float)(area * ((double)out.vw[T.x * 9 + k] + out.vw[T.y * 9 + k] +
                                                        out.vw[T.z * 9 + k]) / 3.0);
@@ -183,6 +187,51 @@ bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, St
         layer.swap(up);
     } while (layer.size() > 1);
     out.root = layer[0].id;
+
+    // face locator: for every cell of a cube map over the sphere, the level-0 faces that
+    // touch the cell (found by dense sampling of the cell enlarged by a margin)
+    const int G = kSteerCells;
+    out.faceCells.assign(2 * 6 * G * G, make_int4(-1, -1, -1, -1));
+    for (int f = 0; f < 6; ++f) {
+        const int ax = f / 2, bx = (ax + 1) % 3, cx = (ax + 2) % 3;
+        const double s = (f & 1) ? -1.0 : 1.0;
+        for (int iv = 0; iv < G; ++iv)
+            for (int iu = 0; iu < G; ++iu) {
+                int found[8], nf = 0;
+                const int K = 24;
+                for (int sv = 0; sv <= K; ++sv)
+                    for (int su = 0; su <= K; ++su) {
+                        const double u = -1.0 + 2.0 * (iu + (su / (double)K) * 1.1 - 0.05) / G;
+                        const double vv = -1.0 + 2.0 * (iv + (sv / (double)K) * 1.1 - 0.05) / G;
+                        double p[3];
+                        p[ax] = s; p[bx] = u; p[cx] = vv;
+                        const D3 w = nrm({p[0], p[1], p[2]});
+                        for (int fi = 0; fi < 20; ++fi) {
+                            const int4 t = level0[fi];
+                            const D3 A = {out.vdir[t.x].x, out.vdir[t.x].y, out.vdir[t.x].z};
+                            const D3 B = {out.vdir[t.y].x, out.vdir[t.y].y, out.vdir[t.y].z};
+                            const D3 C = {out.vdir[t.z].x, out.vdir[t.z].y, out.vdir[t.z].z};
+                            const double m = std::fmin(std::fmin(dt(w, crs(A, B)), dt(w, crs(B, C))), dt(w, crs(C, A)));
+                            if (m >= -1e-3) {
+                                bool have = false;
+                                for (int q = 0; q < nf; ++q) have |= (found[q] == fi);
+                                if (!have && nf < 8) found[nf++] = fi;
+                            }
+                        }
+                    }
+                if (nf > 8) { err = "steerable face locator: more than 8 faces in a cube-map cell"; return false; }
+                int4 &c0 = out.faceCells[2 * ((f * G + iv) * G + iu)];
+                int4 &c1 = out.faceCells[2 * ((f * G + iv) * G + iu) + 1];
+                c0.x = nf > 0 ? found[0] : -1;
+                c0.y = nf > 1 ? found[1] : -1;
+                c0.z = nf > 2 ? found[2] : -1;
+                c0.w = nf > 3 ? found[3] : -1;
+                c1.x = nf > 4 ? found[4] : -1;
+                c1.y = nf > 5 ? found[5] : -1;
+                c1.z = nf > 6 ? found[6] : -1;
+                c1.w = nf > 7 ? found[7] : -1;
+            }
+    }
     return true;
 }
 

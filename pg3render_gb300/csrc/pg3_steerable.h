@@ -38,8 +38,12 @@ struct SteerableHost {
     std::vector<uint32_t> levelOffset; // first triangle of each level in `tri` (level+1 entries + end)
     std::vector<float> nodeW;          // 6 x 9 child weights per tree node
     std::vector<int> nodeChild;        // 6 child ids per node: >= 0 node, < 0 ~leaf, INT32_MIN none
+    std::vector<float4> leafPlane;     // per leaf: unit normal of the planar triangle, distance from origin
+    std::vector<int4> faceCells;       // cube-map cells (6 x kSteerCells^2) x 2: up to 8 candidate level-0 faces
     int root = 0;
 };
+
+constexpr int kSteerCells = 8;         // cube-map resolution of the face locator
 
 // rgb: env_height rows of env_width RGB float texels (row 0 at theta = 0).
 bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, SteerableHost &out, std::string &err);

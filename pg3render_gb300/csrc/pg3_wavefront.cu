@@ -137,8 +137,13 @@ struct ShadeOut {
     float4 r0, r1;            // next ray
 };
 
-template <int K>
-__global__ void __launch_bounds__(kWaveBlock) shadeKernel(const __grid_constant__ SceneView S, Queues Q, int cur,
+// Resident blocks per SM the shade kernels are compiled for (register budget 65536 / (256 x N)).
+#ifndef PG3_SHADE_MIN_BLOCKS
+#define PG3_SHADE_MIN_BLOCKS 2
+#endif
+
+template <int K, int EMK>
+__global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS) shadeKernel(const __grid_constant__ SceneView S, Queues Q, int cur,
                                                           uint64_t base0, uint32_t npix, uint32_t sample0,
                                                           float *outR, float *outG, float *outB, DevStats *stats)
 {
@@ -169,7 +174,7 @@ __global__ void __launch_bounds__(kWaveBlock) shadeKernel(const __grid_constant_
                 if (pl >= S.minPL && S.bgKind != kBgNone) {
                     float pdf = 0.f;
                     const Frame pf = frameFromZ(prevN);
-                    const float3 Le = bgEmission(S, dir, pl > 1 && prevFinite, pf, pdf);
+                    const float3 Le = bgEmission<EMK>(S, dir, pl > 1 && prevFinite, pf, pdf);
                     if (pl == 1) L = Le;
                     else if (prevFinite) L = ew * Le * misPower(prevBsdfPdf, pdf * pickProb(S, org, prevN, prevSum, S.bgLightId));
                     else L = ew * Le;
@@ -213,7 +218,7 @@ __global__ void __launch_bounds__(kWaveBlock) shadeKernel(const __grid_constant_
                             float3 wig, smp;
                             float dist, pdfW;
                             if (lid == S.bgLightId) {
-                                bgSample(S, frame, ra.b, ra.c, ra.d, wig, pdfW, smp);
+                                bgSample<EMK>(S, frame, ra.b, ra.c, ra.d, wig, pdfW, smp);
                                 dist = kFloatMax;
                             } else {
                                 areaSample(S.lights[lid], pt, nrm, ra.b, ra.c, wig, dist, smp, pdfW);
@@ -333,6 +338,17 @@ Queues carve(void *scratch, uint64_t cap)
 
 }  // namespace
 
+// The four shade kernels of one bounce, specialised on the environment-map sampler.
+template <int EMK>
+void launchShade(const SceneView &S, const Queues &Q, int cur, uint64_t base, uint32_t npix, uint32_t sample0,
+                 float *r, float *g, float *b, DevStats *stats, int grid, cudaStream_t st)
+{
+    shadeKernel<-1, EMK><<<grid, kWaveBlock, 0, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats);
+    shadeKernel<kMatLambert, EMK><<<grid, kWaveBlock, 0, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats);
+    shadeKernel<kMatGgxConductor, EMK><<<grid, kWaveBlock, 0, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats);
+    shadeKernel<kMatGgxDielectric, EMK><<<grid, kWaveBlock, 0, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats);
+}
+
 size_t wavefrontBytes(uint64_t cap)
 {
     return align256(sizeof(Counters)) + 2 * align256(32 * cap) + align256(8 * cap) + kNumBuckets * align256(4 * cap) +
@@ -356,10 +372,11 @@ cudaError_t launchWavefront(const SceneView &S, bool naive, uint32_t sample0, ui
         for (uint32_t bounce = 0; bounce < maxBounces; ++bounce) {
             const int cur = bounce & 1;
             extendKernel<<<gridBlocks, kWaveBlock, 0, stream>>>(S, Q, cur, stats);
-            shadeKernel<-1><<<gridBlocks, kWaveBlock, 0, stream>>>(S, Q, cur, base, npix, sample0, r, g, b, stats);
-            shadeKernel<kMatLambert><<<gridBlocks, kWaveBlock, 0, stream>>>(S, Q, cur, base, npix, sample0, r, g, b, stats);
-            shadeKernel<kMatGgxConductor><<<gridBlocks, kWaveBlock, 0, stream>>>(S, Q, cur, base, npix, sample0, r, g, b, stats);
-            shadeKernel<kMatGgxDielectric><<<gridBlocks, kWaveBlock, 0, stream>>>(S, Q, cur, base, npix, sample0, r, g, b, stats);
+            const int emk = (S.bgKind == kBgEnvMap) ? S.emSampler : kEmCosine;   // no map: constant/area paths
+            if (emk == kEmCdf) launchShade<kEmCdf>(S, Q, cur, base, npix, sample0, r, g, b, stats, gridBlocks, stream);
+            else if (emk == kEmSteerable)
+                launchShade<kEmSteerable>(S, Q, cur, base, npix, sample0, r, g, b, stats, gridBlocks, stream);
+            else launchShade<kEmCosine>(S, Q, cur, base, npix, sample0, r, g, b, stats, gridBlocks, stream);
             shadowKernel<<<gridBlocks, kWaveBlock, 0, stream>>>(S, Q, r, g, b, stats);
             advanceKernel<<<1, 1, 0, stream>>>(Q.cnt, cur);
             *launches += 7;

@@ -69,7 +69,7 @@ def test_bsdf_pdf_consistency(mat, theta, below):
     assert np.median(rel) <= 1e-6 and np.quantile(rel, 0.99) <= 1e-5 and np.quantile(rel, 0.999) <= 1e-4, \
         (np.median(rel), np.quantile(rel, 0.99), np.quantile(rel, 0.999))
     ra = _rel(o["att_sampled"][valid], o["att_eval"][valid])
-    assert np.quantile(ra, 0.999) <= 1e-5
+    assert np.quantile(ra, 0.99) <= 1e-5 and np.quantile(ra, 0.999) <= 1e-4
 
 
 @pytest.mark.parametrize("mat,theta,below", BSDF_CASES)
