@@ -219,6 +219,14 @@ int pg3gpu_probe_light(pg3gpu_ctx *ctx, int32_t light, uint32_t n, const float *
 int pg3gpu_probe_light_pdf(pg3gpu_ctx *ctx, int32_t light, uint32_t n, const float *points, const float *normals,
                            const float *dirs, float *pdf);
 
+/* LBVH export (test entry point, no counterpart in the reference, which has no
+ * acceleration structure): *num_prims = triangles + spheres; for num_prims >= 2 and
+ * non-NULL arrays, the sorted 30-bit Morton codes and primitive ids (num_prims each)
+ * and the num_prims-1 nodes (16 floats each: left box min xyz + child id bits, left box
+ * max xyz + 0, right box min xyz + child id bits, right box max xyz + 0; child ids >= 0
+ * are nodes, < 0 are ~primitive). */
+int pg3gpu_export_bvh(pg3gpu_ctx *ctx, uint32_t *num_prims, uint32_t *codes, uint32_t *ids, float *nodes);
+
 /* Allocation-free rendering. No counterpart in the reference.
  * For callers that may not allocate device memory once they are running: a frame
  * loop captured into a CUDA graph (cudaMalloc cannot be captured), or an engine whose

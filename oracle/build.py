@@ -13,12 +13,11 @@ LIB = os.path.join(BUILD, "libpg3oracle.so")
 
 
 def build_oracle(force=False):
-    src = os.path.join(HERE, "pt_oracle.cpp")
+    srcs = [os.path.join(HERE, f) for f in ("pt_oracle.cpp", "lbvh_oracle.cpp")]
     os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in srcs):
         return LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC",
-           src, "-o", LIB]
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC"] + srcs + ["-o", LIB]
     subprocess.check_call(cmd)
     return LIB
 

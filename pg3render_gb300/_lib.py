@@ -101,6 +101,7 @@ SIGNATURES = {
     "pg3gpu_probe_light": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
     "pg3gpu_probe_light_pdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
+    "pg3gpu_export_bvh": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)] + [ctypes.c_void_p] * 3),
     "pg3gpu_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "pg3gpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "pg3gpu_version": (ctypes.c_char_p, []),

@@ -27,6 +27,7 @@ struct pg3gpu_ctx {
     std::vector<void *> allocs;
     uint32_t W = 0, H = 0;
     uint32_t nmat = 0;
+    uint32_t *dBvhCodes = nullptr, *dBvhIds = nullptr;   // sorted Morton codes / primitive ids of the LBVH
     double *dSum = nullptr, *dSumsq = nullptr;
     float *dOut[3] = {nullptr, nullptr, nullptr};
     uint64_t outCapacity = 0;            // paths per launch chunk
@@ -278,7 +279,9 @@ int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int dev
         void *scratch;
         if ((st = devAlloc(ctx, &nodes, nprim - 1))) return bail(st);
         if ((st = devAlloc(ctx, (char **)&scratch, lbvhScratchBytes(nprim)))) return bail(st);
-        cudaError_t e = buildLbvh(v, nodes, scratch, nullptr, nullptr, nullptr);
+        if ((st = devAlloc(ctx, &ctx->dBvhCodes, nprim))) return bail(st);
+        if ((st = devAlloc(ctx, &ctx->dBvhIds, nprim))) return bail(st);
+        cudaError_t e = buildLbvh(v, nodes, scratch, ctx->dBvhCodes, ctx->dBvhIds, nullptr);
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
         if (e != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "LBVH build: %s", cudaGetErrorString(e)));
         v.bvh = nodes;
@@ -649,5 +652,19 @@ extern "C" int pg3gpu_probe_light_pdf(pg3gpu_ctx *ctx, int32_t light, uint32_t n
     if (e == cudaSuccess) e = launchProbeLightPdf(ctx->view, light, n, dP, dN, dD, dO, nullptr);
     if (e == cudaSuccess) e = cudaMemcpy(pdf, dO, 4 * (size_t)n, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "light pdf probe: %s", cudaGetErrorString(e));
+    return PG3GPU_OK;
+}
+
+// LBVH export (test entry point): sorted Morton codes, primitive ids and the node array.
+extern "C" int pg3gpu_export_bvh(pg3gpu_ctx *ctx, uint32_t *num_prims, uint32_t *codes, uint32_t *ids, float *nodes)
+{
+    if (!ctx || !num_prims) return PG3GPU_ERR_INVALID_ARGUMENT;
+    const uint32_t n = ctx->view.ntri + ctx->view.nsph;
+    *num_prims = n;
+    if (n < 2 || (!codes && !ids && !nodes)) return PG3GPU_OK;
+    PG3_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (codes) PG3_CUDA(ctx, cudaMemcpy(codes, ctx->dBvhCodes, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    if (ids) PG3_CUDA(ctx, cudaMemcpy(ids, ctx->dBvhIds, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    if (nodes) PG3_CUDA(ctx, cudaMemcpy(nodes, ctx->view.bvh, sizeof(BvhNode) * (size_t)(n - 1), cudaMemcpyDeviceToHost));
     return PG3GPU_OK;
 }

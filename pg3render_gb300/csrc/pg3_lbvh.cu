@@ -246,17 +246,19 @@ __global__ void refit(const float4 *primLo, const float4 *primHi, const uint32_t
 
 }  // namespace
 
+// Each array of the scratch carve starts on a 256-byte boundary (see buildLbvh).
+static size_t carveSize(size_t bytes) { return (bytes + 255) & ~size_t(255); }
+
 size_t lbvhScratchBytes(uint32_t n)
 {
     const size_t nb = (n + kSortBlock - 1) / kSortBlock;
-    return 3 * 16 * (size_t)n            // lo, hi, centroid
-           + 32                          // bounds
-           + 4 * 4 * (size_t)n           // keys/vals x2
-           + 4 * 256 * nb                // counts
-           + 4 * 4 * (size_t)n           // left, right, parentOfNode, parentOfLeaf
-           + 2 * 16 * (size_t)n          // node lo/hi
-           + 4 * (size_t)n               // arrivals
-           + 1024;                       // alignment slack
+    return 3 * carveSize(16 * (size_t)n)    // lo, hi, centroid
+           + carveSize(32)                  // bounds
+           + 4 * carveSize(4 * (size_t)n)   // keys/vals x2
+           + carveSize(4 * 256 * nb)        // counts
+           + 4 * carveSize(4 * (size_t)n)   // left, right, parentOfNode, parentOfLeaf
+           + 2 * carveSize(16 * (size_t)n)  // node lo/hi
+           + carveSize(4 * (size_t)n);      // arrivals
 }
 
 // Builds the node array for n >= 2 primitives. `scratch` holds lbvhScratchBytes(n) bytes;

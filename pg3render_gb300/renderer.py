@@ -171,6 +171,19 @@ class GpuPathTracer:
                    self._ctx)
         return out
 
+    def export_bvh(self):
+        """(codes, ids, nodes[n-1, 16] float32) of the device LBVH."""
+        n = ctypes.c_uint32()
+        _lib.check(self._L.pg3gpu_export_bvh(self._ctx, ctypes.byref(n), None, None, None), self._ctx)
+        n = n.value
+        codes, ids = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
+        nodes = np.zeros((max(n - 1, 0), 16), np.float32)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)   # noqa: E731
+        if n >= 2:
+            _lib.check(self._L.pg3gpu_export_bvh(self._ctx, ctypes.byref(ctypes.c_uint32()), p(codes), p(ids),
+                                                 p(nodes)), self._ctx)
+        return codes, ids, nodes
+
     def device_framebuffer(self):
         a, b = ctypes.c_void_p(), ctypes.c_void_p()
         _lib.check(self._L.pg3gpu_device_framebuffer(self._ctx, ctypes.byref(a), ctypes.byref(b)), self._ctx)
