@@ -249,6 +249,53 @@ int pg3gpu_export_bvh(pg3gpu_ctx *ctx, uint32_t *num_prims, uint32_t *codes, uin
 int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp,
                                  double *sum_rgb, double *sumsq_rgb);
 
+/* ---- Batched rendering (no counterpart in the reference) ----------------------------
+ * Many scene instances, each with its own scene, options (algorithm 7 on the wavefront
+ * pipeline; the options' seed keys its random numbers) and samples per pixel, rendered by
+ * one persistent wavefront. Paths of all instances share `capacity` slots: a finished path
+ * adds its radiance to its instance's framebuffer and frees its slot, and when fewer than
+ * regen_threshold * capacity paths are active the free slots are refilled with camera paths
+ * of whichever instances have samples left. A run renders spp[i] samples of every instance i;
+ * with use_graph the whole run is one CUDA graph launch whose device-side loop (a conditional
+ * while node) ends when every path of every instance has finished. Instance i renders exactly
+ * the paths (and radiance per path) that a context created from scenes[i] and opts[i] renders
+ * for the same sample indices. All instances with an environment map must use the same
+ * environment-map sampler. At most PG3GPU_BATCH_MAX_INSTANCES instances. */
+#define PG3GPU_BATCH_MAX_INSTANCES 128u
+typedef struct pg3gpu_batch pg3gpu_batch;
+
+typedef struct pg3gpu_batch_tuning {
+    uint32_t capacity;        /* path slots (0: automatic; at most 2^24) */
+    uint32_t block_size;      /* threads per block of the stage kernels: 128 or 256 (0: 256) */
+    uint32_t blocks_per_sm;   /* persistent blocks per SM of the stage kernels (0: automatic) */
+    float regen_threshold;    /* refill when active paths < this fraction of capacity, in (0, 0.875] (0: 0.5) */
+    int32_t use_graph;        /* 1: one CUDA graph launch per run, 0: host-driven steps */
+    uint32_t reserved[3];
+} pg3gpu_batch_tuning;
+
+int pg3gpu_batch_create(const pg3gpu_scene *scenes, const pg3gpu_options *opts, const uint32_t *spp, uint32_t n,
+                        int device, pg3gpu_batch **out);
+int pg3gpu_batch_destroy(pg3gpu_batch *batch);
+int pg3gpu_batch_set_stream(pg3gpu_batch *batch, void *cuda_stream);
+int pg3gpu_batch_set_tuning(pg3gpu_batch *batch, const pg3gpu_batch_tuning *tuning);
+int pg3gpu_batch_get_tuning(pg3gpu_batch *batch, pg3gpu_batch_tuning *tuning);
+/* Renders one run (asynchronous): samples k*spp[i] .. (k+1)*spp[i]-1 of instance i on the k-th run. */
+int pg3gpu_batch_run(pg3gpu_batch *batch);
+/* Waits for the batch's stream; PG3GPU_ERR_DEVICE_LIMIT if a device-side limit was hit. */
+int pg3gpu_batch_synchronize(pg3gpu_batch *batch);
+/* Mean (and per-pixel variance of the mean's samples) of instance `instance`, as pg3gpu_read_framebuffer. */
+int pg3gpu_batch_read_framebuffer(pg3gpu_batch *batch, uint32_t instance, double *mean_rgb, double *var_rgb,
+                                  uint64_t *spp);
+int pg3gpu_batch_clear(pg3gpu_batch *batch);
+/* Autotuner: times up to max_trials runs over capacities, refill thresholds and block shapes
+ * (coordinate descent, graph launches), keeps the fastest tuning and writes it to *chosen
+ * (may be NULL). The trial runs are cleared from the framebuffers afterwards. */
+int pg3gpu_batch_autotune(pg3gpu_batch *batch, uint32_t max_trials, pg3gpu_batch_tuning *chosen);
+/* Counters over all runs since creation: paths, rays, termination reasons, kernel launches;
+ * last_iteration_ms is the device time of the last run (valid after a synchronize). */
+int pg3gpu_batch_get_stats(pg3gpu_batch *batch, pg3gpu_stats *stats);
+const char *pg3gpu_batch_last_error(const pg3gpu_batch *batch);
+
 /* Text of the last error of this context (or of the last failed create when ctx is NULL). */
 const char *pg3gpu_last_error(const pg3gpu_ctx *ctx);
 const char *pg3gpu_status_string(int status);

@@ -76,6 +76,13 @@ class Stats(ctypes.Structure):
                 ("path_kernel_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
 
 
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("capacity", ctypes.c_uint32), ("block_size", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("regen_threshold", ctypes.c_float), ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_uint32 * 3)]
+
+
+BATCH_MAX_INSTANCES = 128
+
 # every exported symbol, with its ctypes signature (checked against include/pg3gpu.h by the tests)
 SIGNATURES = {
     "pg3gpu_default_options": (None, [ctypes.POINTER(Options)]),
@@ -102,6 +109,21 @@ SIGNATURES = {
                                           ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
     "pg3gpu_probe_light_pdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
     "pg3gpu_export_bvh": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)] + [ctypes.c_void_p] * 3),
+    "pg3gpu_batch_create": (ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(Options),
+                                           ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "pg3gpu_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg3gpu_batch_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pg3gpu_batch_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchTuning)]),
+    "pg3gpu_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchTuning)]),
+    "pg3gpu_batch_run": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg3gpu_batch_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg3gpu_batch_read_framebuffer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                                     ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "pg3gpu_batch_clear": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg3gpu_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(BatchTuning)]),
+    "pg3gpu_batch_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "pg3gpu_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "pg3gpu_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "pg3gpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "pg3gpu_version": (ctypes.c_char_p, []),

@@ -13,42 +13,12 @@
 #include <cuda_runtime.h>
 
 #include "../../include/pg3gpu.h"
+#include "pg3_ctx.h"
 #include "pg3_host.h"
 #include "pg3_kernels.h"
 #include "pg3_scene_view.h"
 
 using namespace pg3;
-
-struct pg3gpu_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    pg3gpu_options opts{};
-    SceneView view{};
-    std::vector<void *> allocs;
-    uint32_t W = 0, H = 0;
-    uint32_t nmat = 0;
-    uint32_t *dBvhCodes = nullptr, *dBvhIds = nullptr;   // sorted Morton codes / primitive ids of the LBVH
-    double *dSum = nullptr, *dSumsq = nullptr;
-    float *dOut[3] = {nullptr, nullptr, nullptr};
-    uint64_t outCapacity = 0;            // paths per launch chunk
-    void *dWave = nullptr;               // wavefront queues
-    uint64_t waveCapacity = 0;
-    DevStats *dStats = nullptr;
-    unsigned int *dErr = nullptr;
-    uint64_t iterations = 0;
-    int megaGrid = 0, waveGrid = 0;
-    bool useWavefront = false;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    bool timed = false;
-    // per-launch timing of the path kernel: event pairs recorded around each launch,
-    // folded into kernelMs when the stream is synchronised
-    static constexpr int kTimerSlots = 64;
-    cudaEvent_t tStart[kTimerSlots] = {}, tStop[kTimerSlots] = {};
-    int pendingTimers = 0;
-    double kernelMs = 0.0;
-    uint64_t kernelLaunches = 0, allLaunches = 0;
-    std::string lastError;
-};
 
 namespace {
 
@@ -65,6 +35,12 @@ int fail(pg3gpu_ctx *ctx, int status, const char *fmt, ...)
     else g_createError = buf;
     return status;
 }
+
+}  // namespace
+
+int pg3::ctxError(pg3gpu_ctx *ctx, int status, const std::string &msg) { return fail(ctx, status, "%s", msg.c_str()); }
+
+namespace {
 
 #define PG3_CUDA(ctx, call)                                                                          \
     do {                                                                                             \
@@ -213,7 +189,11 @@ int pg3gpu_destroy(pg3gpu_ctx *ctx)
     return PG3GPU_OK;
 }
 
-int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, pg3gpu_ctx **out)
+}  // extern "C"
+
+// forBatch: a scene instance of a batch (pg3_batch.cu) -- no launch queues, outputs or timers
+int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, bool forBatch,
+                       pg3gpu_ctx **out)
 {
     if (!out) return fail(nullptr, PG3GPU_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
@@ -306,23 +286,32 @@ int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int dev
     // the wavefront pipeline is the default for the NEE path tracer (3x the megakernel on the
     // benchmark scenes); the BSDF-only tracer always runs as a megakernel
     ctx->useWavefront = (opts->pipeline == PG3GPU_PIPELINE_WAVEFRONT || opts->pipeline == PG3GPU_PIPELINE_AUTO);
-    if (ctx->useWavefront) {
+    ctx->waveGrid = sms * 4;
+    if (ctx->useWavefront && !forBatch) {
         const uint64_t npix = (uint64_t)ctx->W * ctx->H;
         const uint64_t cap = opts->max_paths_in_flight ? opts->max_paths_in_flight : (1ull << 22);
         ctx->waveCapacity = std::min<uint64_t>(cap, std::max<uint64_t>(1ull << 16, npix * 16));
         void *w;
-        if ((st = devAlloc(ctx, (char **)&w, wavefrontBytes(ctx->waveCapacity)))) return bail(st);
+        if ((st = devAlloc(ctx, (char **)&w, wavefrontBytes(ctx->waveCapacity, false)))) return bail(st);
         ctx->dWave = w;
-        ctx->waveGrid = sms * 4;
     }
-    if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
-        return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));
-    for (int i = 0; i < pg3gpu_ctx::kTimerSlots; ++i)
-        if (cudaEventCreate(&ctx->tStart[i]) != cudaSuccess || cudaEventCreate(&ctx->tStop[i]) != cudaSuccess)
+    if (!forBatch) {
+        if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
             return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));
+        for (int i = 0; i < pg3gpu_ctx::kTimerSlots; ++i)
+            if (cudaEventCreate(&ctx->tStart[i]) != cudaSuccess || cudaEventCreate(&ctx->tStop[i]) != cudaSuccess)
+                return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));
+    }
     if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "setup sync"));
     *out = ctx;
     return PG3GPU_OK;
+}
+
+extern "C" {
+
+int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, pg3gpu_ctx **out)
+{
+    return createContext(scene, opts, device, false, out);
 }
 
 int pg3gpu_set_stream(pg3gpu_ctx *ctx, void *stream)

@@ -1,0 +1,93 @@
+// Internal: the context behind the opaque pg3gpu_ctx handle of include/pg3gpu.h, shared by
+// the translation units of the C ABI (pg3_api.cu, pg3_diff.cu, pg3_batch.cu).
+#pragma once
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pg3gpu.h"
+#include "pg3_scene_view.h"
+
+struct pg3gpu_ctx {
+    using SceneView = pg3::SceneView;
+    using DevStats = pg3::DevStats;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    pg3gpu_options opts{};
+    SceneView view{};
+    std::vector<void *> allocs;
+    uint32_t W = 0, H = 0;
+    uint32_t nmat = 0;
+    uint32_t *dBvhCodes = nullptr, *dBvhIds = nullptr;   // sorted Morton codes / primitive ids of the LBVH
+    double *dSum = nullptr, *dSumsq = nullptr;
+    float *dOut[3] = {nullptr, nullptr, nullptr};
+    uint64_t outCapacity = 0;            // paths per launch chunk
+    void *dWave = nullptr;               // wavefront queues
+    uint64_t waveCapacity = 0;
+    DevStats *dStats = nullptr;
+    unsigned int *dErr = nullptr;
+    uint64_t iterations = 0;
+    int megaGrid = 0, waveGrid = 0;
+    bool useWavefront = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    // per-launch timing of the path kernel: event pairs recorded around each launch,
+    // folded into kernelMs when the stream is synchronised
+    static constexpr int kTimerSlots = 64;
+    cudaEvent_t tStart[kTimerSlots] = {}, tStop[kTimerSlots] = {};
+    int pendingTimers = 0;
+    double kernelMs = 0.0;
+    uint64_t kernelLaunches = 0, allLaunches = 0;
+    std::string lastError;
+
+    // differentiable rendering (pg3_diff.cu)
+    float *dTot[3] = {nullptr, nullptr, nullptr};   // primal radiance of every path of the last forward
+    float *dAdj[3] = {nullptr, nullptr, nullptr};   // radiance accumulators of the adjoint replay
+    uint64_t totCapacity = 0;
+    void *dWaveGrad = nullptr;                      // queues with gradient records
+    uint64_t waveGradCapacity = 0;
+    float *dRowInt = nullptr;                       // environment-map CDF build: per-row integrals
+    uint32_t diffIteration = 0, diffSpp = 0;        // samples the stored radiance belongs to
+    bool diffValid = false;
+};
+
+namespace pg3 {
+
+// Records msg as the context's last error (or the thread's create error when ctx is null)
+// and returns status.
+int ctxError(pg3gpu_ctx *ctx, int status, const std::string &msg);
+
+// pg3gpu_create; forBatch leaves out the launch queues, per-path outputs and timers.
+int createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, bool forBatch,
+                  pg3gpu_ctx **out);
+
+inline int cudaStatus(pg3gpu_ctx *ctx, cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return PG3GPU_OK;
+    return ctxError(ctx, e == cudaErrorMemoryAllocation ? PG3GPU_ERR_OUT_OF_MEMORY : PG3GPU_ERR_CUDA,
+                    std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Device allocation owned by the context (freed by pg3gpu_destroy).
+template <typename T>
+int ctxAlloc(pg3gpu_ctx *ctx, T **p, size_t count)
+{
+    void *q = nullptr;
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    if (int st = cudaStatus(ctx, cudaMalloc(&q, bytes), "cudaMalloc")) return st;
+    ctx->allocs.push_back(q);
+    *p = reinterpret_cast<T *>(q);
+    return PG3GPU_OK;
+}
+
+inline void ctxFree(pg3gpu_ctx *ctx, void *p)
+{
+    if (!p) return;
+    cudaFree(p);
+    ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), p), ctx->allocs.end());
+}
+
+}  // namespace pg3

@@ -323,6 +323,7 @@ struct BsdfRec {
     float3 att;
     float pdfW;
     float compProb;
+    float dAtt;   // with derivatives requested: Lambert d att_c / d albedo_c, GGX d ln att / d alpha
 };
 PG3_DI bool isBlocker(const BsdfRec &r) { return maxc(r.att) * fabsf(r.wil.z) <= 1e-5f; }   // :63-67
 
@@ -335,14 +336,26 @@ PG3_DI float3 condEval(const DevMaterial &m, float3 wil, float3 wol, float3 h, f
     const float G = smithG1(wil, h, m.alpha) * smithG1(wol, h, m.alpha);
     return f3((F * G * D) / (4.0f * wil.z * wol.z));
 }
-PG3_DI float condPdf(const DevMaterial &m, float3 wol, float3 h, float D)
+// pdfs and sampling use the sampling roughness alphaS (equal to alpha unless derivatives are
+// checked with the sampling held fixed); Dp is D evaluated with alphaS
+PG3_DI float condPdf(const DevMaterial &m, float3 wol, float3 h, float Dp)
 {
     if (wol.z < 0.f) return 0.0f;
-    return ggxPdfVisibleNormals(wol, h, D, m.alpha) * reflectionJacobian(wol, h);
+    return ggxPdfVisibleNormals(wol, h, Dp, m.alphaS) * reflectionJacobian(wol, h);
 }
+// d ln(D(m) G1(wi, m) G1(wo, m)) / d alpha, from ggxD and smithG1 above:
+// d ln D / da = 2/a - 4a / (a^2 + tan^2 m),  d ln G1(v) / da = -a tan^2 v / (s (1 + s)), s = sqrt(1 + a^2 tan^2 v)
+PG3_DI float ggxDlnDGda(float3 wi, float3 wo, float3 m, float a)
+{
+    const float a2 = a * a;
+    const float ti = tanThetaSqr(wi), to = tanThetaSqr(wo);
+    const float si = sqrtf(1.f + a2 * ti), so = sqrtf(1.f + a2 * to);
+    return 2.f / a - 4.f * a / (a2 + tanThetaSqr(m)) - a * ti / (si * (1.f + si)) - a * to / (so * (1.f + so));
+}
+PG3_DI float ggxDp(const DevMaterial &m, float3 h, float D) { return (m.alphaS == m.alpha) ? D : ggxD(h, m.alphaS); }
 
 // GGX dielectric: src/materials.hxx:1123-1266 (directions already switched to the wo side)
-struct DielCtx { float3 wo, wi, m; bool refl; float etaS, etaInvS, F, D; };
+struct DielCtx { float3 wo, wi, m; bool refl; float etaS, etaInvS, F, D, Dp; };
 PG3_DI float3 dielEval(const DevMaterial &mt, const DielCtx &c)
 {
     const float ci = fabsf(c.wi.z), co = fabsf(c.wo.z);
@@ -362,27 +375,31 @@ PG3_DI float3 dielEval(const DevMaterial &mt, const DielCtx &c)
 PG3_DI float dielPdf(const DevMaterial &mt, const DielCtx &c)
 {
     if (c.wo.z < 0.f) return 0.0f;
-    const float vn = ggxPdfVisibleNormals(c.wo, c.m, c.D, mt.alpha);
+    const float vn = ggxPdfVisibleNormals(c.wo, c.m, c.Dp, mt.alphaS);
     const float J = c.refl ? reflectionJacobian(c.wi, c.m) : refractionJacobian(c.wo, c.wi, c.m, c.etaInvS);
     return vn * J * (c.refl ? c.F : (1.f - c.F));
 }
 
 // EvalBsdf + GetOptData(kOptSamplingProbs) per material kind: :277-283 (Lambert),
 // :809-817 (conductor), :1023-1031 with InitEvalContext :1123-1160 (dielectric)
-template <int K>
+// DA: also compute BsdfRec::dAtt
+template <int K, bool DA = false>
 PG3_DI void evalBsdfK(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
 {
     r.wil = wil;
     r.compProb = 1.f;
     if (K == kMatLambert) {
-        r.att = (wil.z <= 0.f || wol.z <= 0.f) ? f3(0.f) : make_float3(m.r, m.g, m.b) * kPiInvF;
+        const bool valid = !(wil.z <= 0.f || wol.z <= 0.f);
+        r.att = valid ? make_float3(m.r, m.g, m.b) * kPiInvF : f3(0.f);
         r.pdfW = cosHemispherePdf(wil.z);
+        if (DA) r.dAtt = valid ? kPiInvF : 0.f;
     } else if (K == kMatGgxConductor) {
         const float3 h = halfwayReflection(wil, wol);
         const float D = ggxD(h, m.alpha);
         const float F = fresnelConductor(dot(h, wol), m.eta, m.absorb);
         r.att = condEval(m, wil, wol, h, F, D);
-        r.pdfW = condPdf(m, wol, h, D);
+        r.pdfW = condPdf(m, wol, h, ggxDp(m, h, D));
+        if (DA) r.dAtt = ggxDlnDGda(wil, wol, h, m.alpha);
     } else {
         DielCtx c;
         const bool below = wol.z < 0.f;
@@ -394,9 +411,11 @@ PG3_DI void evalBsdfK(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
         c.etaInvS = below ? m.eta : m.etaInv;
         c.m = c.refl ? halfwayReflection(c.wi, c.wo) : halfwayRefraction(c.wi, c.wo, c.etaInvS);
         c.D = ggxD(c.m, m.alpha);
+        c.Dp = ggxDp(m, c.m, c.D);
         c.F = fresnelDielectric(dot(c.m, c.wo), c.etaS);
         r.att = dielEval(m, c);
         r.pdfW = dielPdf(m, c);
+        if (DA) r.dAtt = ggxDlnDGda(c.wi, c.wo, c.m, m.alpha);
     }
 }
 PG3_DI void evalBsdf(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
@@ -407,21 +426,24 @@ PG3_DI void evalBsdf(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
 }
 
 // SampleBsdf per material kind: :285-292 (Lambert), :819-851 (conductor), :1033-1100 (dielectric)
-template <int K>
+template <int K, bool DA = false>
 PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, float u2, BsdfRec &r)
 {
     r.compProb = 1.f;
     if (K == kMatLambert) {
         r.wil = sampleCosHemisphere(u0, u1, r.pdfW);
-        r.att = (r.wil.z <= 0.f || wol.z <= 0.f) ? f3(0.f) : make_float3(m.r, m.g, m.b) * kPiInvF;
+        const bool valid = !(r.wil.z <= 0.f || wol.z <= 0.f);
+        r.att = valid ? make_float3(m.r, m.g, m.b) * kPiInvF : f3(0.f);
+        if (DA) r.dAtt = valid ? kPiInvF : 0.f;
     } else if (K == kMatGgxConductor) {
-        const float3 h = sampleGgxVndf(wol, m.alpha, u0, u1, m.vndfExact != 0);
+        const float3 h = sampleGgxVndf(wol, m.alphaS, u0, u1, m.vndfExact != 0);
         const float D = ggxD(h, m.alpha);
         bool above;
         r.wil = reflect(above, wol, h);
         const float F = fresnelConductor(dot(h, wol), m.eta, m.absorb);
-        r.pdfW = condPdf(m, wol, h, D);
+        r.pdfW = condPdf(m, wol, h, ggxDp(m, h, D));
         r.att = (!above || r.wil.z < 0.0f) ? f3(0.f) : condEval(m, r.wil, wol, h, F, D);
+        if (DA) r.dAtt = ggxDlnDGda(r.wil, wol, h, m.alpha);
     } else {
         DielCtx c;
         const bool below = wol.z < 0.f;
@@ -429,8 +451,9 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         c.wo = wol * s;
         c.etaS = below ? m.etaInv : m.eta;
         c.etaInvS = below ? m.eta : m.etaInv;
-        c.m = sampleGgxVndf(c.wo, m.alpha, u0, u1, m.vndfExact != 0);
+        c.m = sampleGgxVndf(c.wo, m.alphaS, u0, u1, m.vndfExact != 0);
         c.D = ggxD(c.m, m.alpha);
+        c.Dp = ggxDp(m, c.m, c.D);
         c.F = fresnelDielectric(dot(c.m, c.wo), c.etaS);
         bool above;
         float cosAbs;
@@ -446,6 +469,7 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         r.wil = c.wi * s;
         r.pdfW = dielPdf(m, c);
         r.att = (!above || cosAbs < 0.0f) ? f3(0.f) : dielEval(m, c);
+        if (DA) r.dAtt = ggxDlnDGda(c.wi, c.wo, c.m, m.alpha);
     }
 }
 PG3_DI void sampleBsdf(const DevMaterial &m, float3 wol, float u0, float u1, float u2, BsdfRec &r)

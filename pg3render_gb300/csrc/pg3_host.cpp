@@ -129,6 +129,7 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         d.kind = m.kind;
         d.r = m.albedo[0]; d.g = m.albedo[1]; d.b = m.albedo[2];
         d.alpha = std::min(std::max(m.alpha, 0.001f), 1.0f);
+        d.alphaS = d.alpha;
         d.eta = 1.f; d.etaInv = 1.f;
         if (m.kind == PG3GPU_MAT_LAMBERT) {
             if (!finite3(m.albedo) || m.albedo[0] < 0.f || m.albedo[1] < 0.f || m.albedo[2] < 0.f)

@@ -25,10 +25,12 @@ cudaError_t buildLbvh(const SceneView &S, BvhNode *nodes, void *scratch, uint32_
                       uint32_t *sortedIdsOut, cudaStream_t stream);
 
 // pg3_wavefront.cu
-size_t wavefrontBytes(uint64_t capacity);
+// grad: null renders; otherwise a primal replay (grad->adjoint == 0) or the adjoint pass
+size_t wavefrontBytes(uint64_t capacity, bool grad);
 cudaError_t launchWavefront(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch,
-                            uint64_t capacity, int gridBlocks, cudaStream_t stream, uint64_t *launches);
+                            uint64_t capacity, int gridBlocks, cudaStream_t stream, uint64_t *launches,
+                            const GradArgs *grad = nullptr);
 
 // pg3_probe.cu (sampler probes for tests)
 cudaError_t launchProbeBsdf(const SceneView &S, int mat, uint32_t n, const float *wol, uint32_t seed, float *wil,

@@ -25,7 +25,7 @@ struct DevMaterial {          // 48 bytes
     float rrProb;             // Russian-roulette continuation probability (clamped to 0.997)
     int zeroRefl;             // Lambert with zero reflectance: paths end here (lights)
     int vndfExact;            // GGX: exact visible-normal sampling (1) or the reference's fitted routine (0)
-    int pad1;
+    float alphaS;             // GGX roughness the sampling routines and pdfs use (normally == alpha)
 };
 
 struct DevAreaLight {         // 64 bytes; radiance rides in the w lanes
@@ -115,6 +115,16 @@ struct DevStats {
     unsigned long long byBlocker;
     unsigned long long byMax;
     unsigned long long bySafety;
+};
+
+// Adjoint inputs and outputs of one path-replay launch (pg3_wave.cuh).
+struct GradArgs {
+    const float *dLdI;        // dLoss / d(mean image), rgb per pixel
+    float invSpp;             // the mean image is the sum of the samples / spp
+    const float *totR, *totG, *totB;   // primal radiance of each path (indexed like the output buffers)
+    float *gMat;              // per material: d/d albedo rgb, d/d roughness
+    float *gEm;               // per environment-map texel: rgb
+    int adjoint;              // 0: primal replay (radiance only), 1: adjoint
 };
 
 enum : unsigned int { kErrTraversalStack = 1u, kErrQueueOverflow = 2u, kErrSteerDescent = 4u };

@@ -207,6 +207,94 @@ class GpuPathTracer:
         self.close()
 
 
+class GpuBatch:
+    """Many scene instances rendered by one persistent wavefront (pg3gpu_batch_* of the C ABI).
+
+    ``configs`` are Config objects (one scene each; ``seeds`` optionally overrides their seeds)
+    and ``spp`` the samples per pixel of each instance per run. No counterpart in the reference.
+    """
+
+    def __init__(self, configs, spp, seeds=None, device=0):
+        n = len(configs)
+        self._L = _lib.load()
+        self._descs = [_lib.scene_desc(c.scene) for c in configs]
+        descs = (_lib.SceneDesc * n)(*self._descs)
+        opts = (_lib.Options * n)(*[c.options(None if seeds is None else seeds[i]) for i, c in enumerate(configs)])
+        self._keep = (descs, opts)
+        spps = (ctypes.c_uint32 * n)(*[int(x) for x in spp])
+        h = ctypes.c_void_p()
+        st = self._L.pg3gpu_batch_create(descs, opts, spps, n, device, ctypes.byref(h))
+        if st:
+            raise Pg3Error(st, self._L.pg3gpu_batch_last_error(None).decode(errors="replace"))
+        self._b = h
+        self.sizes = [(c.scene.camera.height, c.scene.camera.width) for c in configs]
+        self.spp = list(spp)
+
+    def _check(self, st):
+        if st:
+            raise Pg3Error(st, self._L.pg3gpu_batch_last_error(self._b).decode(errors="replace"))
+
+    def run(self):
+        self._check(self._L.pg3gpu_batch_run(self._b))
+
+    def synchronize(self):
+        self._check(self._L.pg3gpu_batch_synchronize(self._b))
+
+    def clear(self):
+        self._check(self._L.pg3gpu_batch_clear(self._b))
+
+    def framebuffer(self, i, with_variance=False):
+        h, w = self.sizes[i]
+        mean = np.zeros(h * w * 3, np.float64)
+        var = np.zeros(h * w * 3, np.float64) if with_variance else None
+        it = ctypes.c_uint64()
+        self._check(self._L.pg3gpu_batch_read_framebuffer(
+            self._b, i, mean.ctypes.data_as(ctypes.c_void_p),
+            var.ctypes.data_as(ctypes.c_void_p) if var is not None else None, ctypes.byref(it)))
+        return mean.reshape(h, w, 3), (var.reshape(h, w, 3) if var is not None else None), int(it.value)
+
+    def tuning(self):
+        t = _lib.BatchTuning()
+        self._check(self._L.pg3gpu_batch_get_tuning(self._b, ctypes.byref(t)))
+        return dict(capacity=t.capacity, block_size=t.block_size, blocks_per_sm=t.blocks_per_sm,
+                    regen_threshold=t.regen_threshold, use_graph=t.use_graph)
+
+    def set_tuning(self, capacity=0, block_size=0, blocks_per_sm=0, regen_threshold=0.0, use_graph=1):
+        t = _lib.BatchTuning(capacity, block_size, blocks_per_sm, regen_threshold, use_graph)
+        self._check(self._L.pg3gpu_batch_set_tuning(self._b, ctypes.byref(t)))
+
+    def autotune(self, max_trials=16):
+        t = _lib.BatchTuning()
+        self._check(self._L.pg3gpu_batch_autotune(self._b, max_trials, ctypes.byref(t)))
+        return self.tuning()
+
+    def stats(self):
+        s = _lib.Stats()
+        self._check(self._L.pg3gpu_batch_get_stats(self._b, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+
+    def set_stream(self, stream):
+        ptr = stream if isinstance(stream, int) else getattr(stream, "cuda_stream", stream)
+        self._check(self._L.pg3gpu_batch_set_stream(self._b, ctypes.c_void_p(ptr)))
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._L.pg3gpu_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 def render(config: Config, spp=None, seed=None, device=0):
     """Convenience: renders config.iterations (or spp) samples and returns the mean image."""
     with GpuPathTracer(config, seed=seed, device=device) as r:
