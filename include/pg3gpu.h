@@ -249,6 +249,40 @@ int pg3gpu_export_bvh(pg3gpu_ctx *ctx, uint32_t *num_prims, uint32_t *codes, uin
 int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp,
                                  double *sum_rgb, double *sumsq_rgb);
 
+/* ---- Differentiable rendering (no counterpart in the reference) ----------------------
+ * Path-replay backpropagation (Vicini, Speierer and Jakob, SIGGRAPH 2021) on the wavefront
+ * pipeline of algorithm 7. pg3gpu_diff_forward renders samples iteration..iteration+spp-1 of
+ * the current parameters, writes their mean image and keeps each path's radiance (12 bytes
+ * per path). pg3gpu_diff_adjoint then re-traces the same paths from their random-number keys
+ * (no path vertices are stored) and ADDS dLoss/dparameters to the caller's gradient arrays,
+ * given dLoss/dimage. Sampling (directions, pdfs, MIS weights, roulette) is treated as
+ * constant ("detached"). Differentiable parameters, in the layouts below:
+ *   materials: 4 floats per material -- Lambert: albedo rgb, w unused; GGX: xyz unused,
+ *              w = roughness alpha (derivative with respect to the clamped alpha),
+ *   environment map: env_height x env_width x 3 texels (rgb, the scene's layout).
+ * Not for algorithm 6, the megakernel pipeline or scenes with more than 2048 materials.
+ * All device pointers are stream-ordered on the context's stream: the calls allocate only on
+ * their first use (or when spp grows), so after one warm-up call they can be captured into a
+ * CUDA graph together with the caller's loss and optimiser. */
+#define PG3GPU_PARAMS_DEVICE 1u          /* pointers are device memory (else host memory) */
+#define PG3GPU_PARAMS_KEEP_SAMPLING 2u   /* keep the sampling data (roulette probabilities, GGX sampling
+                                            roughness, environment-map CDF) of the current parameters */
+/* Replaces the parameters; either pointer may be NULL. Clamps albedo to >= 0, alpha to
+ * [0.001, 1] and texels to >= 0. Unless KEEP_SAMPLING, the sampling data follow the new
+ * values: the environment-map CDF is rebuilt on the device (CDF and cosine samplers; the
+ * steerable sampler's tables are built on the host at create time, so it needs KEEP_SAMPLING
+ * when texels change). */
+int pg3gpu_set_params(pg3gpu_ctx *ctx, const float *material_params, const float *env_texels, uint32_t flags);
+/* Current parameters into host arrays (either may be NULL). */
+int pg3gpu_get_params(pg3gpu_ctx *ctx, float *material_params, float *env_texels);
+/* image: width x height x 3 floats (device memory), the mean of the spp samples. The
+ * context's framebuffer is not touched. */
+int pg3gpu_diff_forward(pg3gpu_ctx *ctx, uint32_t iteration, uint32_t spp, float *image);
+/* dloss_dimage: width x height x 3 (device); grad_materials: num_materials x 4 (device, added
+ * to); grad_env: env_height x env_width x 3 (device, added to; NULL skips the map). Replays the
+ * paths of the last pg3gpu_diff_forward, whose parameters must still be current. */
+int pg3gpu_diff_adjoint(pg3gpu_ctx *ctx, const float *dloss_dimage, float *grad_materials, float *grad_env);
+
 /* ---- Batched rendering (no counterpart in the reference) ----------------------------
  * Many scene instances, each with its own scene, options (algorithm 7 on the wavefront
  * pipeline; the options' seed keys its random numbers) and samples per pixel, rendered by

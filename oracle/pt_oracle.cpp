@@ -417,6 +417,11 @@ struct Material {
     int kind = kLambert;
     V3 reflectance;
     float alpha = 0.1f, eta = 1.f, etaInv = 1.f, absorb = 0.f;
+    // Sampling overrides (not in the reference): the GGX roughness that sampling and pdfs use and
+    // the roulette continuation probability, for finite differences that hold sampling fixed
+    // while the BSDF value changes. Negative: follow alpha / the reflectance.
+    float alphaSample = -1.f, rrOverride = -1.f;
+    float AlphaS() const { return alphaSample >= 0.f ? alphaSample : alpha; }
 
     // src/materials.hxx:262-266, 791-806, 996-1021
     static Material Lambert(V3 r) { Material m; m.kind = kLambert; m.reflectance = r; return m; }
@@ -443,13 +448,14 @@ struct Material {
 
     float RRContinuationProb() const  // :300-319, 853-858, 1102-1108
     {
+        if (rrOverride >= 0.f) return rrOverride;
         if (kind != kLambert) return 1.0f;
         const float p = 0.15f * Luminance(reflectance) + 0.85f * MaxC(reflectance);
         return Clampf(p, 0.f, 1.f);
     }
 
     // ---- GGX conductor helpers (src/materials.hxx:878-989)
-    struct CondCtx { V3 wol, wil, m; float F, D; };
+    struct CondCtx { V3 wol, wil, m; float F, D, Dp; };   // Dp: D of the sampling roughness
     V3 CondEval(const CondCtx &c) const
     {
         if (c.wil.z <= 0.f || c.wol.z <= 0.f || IsTiny(4.0f * c.wil.z * c.wol.z)) return V3(0.f);
@@ -460,11 +466,11 @@ struct Material {
     float CondPdf(const CondCtx &c) const
     {
         if (c.wol.z < 0.f) return 0.0f;
-        return GgxPdfVisibleNormals(c.wol, c.m, c.D, alpha) * ReflectionJacobian(c.wol, c.m);
+        return GgxPdfVisibleNormals(c.wol, c.m, c.Dp, AlphaS()) * ReflectionJacobian(c.wol, c.m);
     }
 
     // ---- GGX dielectric helpers (src/materials.hxx:1123-1266)
-    struct DielCtx { V3 wo, wi, m; bool below, refl; float etaS, etaInvS, F, D; };
+    struct DielCtx { V3 wo, wi, m; bool below, refl; float etaS, etaInvS, F, D, Dp; };
     V3 DielEval(const DielCtx &c) const
     {
         const float ci = std::fabs(c.wi.z), co = std::fabs(c.wo.z);
@@ -484,7 +490,7 @@ struct Material {
     float DielPdf(const DielCtx &c) const
     {
         if (c.wo.z < 0.f) return 0.0f;
-        const float vn = GgxPdfVisibleNormals(c.wo, c.m, c.D, alpha);
+        const float vn = GgxPdfVisibleNormals(c.wo, c.m, c.Dp, AlphaS());
         const float J = c.refl ? ReflectionJacobian(c.wi, c.m)
                                : RefractionJacobian(c.wo, c.wi, c.m, c.etaInvS);
         const float comp = c.refl ? c.F : (1.f - c.F);
@@ -502,6 +508,7 @@ struct Material {
         c.etaInvS = c.below ? eta : etaInv;
         c.m = c.refl ? HalfwayReflection(c.wi, c.wo) : HalfwayRefraction(c.wi, c.wo, c.etaInvS);
         c.D = DistributionGgx(c.m, alpha);
+        c.Dp = DistributionGgx(c.m, AlphaS());
         c.F = FresnelDielectric(Dot(c.m, c.wo), c.etaS);
         return c;
     }
@@ -518,6 +525,7 @@ struct Material {
             c.wol = r.wol; c.wil = r.wil;
             c.m = HalfwayReflection(c.wil, c.wol);
             c.D = DistributionGgx(c.m, alpha);
+            c.Dp = DistributionGgx(c.m, AlphaS());
             c.F = FresnelConductor(Dot(c.m, c.wol), eta, absorb);
             r.attenuation = CondEval(c);
             r.compProb = 1.0f;
@@ -540,8 +548,9 @@ struct Material {
         } else if (kind == kGgxConductor) {
             CondCtx c;
             c.wol = r.wol;
-            c.m = SampleVndf(c.wol, alpha, u[0], u[1]);
+            c.m = SampleVndf(c.wol, AlphaS(), u[0], u[1]);
             c.D = DistributionGgx(c.m, alpha);
+            c.Dp = DistributionGgx(c.m, AlphaS());
             bool above;
             c.wil = Reflect(above, c.wol, c.m);
             r.wil = c.wil;
@@ -557,8 +566,9 @@ struct Material {
             c.wo = r.wol * s;
             c.etaS = c.below ? etaInv : eta;
             c.etaInvS = c.below ? eta : etaInv;
-            c.m = SampleVndf(c.wo, alpha, u[0], u[1]);
+            c.m = SampleVndf(c.wo, AlphaS(), u[0], u[1]);
             c.D = DistributionGgx(c.m, alpha);
+            c.Dp = DistributionGgx(c.m, AlphaS());
             c.F = FresnelDielectric(Dot(c.m, c.wo), c.etaS);
             bool above;
             float cosAbs;
@@ -1146,6 +1156,8 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
     std::istringstream in(text);
     std::string line;
     std::vector<std::pair<int, V3>> pendingLights;   // (mat, radiance) for area_light records
+    EnvMap samplingEm;
+    bool hasSamplingEm = false;
     while (std::getline(in, line)) {
         std::istringstream ls(line);
         std::string k;
@@ -1192,6 +1204,18 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
         } else if (k == "options") {
             std::string alg; ls >> alg >> s.minPL >> s.maxPL;
             s.algorithm = (alg == "ptn") ? 6 : 7;
+        } else if (k == "sampling_material") {
+            // sampling overrides of one material: GGX sampling roughness, roulette probability
+            // (negative: unchanged); finite differences with the sampling held fixed
+            int mat; float aS, rr; ls >> mat >> aS >> rr;
+            if (mat < 0 || mat >= (int)s.mats.size()) { err = "sampling_material: material out of range"; return false; }
+            if (aS >= 0.f) s.mats[mat].alphaSample = Clampf(aS, 0.001f, 1.0f);
+            if (rr >= 0.f) s.mats[mat].rrOverride = rr;
+        } else if (k == "background_em_sampling") {
+            // the environment-map sampler's tables come from this map instead of the lit one
+            std::string p; ls >> p;
+            if (!LoadEnv(p, samplingEm)) { err = "cannot read environment map " + p; return false; }
+            hasSamplingEm = true;
         } else {
             err = "unknown record " + k;
             return false;
@@ -1199,7 +1223,15 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
     }
     s.mat2light.resize(std::max(s.mat2light.size(), s.mats.size()), -1);
     if (s.hasBg) s.bgLightId = (int)s.lights.size();   // the background is pushed last (src/scene.hxx:948-953)
-    if (s.bgIsEm) s.em.BuildCdf();
+    if (s.bgIsEm) {
+        s.em.BuildCdf();
+        if (hasSamplingEm) {
+            if (samplingEm.W != s.em.W || samplingEm.H != s.em.H) { err = "sampling map size differs"; return false; }
+            samplingEm.BuildCdf();
+            s.em.cond = samplingEm.cond;
+            s.em.marg = samplingEm.marg;
+        }
+    }
     s.SetupCamera();
     if (s.hasBg && s.bgIsEm && s.lights.size() > 0) {
         err = "environment map together with area lights is not restated by the oracle";

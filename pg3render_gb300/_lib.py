@@ -109,6 +109,10 @@ SIGNATURES = {
                                           ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
     "pg3gpu_probe_light_pdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
     "pg3gpu_export_bvh": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)] + [ctypes.c_void_p] * 3),
+    "pg3gpu_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]),
+    "pg3gpu_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pg3gpu_diff_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]),
+    "pg3gpu_diff_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pg3gpu_batch_create": (ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(Options),
                                            ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_void_p)]),

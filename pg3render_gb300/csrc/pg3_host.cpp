@@ -122,6 +122,7 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
     }
 
     // materials (src/materials.hxx:262-266, 791-806, 996-1021)
+    v.nmat = sc.num_materials;
     out.mats.resize(sc.num_materials);
     for (uint32_t i = 0; i < sc.num_materials; ++i) {
         const pg3gpu_material &m = sc.materials[i];

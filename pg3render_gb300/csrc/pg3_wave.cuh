@@ -130,6 +130,7 @@ PG3_DI void gradMatAdd(float *sGrad, int mat, float4 g)
 // times dLoss/dradiance. Lambert: every later term is linear in albedo_c; GGX: times d ln f / da.
 PG3_DI void gradContinuation(const SceneView &S, float *sGrad, int mat, float dAtt, float3 after)
 {
+    if ((uint32_t)mat >= S.nmat) return;   // sGrad holds 4 * nmat floats
     const DevMaterial m = loadMat(S, mat);
     if (m.kind == kMatLambert)
         gradMatAdd(sGrad, mat, make_float4(m.r > 0.f ? after.x / m.r : 0.f, m.g > 0.f ? after.y / m.g : 0.f,
@@ -202,7 +203,8 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
                 mis = misPower(prevBsdfPdf, pdf * pickProb(S, org, prevN, prevSum, S.bgLightId));
                 L = ew * Le * mis;
             } else L = ew * Le;
-            if (adj && S.bgKind == kBgEnvMap) gradEmDir(S, G.gEm, dir, delta * ((pl == 1) ? f3(1.f) : ew * mis));
+            if (adj && S.bgKind == kBgEnvMap && G.gEm)
+                gradEmDir(S, G.gEm, dir, delta * ((pl == 1) ? f3(1.f) : ew * mis));
         }
         if (computeRefl) ++pc.bg;
         return;
@@ -268,7 +270,7 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
                             o.s3 = make_float4(0.f, 0.f, 0.f, dot(delta, c) * br.dAtt);
                         }
                         float3 e = f3(0.f);
-                        if (lid == S.bgLightId && S.bgKind == kBgEnvMap)
+                        if (lid == S.bgLightId && S.bgKind == kBgEnvMap && G.gEm)
                             e = delta * beta * br.att * (fabsf(dot(wig, nrm)) * mis / lightPdf);
                         o.s4 = make_float4(e.x, e.y, e.z, __int_as_float(matId));
                     }
@@ -340,7 +342,7 @@ PG3_DI void shadowGrad(const SceneView &S, const float4 *rec, float3 dir, const 
     if (!GRAD || !G.adjoint) return;
     const float4 g = rec[3], e = rec[4];
     const int mat = __float_as_int(e.w);
-    if (mat < 0) return;
+    if (mat < 0 || (uint32_t)mat >= S.nmat) return;   // sGrad holds 4 * nmat floats
     gradMatAdd(sGrad, mat, g);
     if (e.x != 0.f || e.y != 0.f || e.z != 0.f) gradEmDir(S, G.gEm, dir, xyz(e));
 }

@@ -281,6 +281,35 @@ def cornell_env(width: int = 512, height: int = 512, em_width: int = 1024, em_he
     return s
 
 
+def cornell_env_diff(width: int = 256, height: int = 256, em_width: int = 512, em_height: int = 256,
+                     em_seed: int = 7) -> Scene:
+    """The environment-lit box for gradients: four Lambert materials (floor, back wall, red
+    left, green right), the two spheres of cornell_env (GGX dielectric alpha 0.3, GGX
+    conductor alpha 0.05) and two smaller ones (GGX conductor alpha 0.2, GGX dielectric
+    alpha 0.15), i.e. four albedo triples and four roughnesses."""
+    s = Scene(_camera_for_box(width, height), name="cornell_diff_%dx%d_em%dx%d" % (width, height, em_width, em_height))
+    m_floor = s.add_material(Material(MAT_LAMBERT, WHITE))
+    m_back = s.add_material(Material(MAT_LAMBERT, (0.55, 0.60, 0.70)))
+    m_left = s.add_material(Material(MAT_LAMBERT, RED))
+    m_right = s.add_material(Material(MAT_LAMBERT, GREEN))
+    s.add_quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), m_floor, (0, 0, 1))
+    s.add_quad((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), m_back, (0, -1, 0))
+    s.add_quad((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), m_left, (1, 0, 0))
+    s.add_quad((1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1), m_right, (-1, 0, 0))
+    m_diel = s.add_material(Material(MAT_GGX_DIELECTRIC, alpha=0.3, ior=1.5, ior_outer=1.0))
+    m_cond = s.add_material(Material(MAT_GGX_CONDUCTOR, alpha=0.05, ior=COPPER_IOR, ior_outer=AIR_IOR,
+                                     absorb=COPPER_ABSORB))
+    m_cond2 = s.add_material(Material(MAT_GGX_CONDUCTOR, alpha=0.2, ior=COPPER_IOR, ior_outer=AIR_IOR,
+                                      absorb=COPPER_ABSORB))
+    m_diel2 = s.add_material(Material(MAT_GGX_DIELECTRIC, alpha=0.15, ior=1.5, ior_outer=1.0))
+    s.spheres.append(((-0.45, 0.25, -0.65), 0.35, m_diel))
+    s.spheres.append(((0.45, -0.25, -0.65), 0.35, m_cond))
+    s.spheres.append(((0.5, 0.6, -0.8), 0.2, m_cond2))
+    s.spheres.append(((-0.55, -0.45, -0.8), 0.2, m_diel2))
+    s.env_map = synthetic_sky(em_width, em_height, seed=em_seed)
+    return s
+
+
 def random_variant(seed: int, em_width: int = 256, em_height: int = 128,
                    side_range: Tuple[int, int] = (64, 512), spp_range: Tuple[int, int] = (4, 64),
                    max_spheres: int = 8, use_env: Optional[bool] = None):
