@@ -17,6 +17,11 @@ A step renders the whole workload once (512*512*256 = 67,108,864 camera paths).
            event-timed launch duration, against the measured HBM copy peak;
 * cpu_baseline the reference's own CPU renderer (oracle/_ref, built from the
            reference sources) on all host cores over a bounded sample.
+* secondary the other two parts of the metric, on their own workloads: batched
+           scenes/s (64 seeded variants in one persistent launch vs a loop of
+           single-scene launches), forward+adjoint ms/iteration with a
+           finite-difference check of the gradient, and the inverse-rendering loop
+           (500 Adam steps, one CUDA graph per iteration).
 --impl reference times that CPU renderer alone as the main line.
 With N > 1 (torchrun) every rank renders its own sample range of the same
 workload (weak scaling, no collective on the data path).
@@ -64,6 +69,8 @@ def parse():
     ap.add_argument("--spp", type=int, default=256)
     ap.add_argument("--cpu-iters", type=int, default=12)
     ap.add_argument("--paths-in-flight", type=int, default=0, help="wavefront chunk size (0: automatic)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the batched (64 scenes), forward+adjoint and inverse-rendering measurements")
     a = ap.parse_args()
     global WIDTH, HEIGHT, SPP
     WIDTH = HEIGHT = a.width
@@ -286,7 +293,173 @@ def run_gpu(args, rank, world, local_rank):
     line["clocks"] = clk.summary()
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(scene, sampler, iters=args.cpu_iters)
+    if world == 1 and not args.no_secondary:
+        line["secondary"] = secondary_metrics()
     return line
+
+
+# ----------------------------------------------------------------------------- secondary metrics
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def batched_metric(reps=3):
+    """64 seeded Cornell-box variants (side 64..512 log-uniform, 4..64 spp, 0..8 spheres, half
+    area light / half 256x128 sky, Russian roulette path lengths): one autotuned batch run (one
+    CUDA graph launch) against a loop of plain single-scene launches of the same scenes."""
+    import torch
+    import pg3render_gb300 as P
+    from pg3render_gb300 import scene as S
+    R = P.renderer
+    cfgs, spps = [], []
+    for i in range(64):
+        s, k = S.random_variant(i)
+        cfgs.append(P.Config(scene=s, max_path_length=0, base_seed=1000 + i, max_paths_in_flight=1 << 21))
+        spps.append(k)
+    paths = sum(c.scene.camera.width * c.scene.camera.height * k for c, k in zip(cfgs, spps))
+    ctxs = [P.GpuPathTracer(c) for c in cfgs]
+    for r, k in zip(ctxs, spps):
+        r.RunIteration(R.kPathTracing, 0, k)
+    for r in ctxs:
+        r.synchronize()
+    loop = []
+    for rep in range(reps):
+        t0 = time.perf_counter()
+        for r, k in zip(ctxs, spps):
+            r.RunIteration(R.kPathTracing, (rep + 1) * k, k)
+        for r in ctxs:
+            r.synchronize()
+        loop.append(time.perf_counter() - t0)
+    for r in ctxs:
+        r.close()
+    b = P.GpuBatch(cfgs, spps)
+    t0 = time.perf_counter()
+    tuning = b.autotune(16)
+    tune_s = time.perf_counter() - t0
+    b.run()
+    b.synchronize()
+    batch, dev = [], []
+    for rep in range(reps):
+        t0 = time.perf_counter()
+        b.run()
+        b.synchronize()
+        batch.append(time.perf_counter() - t0)
+        dev.append(b.stats()["last_iteration_ms"])
+    st = b.stats()
+    b.close()
+    lt, bt = statistics.median(loop), statistics.median(batch)
+    return {"metric": "batched scenes/s", "scenes": 64, "paths_per_run": paths,
+            "batched_scenes_per_s": round(64 / bt, 2), "loop_scenes_per_s": round(64 / lt, 2),
+            "speedup_vs_loop": round(lt / bt, 2), "batch_run_ms": round(bt * 1e3, 2),
+            "batch_device_ms": round(statistics.median(dev), 2), "loop_run_ms": round(lt * 1e3, 2),
+            "batch_msamples_per_s": round(paths / bt / 1e6, 1), "tuning": tuning, "autotune_s": round(tune_s, 2),
+            "timing": "host wall clock of whole runs incl. synchronisation, median of %d" % reps,
+            "paths_counted": int(st["paths"])}
+
+
+def differentiable_metric(steps=5):
+    """The gradient configuration: the environment-lit box with 4 Lambert and 4 GGX materials at
+    256x256, 64 spp, 512x256 map, max path length 12, roulette after 3 bounces; L2 loss against a
+    fixed target. Reports forward+adjoint ms/iteration against the plain forward, and the
+    adjoint against central differences (step 1e-3, common random numbers, sampling held fixed)
+    of the loss restricted to a 32x32 crop."""
+    import numpy as np
+    import torch
+    import pg3render_gb300 as P
+    from pg3render_gb300 import scene as S, _lib
+    R = P.renderer
+    sc = S.cornell_env_diff(256, 256, 512, 256)
+    cfg = P.Config(scene=sc, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM, em_sampler=_lib.EM_STEERABLE,
+                   base_seed=3)
+    spp = 64
+    out = {"metric": "fwd+adjoint ms/iter", "workload": "cornell_env_diff_256x256_64spp_maxpl12_rr3_em512x256_steerable",
+           "paths": 256 * 256 * spp}
+    with P.diff.DiffRenderer(cfg) as dr:
+        dr.use_torch_stream()
+        for _ in range(3):
+            dr.RunIteration(R.kPathTracing, 0, spp)
+        a, b = _events()
+        torch.cuda.synchronize()
+        a.record()
+        for k in range(steps):
+            dr.RunIteration(R.kPathTracing, 0, spp)
+        b.record()
+        torch.cuda.synchronize()
+        fwd = a.elapsed_time(b) / steps
+        img = torch.empty((256, 256, 3), device="cuda")
+        target = torch.full_like(img, 0.25)
+        crop = torch.zeros_like(img)
+        crop[112:144, 112:144] = 1
+        gm = torch.zeros((len(sc.materials), 4), device="cuda")
+        ge = torch.zeros((256, 512, 3), device="cuda")
+        for _ in range(3):
+            dr.forward_into(img, 0, spp)
+            dr.adjoint_into(2 * (img - target), gm, ge)
+        torch.cuda.synchronize()
+        a, b = _events()
+        a.record()
+        for k in range(steps):
+            dr.forward_into(img, 0, spp)
+            dr.adjoint_into(2 * (img - target), gm, ge)
+        b.record()
+        torch.cuda.synchronize()
+        fa = a.elapsed_time(b) / steps
+        out.update(plain_forward_ms=round(fwd, 3), fwd_adjoint_ms=round(fa, 3), ratio_to_forward=round(fa / fwd, 3))
+        # gradient check on the crop
+        dr.forward_into(img, 0, spp)
+        dl = (2 * (img - target) * crop).contiguous()
+        gm.zero_()
+        dr.adjoint_into(dl, gm, None)
+        torch.cuda.synchronize()
+        adj = gm.cpu().numpy().astype(np.float64)
+        base, _ = dr.get_params()
+        errs, h = [], 1e-3
+
+        def loss_at(p):
+            dr.set_params(p, None, keep_sampling=True)
+            dr.forward_into(img, 0, spp)
+            torch.cuda.synchronize()
+            return float((((img - target) ** 2) * crop).double().sum())
+        names = []
+        for i, m in enumerate(sc.materials):
+            cols = [0, 1, 2] if m.kind == S.MAT_LAMBERT else [3]
+            for c in cols:
+                p1, p2 = base.copy(), base.copy()
+                p1[i, c] += h
+                p2[i, c] -= h
+                fd = (loss_at(p1) - loss_at(p2)) / (2 * h)
+                errs.append((abs(adj[i, c] - fd), abs(fd), adj[i, c], fd))
+                names.append("%s%d.%s" % ("albedo" if c < 3 else "alpha", i, "rgba"[c]))
+        dr.set_params(base, None)
+        scale = max(e[1] for e in errs)
+        big = [e for e in errs if e[1] > 0.02 * scale]
+        out["gradient_check"] = {
+            "params": len(errs), "crop": [32, 32], "step": h,
+            "max_rel_err": round(max(e[0] / e[1] for e in big), 5),
+            "median_rel_err": round(statistics.median(e[0] / e[1] for e in big), 6),
+            "params_compared": len(big), "note": "relative errors over parameters whose derivative exceeds 2% of the "
+                                                 "largest; sampling held fixed (detached estimator)"}
+    return out
+
+
+def inverse_metric():
+    from pg3render_gb300 import inverse
+    r = inverse.run()
+    r["metric"] = "inverse rendering: 500 Adam steps, one CUDA graph per iteration"
+    r.pop("loss_trace", None)
+    return r
+
+
+def secondary_metrics():
+    out = {}
+    for name, fn in (("batched", batched_metric), ("differentiable", differentiable_metric),
+                     ("inverse_rendering", inverse_metric)):
+        try:
+            out[name] = fn()
+        except Exception as e:   # reported, never hidden
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+    return out
 
 
 # ----------------------------------------------------------------------------- reference arm

@@ -282,6 +282,10 @@ int pg3gpu_diff_forward(pg3gpu_ctx *ctx, uint32_t iteration, uint32_t spp, float
  * to); grad_env: env_height x env_width x 3 (device, added to; NULL skips the map). Replays the
  * paths of the last pg3gpu_diff_forward, whose parameters must still be current. */
 int pg3gpu_diff_adjoint(pg3gpu_ctx *ctx, const float *dloss_dimage, float *grad_materials, float *grad_env);
+/* offset: a device word (NULL: none) that pg3gpu_diff_forward and pg3gpu_diff_adjoint read when
+ * they run and add to their sample indices, so a captured graph can advance it between replays
+ * and render new samples each time; a forward and its adjoint must see the same value. */
+int pg3gpu_set_sample_offset(pg3gpu_ctx *ctx, const uint32_t *offset);
 
 /* ---- Batched rendering (no counterpart in the reference) ----------------------------
  * Many scene instances, each with its own scene, options (algorithm 7 on the wavefront

@@ -113,6 +113,7 @@ SIGNATURES = {
     "pg3gpu_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pg3gpu_diff_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]),
     "pg3gpu_diff_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pg3gpu_set_sample_offset": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pg3gpu_batch_create": (ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(Options),
                                            ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_void_p)]),

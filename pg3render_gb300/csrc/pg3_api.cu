@@ -88,6 +88,23 @@ int ensureOutput(pg3gpu_ctx *ctx, uint64_t paths)
     return PG3GPU_OK;
 }
 
+// Wavefront queues for launches of `paths` paths: max_paths_in_flight slots (default 2^22), fewer
+// when a launch has fewer paths; they only grow.
+int ensureWave(pg3gpu_ctx *ctx, uint64_t paths)
+{
+    const uint64_t cap = ctx->opts.max_paths_in_flight ? ctx->opts.max_paths_in_flight : (1ull << 22);
+    const uint64_t want = std::min<uint64_t>(cap, paths);
+    if (ctx->dWave && ctx->waveCapacity >= want) return PG3GPU_OK;
+    ctxFree(ctx, ctx->dWave);
+    ctx->dWave = nullptr;
+    ctx->waveCapacity = 0;
+    char *w = nullptr;
+    if (int st = devAlloc(ctx, &w, wavefrontBytes(want, false))) return st;
+    ctx->dWave = w;
+    ctx->waveCapacity = want;
+    return PG3GPU_OK;
+}
+
 // Paths per launch chunk: whole sample passes, bounded by max_paths_in_flight.
 uint32_t passesPerChunk(const pg3gpu_ctx *ctx, uint32_t spp)
 {
@@ -112,6 +129,7 @@ int renderChunk(pg3gpu_ctx *ctx, bool naive, uint32_t sample0, uint32_t passes)
     const uint32_t npix = ctx->W * ctx->H;
     const uint64_t paths = (uint64_t)passes * npix;
     int st = ensureOutput(ctx, paths);
+    if (!st && ctx->useWavefront && !naive) st = ensureWave(ctx, paths);
     if (st) return st;
     if (ctx->pendingTimers == pg3gpu_ctx::kTimerSlots) {
         cudaStreamSynchronize(ctx->stream);
@@ -286,15 +304,7 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
     // the wavefront pipeline is the default for the NEE path tracer (3x the megakernel on the
     // benchmark scenes); the BSDF-only tracer always runs as a megakernel
     ctx->useWavefront = (opts->pipeline == PG3GPU_PIPELINE_WAVEFRONT || opts->pipeline == PG3GPU_PIPELINE_AUTO);
-    ctx->waveGrid = sms * 4;
-    if (ctx->useWavefront && !forBatch) {
-        const uint64_t npix = (uint64_t)ctx->W * ctx->H;
-        const uint64_t cap = opts->max_paths_in_flight ? opts->max_paths_in_flight : (1ull << 22);
-        ctx->waveCapacity = std::min<uint64_t>(cap, std::max<uint64_t>(1ull << 16, npix * 16));
-        void *w;
-        if ((st = devAlloc(ctx, (char **)&w, wavefrontBytes(ctx->waveCapacity, false)))) return bail(st);
-        ctx->dWave = w;
-    }
+    ctx->waveGrid = sms * 4;   // the wavefront queues are allocated by the first launch (ensureWave)
     if (!forBatch) {
         if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
             return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));

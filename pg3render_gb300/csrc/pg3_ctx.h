@@ -51,6 +51,7 @@ struct pg3gpu_ctx {
     uint64_t waveGradCapacity = 0;
     float *dRowInt = nullptr;                       // environment-map CDF build: per-row integrals
     uint32_t diffIteration = 0, diffSpp = 0;        // samples the stored radiance belongs to
+    const uint32_t *dSampleOffset = nullptr;        // caller's device word added to sample indices
     bool diffValid = false;
 };
 

@@ -300,6 +300,7 @@ extern "C" int pg3gpu_diff_forward(pg3gpu_ctx *ctx, uint32_t iteration, uint32_t
     if (int st = ensureDiffBuffers(ctx, paths)) return st;
     GradArgs G{};
     G.adjoint = 0;
+    G.sampleOffset = ctx->dSampleOffset;
     uint64_t launches = 0;
     cudaError_t e = launchWavefront(ctx->view, false, iteration, paths, npix, ctx->dTot[0], ctx->dTot[1], ctx->dTot[2],
                                     ctx->dStats, ctx->dWaveGrad, ctx->waveGradCapacity, ctx->waveGrid, ctx->stream,
@@ -336,11 +337,20 @@ extern "C" int pg3gpu_diff_adjoint(pg3gpu_ctx *ctx, const float *dLdI, float *gM
     G.gMat = gMat;
     G.gEm = (ctx->view.bgKind == kBgEnvMap) ? gEm : nullptr;
     G.adjoint = 1;
+    G.sampleOffset = ctx->dSampleOffset;
     uint64_t launches = 0;
     const cudaError_t e = launchWavefront(ctx->view, false, ctx->diffIteration, paths, npix, ctx->dAdj[0],
                                           ctx->dAdj[1], ctx->dAdj[2], ctx->dStats, ctx->dWaveGrad,
                                           ctx->waveGradCapacity, ctx->waveGrid, ctx->stream, &launches, &G);
     if (int st = cudaStatus(ctx, e, "adjoint")) return st;
     ctx->allLaunches += launches;
+    return PG3GPU_OK;
+}
+
+extern "C" int pg3gpu_set_sample_offset(pg3gpu_ctx *ctx, const uint32_t *offset)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    ctx->dSampleOffset = offset;
+    ctx->diffValid = false;
     return PG3GPU_OK;
 }

@@ -125,6 +125,7 @@ struct GradArgs {
     float *gMat;              // per material: d/d albedo rgb, d/d roughness
     float *gEm;               // per environment-map texel: rgb
     int adjoint;              // 0: primal replay (radiance only), 1: adjoint
+    const uint32_t *sampleOffset;   // device word added to every sample index (null: none)
 };
 
 enum : unsigned int { kErrTraversalStack = 1u, kErrQueueOverflow = 2u, kErrSteerDescent = 4u };

@@ -35,11 +35,18 @@ namespace pg3 {
 namespace {
 
 template <bool GRAD>
+PG3_DI uint32_t sampleBase(uint32_t sample0, const GradArgs &G)
+{
+    return (GRAD && G.sampleOffset) ? sample0 + *G.sampleOffset : sample0;
+}
+
+template <bool GRAD>
 __global__ void __launch_bounds__(kWaveBlock) raygenKernel(const __grid_constant__ SceneView S, Queues Q,
                                                            uint64_t base, uint32_t count, uint32_t npix,
                                                            uint32_t sample0, float *outR, float *outG, float *outB,
-                                                           DevStats *stats)
+                                                           DevStats *stats, GradArgs G)
 {
+    sample0 = sampleBase<GRAD>(sample0, G);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint64_t g = base + i;
         const uint32_t pixel = (uint32_t)(g % npix), sample = sample0 + (uint32_t)(g / npix);
@@ -89,6 +96,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
 {
     extern __shared__ float sGrad[];
     initBlockGrad<GRAD>(sGrad, S.nmat);
+    sample0 = sampleBase<GRAD>(sample0, G);
     constexpr int kBucket = (K < 0) ? kBucketMiss : 1 + K;
     const uint32_t n = Q.cnt->bucket[kBucket];
     const float4 *rq = Q.ray[cur];
@@ -215,7 +223,7 @@ cudaError_t runWavefront(const SceneView &S, uint32_t sample0, uint64_t numPaths
         }
         cudaMemsetAsync(Q.cnt, 0, sizeof(Counters), stream);
         const int gen = (int)std::min<uint64_t>((count + kWaveBlock - 1) / kWaveBlock, (uint64_t)gridBlocks * 4);
-        raygenKernel<GRAD><<<gen, kWaveBlock, 0, stream>>>(S, Q, base, count, npix, sample0, r, g, b, stats);
+        raygenKernel<GRAD><<<gen, kWaveBlock, 0, stream>>>(S, Q, base, count, npix, sample0, r, g, b, stats, G);
         *launches += 1;
         for (uint32_t bounce = 0; bounce < maxBounces; ++bounce) {
             const int cur = bounce & 1;

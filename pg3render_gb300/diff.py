@@ -61,6 +61,13 @@ class DiffRenderer(GpuPathTracer):
                     e.ctypes.data_as(ctypes.c_void_p) if e is not None else None)
         _lib.check(self._L.pg3gpu_set_params(self._ctx, args[0], args[1], flags), self._ctx)
 
+    def set_sample_offset(self, offset):
+        """A one-element int32/uint32 CUDA tensor added to the sample indices of every
+        differentiable launch (None: off); advancing it inside a captured graph renders new
+        samples on every replay."""
+        self._offset = offset
+        _lib.check(self._L.pg3gpu_set_sample_offset(self._ctx, _dptr(offset)), self._ctx)
+
     # -- device tensors -----------------------------------------------------------------------
     def forward_into(self, image, iteration, spp):
         self.use_torch_stream()
