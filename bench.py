@@ -49,9 +49,10 @@ EM_W, EM_H = 1024, 512
 # per-unit algorithmic bytes of the wavefront record layout (ray 32, hit 16, state 40, shadow 48)
 BYTES_PER_SEGMENT = 360
 BYTES_PER_PATH = 72 + 36
-# DRAM bytes per path-kernel launch measured by ncu on the same workload
-# (profiles/megakernel_cornell_env.md); None until captured for the current kernel.
-NCU_TRAFFIC_PER_PATH = None
+# DRAM bytes (read + write) per camera path of one launch chunk, measured by ncu over all stage
+# kernels of one step of the 128x128 x 64 spp case of this workload (one chunk of 2^20 paths;
+# profiles/wavefront_cornell_env.md); the chunk's traffic grows with its paths.
+NCU_TRAFFIC_PER_PATH = 1330.2
 
 
 def parse():
