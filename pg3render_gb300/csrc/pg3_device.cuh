@@ -436,14 +436,14 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         r.att = valid ? make_float3(m.r, m.g, m.b) * kPiInvF : f3(0.f);
         if (DA) r.dAtt = valid ? kPiInvF : 0.f;
     } else if (K == kMatGgxConductor) {
+        // The value and pdf of the drawn direction come from the evaluation routine, so that
+        // sampled and evaluated pdfs agree to the bit (the reference evaluates them from the
+        // drawn microfacet normal, which equals the recomputed half vector up to rounding).
         const float3 h = sampleGgxVndf(wol, m.alphaS, u0, u1, m.vndfExact != 0);
-        const float D = ggxD(h, m.alpha);
         bool above;
-        r.wil = reflect(above, wol, h);
-        const float F = fresnelConductor(dot(h, wol), m.eta, m.absorb);
-        r.pdfW = condPdf(m, wol, h, ggxDp(m, h, D));
-        r.att = (!above || r.wil.z < 0.0f) ? f3(0.f) : condEval(m, r.wil, wol, h, F, D);
-        if (DA) r.dAtt = ggxDlnDGda(r.wil, wol, h, m.alpha);
+        const float3 wil = reflect(above, wol, h);
+        evalBsdfK<K, DA>(m, wil, wol, r);
+        if (!above || wil.z < 0.0f) r.att = f3(0.f);
     } else {
         DielCtx c;
         const bool below = wol.z < 0.f;
@@ -452,24 +452,20 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         c.etaS = below ? m.etaInv : m.eta;
         c.etaInvS = below ? m.eta : m.etaInv;
         c.m = sampleGgxVndf(c.wo, m.alphaS, u0, u1, m.vndfExact != 0);
-        c.D = ggxD(c.m, m.alpha);
-        c.Dp = ggxDp(m, c.m, c.D);
         c.F = fresnelDielectric(dot(c.m, c.wo), c.etaS);
         bool above;
         float cosAbs;
         if (u2 <= c.F) {
             c.wi = reflect(above, c.wo, c.m);
             cosAbs = c.wi.z;
-            c.refl = true;
         } else {
             c.wi = refract(above, c.wo, c.m, c.etaS);
             cosAbs = -c.wi.z;
-            c.refl = false;
         }
-        r.wil = c.wi * s;
-        r.pdfW = dielPdf(m, c);
-        r.att = (!above || cosAbs < 0.0f) ? f3(0.f) : dielEval(m, c);
-        if (DA) r.dAtt = ggxDlnDGda(c.wi, c.wo, c.m, m.alpha);
+        // value and pdf (with the Fresnel component probability) from the evaluation routine
+        const float3 wil = c.wi * s;
+        evalBsdfK<K, DA>(m, wil, wol, r);
+        if (!above || cosAbs < 0.0f) r.att = f3(0.f);
     }
 }
 PG3_DI void sampleBsdf(const DevMaterial &m, float3 wol, float u0, float u1, float u2, BsdfRec &r)
