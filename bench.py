@@ -183,6 +183,29 @@ def cpu_baseline(scene, sampler, threads=None, iters=1):
                 "sample": "%d spp of the %dx%d scene" % (spp, WIDTH, HEIGHT)}
 
 
+# ----------------------------------------------------------------------------- ranks
+SAMPLES_PER_RANK = 1 << 24   # sample-index stride between ranks: disjoint random streams
+
+
+def rank_sample_base(rank):
+    """First sample index a rank renders. Ranks render disjoint sample ranges of the same
+    workload (weak scaling, no collective on the data path)."""
+    return rank * SAMPLES_PER_RANK
+
+
+def max_over_ranks(x, device):
+    """The slowest rank's value (the timing rule: max over ranks)."""
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(world, steps, paths_per_step, total_s):
+    """Msamples/s of the whole job: every rank renders paths_per_step per step."""
+    return world * steps * paths_per_step / total_s / 1e6
+
+
 # ----------------------------------------------------------------------------- GPU arm
 def run_gpu(args, rank, world, local_rank):
     import torch
@@ -203,7 +226,9 @@ def run_gpu(args, rank, world, local_rank):
                    max_paths_in_flight=args.paths_in_flight)
     npix = WIDTH * HEIGHT
     paths_per_step = npix * SPP
-    sample_base = rank * (1 << 24)
+    sample_base = rank_sample_base(rank)
+    if (args.warmup + args.steps) * SPP > SAMPLES_PER_RANK:
+        raise ValueError("warmup + steps exceed the sample range of a rank")
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     r = P.GpuPathTracer(cfg, device=local_rank)
@@ -228,11 +253,9 @@ def run_gpu(args, rank, world, local_rank):
     total_s = sum(step_ms) / 1e3
     st = r.stats()
     if world > 1:
-        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = max_over_ranks(total_s, "cuda")
         torch.distributed.barrier()
-        total_s = float(t.item())
-    value = world * args.steps * paths_per_step / total_s / 1e6
+    value = whole_job_value(world, args.steps, paths_per_step, total_s)
 
     # roofline of the path kernel
     launches = max(1, st["path_kernel_launches"])
@@ -252,8 +275,6 @@ def run_gpu(args, rank, world, local_rank):
 
     # end to end through the C ABI with host buffers
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 5))
-    if e2e_steps == 0:
-        e2e = None
     desc_bytes = (scene.env_map.nbytes + 40 * len(scene.triangles) + 20 * len(scene.spheres)
                   + 32 * len(scene.materials) + 16 * len(scene.area_lights))
     d2h = npix * 3 * 8
@@ -267,14 +288,12 @@ def run_gpu(args, rank, world, local_rank):
     torch.cuda.synchronize()
     e2e_s = max(time.perf_counter() - t0, 1e-9)
     if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = None if e2e_steps == 0 else {"value": round(world * e2e_steps * paths_per_step / e2e_s / 1e6, 3), "unit": UNIT,
-           "h2d_bytes_per_step": int(desc_bytes), "d2h_bytes_per_step": int(d2h),
-           "steps": e2e_steps, "image_mean": [round(float(x), 5) for x in img.mean(axis=(0, 1))]}
-    if e2e_steps == 0:
-        e2e = None
+        e2e_s = max_over_ranks(e2e_s, "cuda")
+    e2e = None
+    if e2e_steps > 0:
+        e2e = {"value": round(whole_job_value(world, e2e_steps, paths_per_step, e2e_s), 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(desc_bytes), "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+               "image_mean": [round(float(x), 5) for x in img.mean(axis=(0, 1))]}
 
     if rank != 0:
         return None
