@@ -260,7 +260,21 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
         if ((st = upload(ctx, (int4 **)&sv.tri, hs.steer.tri))) return bail(st);
         if ((st = upload(ctx, (float **)&sv.nodeW, hs.steer.nodeW))) return bail(st);
         if ((st = upload(ctx, (int **)&sv.nodeChild, hs.steer.nodeChild))) return bail(st);
-        if ((st = upload(ctx, (float4 **)&sv.leafPlane, hs.steer.leafPlane))) return bail(st);
+        // leaf planes, then (pg3_steer.cuh) edge normals, leaf-locator cells, whole-sphere weights
+        std::vector<float4> aux = hs.steer.leafPlane;
+        aux.insert(aux.end(), hs.steer.leafEdge.begin(), hs.steer.leafEdge.end());
+        for (const uint4 &c : hs.steer.leafCells) {
+            float4 f;
+            std::memcpy(&f, &c, sizeof f);
+            aux.push_back(f);
+        }
+        for (int k = 0; k < 9; k += 4)
+            aux.push_back(make_float4(hs.steer.rootW[k], k + 1 < 9 ? hs.steer.rootW[k + 1] : 0.f,
+                                      k + 2 < 9 ? hs.steer.rootW[k + 2] : 0.f, k + 3 < 9 ? hs.steer.rootW[k + 3] : 0.f));
+        if (hs.steer.leafPlane.size() != (20ull << (2 * hs.steer.level)) ||
+            hs.steer.leafGrid != (4u << hs.steer.level))
+            return bail(fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: unexpected leaf count or grid"));
+        if ((st = upload(ctx, (float4 **)&sv.leafPlane, aux))) return bail(st);
         if ((st = upload(ctx, (int4 **)&sv.faceCells, hs.steer.faceCells))) return bail(st);
         sv.level = hs.steer.level;
         for (size_t l = 0; l < hs.steer.levelOffset.size() && l < 10; ++l) sv.levelOff[l] = hs.steer.levelOffset[l];

@@ -52,7 +52,8 @@ struct SteerView {
     const int4 *tri;          // vertex ids of the triangles of every subdivision level
     const float *nodeW;       // per 6-ary tree node: 6 children x 9 summed weights
     const int *nodeChild;     // per node: 6 child ids (>= 0 node, < 0 ~leaf, INT_MIN none)
-    const float4 *leafPlane;  // per leaf: unit plane normal, distance from the origin
+    const float4 *leafPlane;  // per leaf: unit plane normal, distance from the origin; followed in the
+                              // same allocation by the leaf-locator tables (pg3_steer.cuh)
     const int4 *faceCells;    // cube-map cells: up to 4 candidate level-0 faces (-1 none)
     uint32_t level;           // leaf subdivision level
     uint32_t levelOff[10];    // first entry of each level in `tri`

@@ -44,14 +44,26 @@ PG3_DI float dot9(const float *__restrict__ w, const float c[9])
     return s;
 }
 
-// Whole-sphere integral Z(n): the root node's children.
-PG3_DI float steerTotal(const SteerView &T, const float c[9])
+// Tables that follow the leaf planes in one allocation (pg3gpu_create): per leaf 3 inward edge
+// normals, the leaf-locator cube map (6 x grid^2 cells of up to 8 16-bit leaf ids), and the
+// 9 weights of the whole sphere. Leaves = 20 * 4^level, grid = 4 * 2^level.
+PG3_DI uint32_t steerLeaves(const SteerView &T) { return 20u << (2 * T.level); }
+PG3_DI uint32_t steerGrid(const SteerView &T) { return 4u << T.level; }
+PG3_DI const float4 *steerEdges(const SteerView &T) { return T.leafPlane + steerLeaves(T); }
+PG3_DI const uint4 *steerCells(const SteerView &T)
 {
-    float z = 0.f;
-    for (int i = 0; i < 6; ++i)
-        if (__ldg(&T.nodeChild[T.root * 6 + i]) != INT_MIN) z += fmaxf(dot9(&T.nodeW[(T.root * 6 + i) * 9], c), 0.f);
-    return z;
+    return reinterpret_cast<const uint4 *>(T.leafPlane + 4 * steerLeaves(T));
 }
+PG3_DI const float *steerRootW(const SteerView &T)
+{
+    const uint32_t g = steerGrid(T);
+    return reinterpret_cast<const float *>(T.leafPlane + 4 * steerLeaves(T) + 6 * g * g);
+}
+
+// Whole-sphere integral Z(n): every node value is positive (the clamped-cosine approximation
+// with its +0.15 term is), so the sum over the root's children is one dot product with the
+// summed weights.
+PG3_DI float steerTotal(const SteerView &T, const float c[9]) { return fmaxf(dot9(steerRootW(T), c), 0.f); }
 
 PG3_DI float3 vdir(const SteerView &T, int v) { return xyz(__ldg(&T.vdir[v])); }
 PG3_DI float vval(const SteerView &T, int v, const float c[9]) { return fmaxf(dot9(&T.vw[v * 9], c), 0.f); }
@@ -71,10 +83,9 @@ PG3_DI float faceMinEdge(const SteerView &T, int f, float3 w)
     return fminf(fminf(dot(w, cross(a, b)), dot(w, cross(b, c))), dot(w, cross(c, a)));
 }
 
-// Leaf (level-L triangle) containing direction w: a cube-map cell gives at most four
-// candidate icosahedron faces (all 20 are scanned if none contains w), then one of
-// four children per subdivision level by three great-circle tests.
-PG3_DI int steerLocate(const SteerView &T, float3 w)
+// Cube-map coordinates of a direction: face 0..5 (+x, -x, +y, -y, +z, -z) and the position
+// (u, v) in [-1, 1]^2 on it.
+PG3_DI int cubeFace(float3 w, float &u, float &v)
 {
     const float ax = fabsf(w.x), ay = fabsf(w.y), az = fabsf(w.z);
     int a;
@@ -82,11 +93,25 @@ PG3_DI int steerLocate(const SteerView &T, float3 w)
     if (ax >= ay && ax >= az) { a = 0; wa = w.x; wb = w.y; wc = w.z; }
     else if (ay >= az) { a = 1; wa = w.y; wb = w.z; wc = w.x; }
     else { a = 2; wa = w.z; wb = w.x; wc = w.y; }
-    const int face = 2 * a + (wa < 0.f ? 1 : 0);
     const float inv = 1.f / fabsf(wa);
-    const int iu = min(max((int)((wb * inv + 1.f) * (0.5f * kSteerCellsDev)), 0), kSteerCellsDev - 1);
-    const int iv = min(max((int)((wc * inv + 1.f) * (0.5f * kSteerCellsDev)), 0), kSteerCellsDev - 1);
-    const int cell = (face * kSteerCellsDev + iv) * kSteerCellsDev + iu;
+    u = wb * inv;
+    v = wc * inv;
+    return 2 * a + (wa < 0.f ? 1 : 0);
+}
+PG3_DI int cubeCell(int face, float u, float v, int G)
+{
+    const int iu = min(max((int)((u + 1.f) * (0.5f * G)), 0), G - 1);
+    const int iv = min(max((int)((v + 1.f) * (0.5f * G)), 0), G - 1);
+    return (face * G + iv) * G + iu;
+}
+
+// Leaf containing direction w through the hierarchy: a cube-map cell gives at most eight
+// candidate icosahedron faces (all 20 are scanned if none contains w), then one of four
+// children per subdivision level by three great-circle tests.
+PG3_DI int steerLocateFaces(const SteerView &T, float3 w)
+{
+    float fu, fv;
+    const int cell = cubeCell(cubeFace(w, fu, fv), fu, fv, kSteerCellsDev);
     const int4 ca = __ldg(&T.faceCells[2 * cell]), cb = __ldg(&T.faceCells[2 * cell + 1]);
     const int cs[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
     int best = cs[0] >= 0 ? cs[0] : 0;
@@ -112,6 +137,33 @@ PG3_DI int steerLocate(const SteerView &T, float3 w)
         local = 4 * local + child;
     }
     return local;
+}
+
+// Leaf containing direction w: the leaf-locator cell lists every leaf that can touch it, so
+// the one whose three edge planes all face w is among them (the face hierarchy decides for
+// cells with more than eight candidates, and if rounding puts w outside all candidates).
+PG3_DI int steerLocate(const SteerView &T, float3 w)
+{
+    float fu, fv;
+    const int face = cubeFace(w, fu, fv);
+    const uint4 cell = __ldg(&steerCells(T)[cubeCell(face, fu, fv, (int)steerGrid(T))]);
+    if (cell.x != 0xfffefffeu) {
+        const uint32_t words[4] = {cell.x, cell.y, cell.z, cell.w};
+        const float4 *E = steerEdges(T);
+        int best = -1;
+        float bestMin = -1e30f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t id = (words[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
+            if (id == 0xffffu) break;
+            const float m = fminf(fminf(dot(w, xyz(__ldg(&E[3 * id]))), dot(w, xyz(__ldg(&E[3 * id + 1])))),
+                                  dot(w, xyz(__ldg(&E[3 * id + 2]))));
+            if (m > bestMin) { bestMin = m; best = (int)id; }
+            if (m >= 0.f) break;
+        }
+        if (best >= 0 && bestMin >= -1e-6f) return best;
+    }
+    return steerLocateFaces(T, w);
 }
 
 // base(w) for any direction.

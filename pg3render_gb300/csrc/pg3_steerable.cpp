@@ -187,6 +187,73 @@ bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, St
         layer.swap(up);
     } while (layer.size() > 1);
     out.root = layer[0].id;
+    out.rootW.assign(9, 0.f);
+    {
+        double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (uint32_t i = 0; i < nLeaf; ++i)
+            for (int k = 0; k < 9; ++k) acc[k] += leafW[(size_t)i * 9 + k];
+        for (int k = 0; k < 9; ++k) out.rootW[k] = (float)acc[k];
+    }
+
+    // leaf locator: inward edge normals of every leaf, and for every cell of a finer cube map
+    // the leaves whose bounding cap meets the cell's bounding cap (a superset of the leaves
+    // that touch the cell); cells with more than 8 keep the face locator
+    out.leafEdge.resize((size_t)nLeaf * 3);
+    std::vector<D3> capC(nLeaf);
+    std::vector<double> capR(nLeaf);
+    for (uint32_t i = 0; i < nLeaf; ++i) {
+        const int4 T = cur[i];
+        const D3 a = {out.vdir[T.x].x, out.vdir[T.x].y, out.vdir[T.x].z};
+        const D3 b = {out.vdir[T.y].x, out.vdir[T.y].y, out.vdir[T.y].z};
+        const D3 c = {out.vdir[T.z].x, out.vdir[T.z].y, out.vdir[T.z].z};
+        const D3 e[3] = {nrm(crs(a, b)), nrm(crs(b, c)), nrm(crs(c, a))};
+        for (int k = 0; k < 3; ++k)
+            out.leafEdge[3 * (size_t)i + k] = make_float4((float)e[k].x, (float)e[k].y, (float)e[k].z, 0.f);
+        capC[i] = nrm(add(add(a, b), c));
+        capR[i] = std::acos(std::fmin(1.0, std::fmin(dt(capC[i], a), std::fmin(dt(capC[i], b), dt(capC[i], c)))));
+    }
+    const uint32_t LG = 4u << level;
+    out.leafGrid = LG;
+    out.leafCells.assign((size_t)6 * LG * LG, make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu));
+    for (int f = 0; f < 6; ++f) {
+        const int ax = f / 2, bx = (ax + 1) % 3, cx = (ax + 2) % 3;
+        const double sg = (f & 1) ? -1.0 : 1.0;
+        auto dirOf = [&](double u, double vv) {
+            double p[3];
+            p[ax] = sg; p[bx] = u; p[cx] = vv;
+            return nrm({p[0], p[1], p[2]});
+        };
+        for (uint32_t iv = 0; iv < LG; ++iv)
+            for (uint32_t iu = 0; iu < LG; ++iu) {
+                const double u0 = -1.0 + 2.0 * iu / LG, u1 = -1.0 + 2.0 * (iu + 1) / LG;
+                const double v0 = -1.0 + 2.0 * iv / LG, v1 = -1.0 + 2.0 * (iv + 1) / LG;
+                const D3 cc = dirOf(0.5 * (u0 + u1), 0.5 * (v0 + v1));
+                double rc = 0.0;
+                for (const D3 &q : {dirOf(u0, v0), dirOf(u1, v0), dirOf(u0, v1), dirOf(u1, v1)})
+                    rc = std::fmax(rc, std::acos(std::fmin(1.0, dt(cc, q))));
+                uint32_t ids[8];
+                int n = 0;
+                bool many = false;
+                for (uint32_t i = 0; i < nLeaf && !many; ++i) {
+                    const double ang = std::acos(std::fmax(-1.0, std::fmin(1.0, dt(cc, capC[i]))));
+                    if (ang <= capR[i] + rc + 1e-4) {
+                        if (n == 8 || i >= kSteerLeafMany) many = true;
+                        else ids[n++] = i;
+                    }
+                }
+                uint4 &cell = out.leafCells[((size_t)f * LG + iv) * LG + iu];
+                if (many) {
+                    cell = make_uint4(0xfffefffeu, 0xfffefffeu, 0xfffefffeu, 0xfffefffeu);
+                    continue;
+                }
+                uint32_t w[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
+                for (int k = 0; k < n; ++k) {
+                    const uint32_t shift = (k & 1) ? 16u : 0u;
+                    w[k >> 1] = (w[k >> 1] & ~(0xffffu << shift)) | (ids[k] << shift);
+                }
+                cell = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+    }
 
     // face locator: for every cell of a cube map over the sphere, the level-0 faces that
     // touch the cell (found by dense sampling of the cell enlarged by a margin)

@@ -40,10 +40,16 @@ struct SteerableHost {
     std::vector<int> nodeChild;        // 6 child ids per node: >= 0 node, < 0 ~leaf, INT32_MIN none
     std::vector<float4> leafPlane;     // per leaf: unit normal of the planar triangle, distance from origin
     std::vector<int4> faceCells;       // cube-map cells (6 x kSteerCells^2) x 2: up to 8 candidate level-0 faces
+    std::vector<float> rootW;          // 9 weights: the sum over all leaves (whole-sphere integral)
+    std::vector<float4> leafEdge;      // per leaf 3 inward great-circle normals (edges ab, bc, ca)
+    std::vector<uint4> leafCells;      // cube-map cells (6 x leafGrid^2): up to 8 candidate leaves as
+                                       // 16-bit ids (0xffff none); all 0xfffe: more, use the face locator
+    uint32_t leafGrid = 0;
     int root = 0;
 };
 
 constexpr int kSteerCells = 8;         // cube-map resolution of the face locator
+constexpr uint32_t kSteerLeafNone = 0xffffu, kSteerLeafMany = 0xfffeu;
 
 // rgb: env_height rows of env_width RGB float texels (row 0 at theta = 0).
 bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, SteerableHost &out, std::string &err);
