@@ -318,7 +318,7 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
     // the wavefront pipeline is the default for the NEE path tracer (3x the megakernel on the
     // benchmark scenes); the BSDF-only tracer always runs as a megakernel
     ctx->useWavefront = (opts->pipeline == PG3GPU_PIPELINE_WAVEFRONT || opts->pipeline == PG3GPU_PIPELINE_AUTO);
-    ctx->waveGrid = sms * 4;   // the wavefront queues are allocated by the first launch (ensureWave)
+    ctx->waveGrid = sms * (1024 / PG3_WAVE_BLOCK);   // queues are allocated by the first launch (ensureWave)
     if (!forBatch) {
         if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
             return bail(fail(ctx, PG3GPU_ERR_CUDA, "event create"));

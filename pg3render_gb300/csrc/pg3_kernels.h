@@ -11,6 +11,11 @@ namespace pg3 {
 
 constexpr int kMegaBlock = 128;
 
+// Threads per block of the wavefront stage kernels (a build option for occupancy sweeps).
+#ifndef PG3_WAVE_BLOCK
+#define PG3_WAVE_BLOCK 256
+#endif
+
 // pg3_megakernel.cu
 cudaError_t launchMegakernel(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                              float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,

@@ -25,12 +25,13 @@
 #include <cooperative_groups/reduce.h>
 
 #include "pg3_estimator.cuh"
+#include "pg3_kernels.h"
 
 namespace pg3 {
 
 namespace cg = cooperative_groups;
 
-constexpr int kWaveBlock = 256;
+constexpr int kWaveBlock = PG3_WAVE_BLOCK;
 enum : int { kBucketMiss = 0, kBucketLambert = 1, kBucketConductor = 2, kBucketDielectric = 3, kNumBuckets = 4 };
 constexpr uint32_t kFlagFinite = 1u << 16, kFlagRefl = 1u << 17;
 constexpr uint32_t kSlotBits = 24, kSlotMask = (1u << kSlotBits) - 1u;

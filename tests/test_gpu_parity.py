@@ -123,3 +123,29 @@ def test_chunked_launches_match_single_launch():
         with P.GpuPathTracer(_cfg(scene, 8, max_paths_in_flight=cap), seed=9) as r:
             outs.append(r.render_samples(P.renderer.kPathTracing, 3, 5))
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("case", ["c1_area_256_16spp", "c2_env_512_2spp_cdf"])
+def test_full_size_path_by_path(case, tmp_path):
+    """The benchmark scenes at their full resolution, every path compared with the oracle:
+    the area-light box at 256x256 x 16 spp, max path length 8 (exactly the C1 workload,
+    1,048,576 paths), and the environment-map box at 512x512 (2 spp, max length 12, roulette
+    after 3 bounces; the CDF sampler, since the oracle restates the reference's samplers)."""
+    if case.startswith("c1"):
+        scene, spp, maxpl, rr, sampler, seed = S.cornell_box(256, 256), 16, 8, 0, P.renderer.EM_CDF, 21
+        text = scene.to_text(max_path_length=maxpl)
+    else:
+        scene, spp, maxpl, rr, sampler, seed = S.cornell_env(512, 512, 1024, 512), 2, 12, 4, P.renderer.EM_CDF, 22
+        em = str(tmp_path / "em.bin")
+        scene.write_env_map(em)
+        text = scene.to_text(em_path=em, max_path_length=maxpl)
+    with P.GpuPathTracer(_cfg(scene, maxpl, sampler=sampler, rr_min_path_length=rr, base_seed=seed)) as r:
+        g = r.render_samples(P.renderer.kPathTracing, 0, spp)
+    o = _oracle_samples(scene, text, spp, seed, sampler=0, rr=rr)
+    assert g.shape == o.shape
+    frac = _match_fraction(g, o)
+    assert frac >= MIN_MATCH, frac
+    # and the image means agree to the statistical error of the sample count
+    gm, om = g.mean(axis=(0, 1, 2)), o.mean(axis=(0, 1, 2))
+    err = o.reshape(-1, 3).std(axis=0) / np.sqrt(o.shape[0] * o.shape[1] * o.shape[2])
+    assert np.all(np.abs(gm - om) <= 4 * err + 1e-6), (gm, om, err)
