@@ -46,8 +46,19 @@ enum {
 };
 
 /* ---- enumerations (values follow the reference where it has them) ----- */
-/* Algorithm ids of src/config.hxx:23-34 that this library renders. */
-enum { PG3GPU_ALG_PATH_TRACING_NAIVE = 6, PG3GPU_ALG_PATH_TRACING = 7 };
+/* Algorithm ids of src/config.hxx:23-34. 7 runs on the wavefront pipeline (by default), the
+ * others on the megakernel; 0-5 shade the first hit only (src/eye_light.hxx,
+ * src/normal_visualiser.hxx, src/direct_illumination.hxx). */
+enum {
+    PG3GPU_ALG_EYE_LIGHT = 0,
+    PG3GPU_ALG_NORMAL_VISUALISER = 1,
+    PG3GPU_ALG_DIRECT_BSDF_SAMPLING = 2,
+    PG3GPU_ALG_DIRECT_LIGHT_SAMPLING_ALL = 3,
+    PG3GPU_ALG_DIRECT_LIGHT_SAMPLING_SINGLE = 4,
+    PG3GPU_ALG_DIRECT_MIS = 5,
+    PG3GPU_ALG_PATH_TRACING_NAIVE = 6,
+    PG3GPU_ALG_PATH_TRACING = 7
+};
 
 enum { PG3GPU_MAT_LAMBERT = 0, PG3GPU_MAT_GGX_CONDUCTOR = 1, PG3GPU_MAT_GGX_DIELECTRIC = 2 };
 enum { PG3GPU_BG_NONE = 0, PG3GPU_BG_CONSTANT = 1, PG3GPU_BG_ENVMAP = 2 };

@@ -1112,13 +1112,162 @@ public:
         }
     }
 
-    // One sample of one pixel (src/path_tracer_base.hxx:66-87)
+    // Light sample of light `lid` from the shading point (area: src/lights.hxx:114-131;
+    // background: :424-445); u holds three uniforms.
+    void SampleLight(int lid, V3 pt, const Frame &frame, const float u[3], V3 &wig, float &dist, V3 &smp,
+                     float &pdfW) const
+    {
+        if (lid == S.bgLightId) {
+            S.BgSample(frame, u, wig, pdfW, smp);
+            dist = std::numeric_limits<float>::max();
+        } else {
+            const AreaLight &L = S.lights[lid];
+            const V3 sp = SampleUniformTriangle(L.p0, L.p0 + L.e1, L.p0 + L.e2, u[0], u[1]);
+            L.ComputeSample(pt, sp, frame, wig, dist, smp, pdfW);
+        }
+    }
+
+    // GetDirectRadianceFromDirection (src/path_tracer_base.hxx:92-154): radiance arriving
+    // along the BSDF-sampled local direction wil, its light-sampling pdf and picking probability.
+    V3 DirectFromDirection(V3 pt, const Frame &frame, V3 wil, const std::vector<float> &est, float *pdfW,
+                           float *pickProb) const
+    {
+        const V3 wig = frame.ToWorld(wil);
+        Hit h;
+        h.dist = 1e36f;
+        int lightId = -1;
+        V3 L(0.f);
+        if (S.Intersect(pt, wig, EpsRayCos(wil.z), h)) {
+            if (h.light >= 0) {
+                const V3 lightPt = pt + wig * h.dist;
+                Frame lf;
+                lf.SetFromZ(h.normal);
+                L = S.lights[h.light].Emission(lightPt, lf.ToLocal(-wig), pt, pdfW);
+                lightId = h.light;
+            }
+        } else if (S.hasBg) {
+            L = S.BgEmission(wig, pdfW, &frame);
+            lightId = S.bgLightId;
+        }
+        if (pickProb && lightId >= 0) *pickProb = PickProb(est, lightId);
+        return L;
+    }
+
+    // Direct illumination (src/direct_illumination.hxx:15-156), eye light
+    // (src/eye_light.hxx:21-60) and normal visualiser (src/normal_visualiser.hxx:21-62).
+    // Random numbers: camera jitter (vertex 0, group 0), light pick + sample (vertex 1, group 0),
+    // BSDF sample (vertex 1, group 1), light i of the all-lights estimator (vertex 1, group 2 + i).
+    V3 EstimateDirect(const PathKey &key, V3 dir) const
+    {
+        const int alg = S.algorithm;
+        Hit h;
+        h.dist = 1e36f;
+        if (!S.Intersect(S.cPos, dir, 0.f, h)) {
+            if (alg <= 1 || !S.hasBg) return V3(0.f);
+            return S.BgEmission(dir, nullptr, nullptr);
+        }
+        if (alg == 0) {
+            const float dotLN = Dot(h.normal, -dir);
+            return dotLN > 0.f ? V3(dotLN) : V3(-dotLN, 0.f, 0.f);
+        }
+        if (alg == 1)
+            return V3(Clampf(h.normal.x / 2.f + 0.5f, 0.f, 1.f), Clampf(h.normal.y / 2.f + 0.5f, 0.f, 1.f),
+                      Clampf(h.normal.z / 2.f + 0.5f, 0.f, 1.f));
+        const V3 pt = S.cPos + dir * h.dist;
+        Frame frame;
+        frame.SetFromZ(h.normal);
+        const V3 wol = frame.ToLocal(-dir);
+        const Material &mat = S.mats[h.mat];
+        std::vector<float> est;
+        if (S.LightCount() > 1) Estimates(pt, frame, est);
+        const Rand4 ra = Draw(key.seed, key.pixel, key.sample, 1, 0);
+        const Rand4 rb = Draw(key.seed, key.pixel, key.sample, 1, 1);
+        V3 Lo(0.f);
+        // AddSingleLightSampleContribution (src/path_tracer_base.hxx:315-348)
+        auto single = [&](int lid, float prob, const float u[3]) {
+            V3 wig, smp;
+            float dist, pdfW;
+            SampleLight(lid, pt, frame, u, wig, dist, smp, pdfW);
+            if (!(MaxC(smp) > 0.) || S.Occluded(pt, wig, dist)) return;
+            MatRecord mr;
+            mr.wil = frame.ToLocal(wig);
+            mr.wol = wol;
+            mat.Eval(mr);
+            Lo += smp * mr.attenuation / (pdfW * prob);
+        };
+        if (alg == 3) {
+            for (size_t i = 0; i < S.LightCount(); ++i) {
+                const Rand4 rl = Draw(key.seed, key.pixel, key.sample, 1, 2 + (uint32_t)i);
+                const float lu[3] = {rl.v[1], rl.v[2], rl.v[3]};
+                single((int)i, 1.f, lu);
+            }
+        } else if (alg == 4) {
+            int lid = -1;
+            float lprob = 0.f;
+            Pick(est, ra.v[0], lid, lprob);
+            const float lu[3] = {ra.v[1], ra.v[2], ra.v[3]};
+            if (lid >= 0) single(lid, lprob, lu);
+        } else if (alg == 2) {
+            MatRecord mr;
+            mr.wol = wol;
+            const float bu[3] = {rb.v[1], rb.v[2], rb.v[3]};
+            mat.Sample(bu, mr);
+            if (!mr.IsBlocker()) {
+                const V3 Li = DirectFromDirection(pt, frame, mr.wil, est, nullptr, nullptr);
+                Lo = mr.IsFinite() ? (mr.attenuation * mr.CosAbs() * Li) / (mr.pdfW * mr.compProb)
+                                   : (mr.attenuation * Li) / mr.compProb;
+            }
+        } else {
+            // kDirectIllumMis: one light sample and one BSDF sample (:99-114), power heuristic
+            int lid = -1;
+            float lprob = 0.f;
+            Pick(est, ra.v[0], lid, lprob);
+            if (lid >= 0) {
+                V3 wig, smp;
+                float dist, pdfW;
+                const float lu[3] = {ra.v[1], ra.v[2], ra.v[3]};
+                SampleLight(lid, pt, frame, lu, wig, dist, smp, pdfW);
+                if (MaxC(smp) > 0. && !S.Occluded(pt, wig, dist)) {   // :350-411
+                    MatRecord mr;
+                    mr.wil = frame.ToLocal(wig);
+                    mr.wol = wol;
+                    mat.Eval(mr);
+                    const float lightPdf = pdfW * lprob;
+                    Lo += (smp * mr.attenuation * MIS(lightPdf, mr.pdfW * mr.compProb)) / lightPdf;
+                }
+            }
+            MatRecord mr;   // AddDirectIllumMISBrdfSampleContribution (:427-486)
+            mr.wol = wol;
+            const float bu[3] = {rb.v[1], rb.v[2], rb.v[3]};
+            mat.Sample(bu, mr);
+            if (!mr.IsBlocker()) {
+                float lightPdfW = 0.f, pick = 0.f;
+                const V3 Li = DirectFromDirection(pt, frame, mr.wil, est, &lightPdfW, &pick);
+                if (MaxC(Li) > 0.f) {
+                    if (mr.IsFinite()) {
+                        const float bsdfPdf = mr.pdfW * mr.compProb;
+                        Lo += (mr.attenuation * mr.CosAbs() * Li * MIS(bsdfPdf, lightPdfW * pick)) / bsdfPdf;
+                    } else {
+                        Lo += (mr.attenuation * Li) / mr.compProb;
+                    }
+                }
+            }
+        }
+        V3 Le(0.f);
+        if (h.light >= 0) Le = S.lights[h.light].Emission(pt, wol, V3(0.f), nullptr);
+        return Le + Lo;
+    }
+
+    // One sample of one pixel (src/path_tracer_base.hxx:66-87; the visualisers take the pixel
+    // centre for sample 0, src/eye_light.hxx:35-37)
     V3 Radiance(uint64_t seed, uint32_t pixel, uint32_t sample) const
     {
         const PathKey key{seed, pixel, sample};
         const uint32_t x = pixel % S.W, y = pixel / S.W;
         const Rand4 rc = Draw(seed, pixel, sample, 0, 0);
-        const V3 dir = S.CameraDir((float)x + rc.v[0], (float)y + rc.v[1]);
+        const bool centre = S.algorithm <= 1 && sample == 0;
+        const V3 dir = S.CameraDir((float)x + (centre ? 0.5f : rc.v[0]), (float)y + (centre ? 0.5f : rc.v[1]));
+        if (S.algorithm <= 5) return EstimateDirect(key, dir);
         if (S.algorithm == 6) return EstimatePTN(key, S.cPos, dir);
         V3 e, r;
         EstimatePT(key, S.cPos, dir, 0.f, 1, true, e, r, nullptr, false, nullptr, nullptr);
@@ -1202,8 +1351,12 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
             s.hasBg = true; s.bgIsEm = true;
             if (!LoadEnv(p, s.em)) { err = "cannot read environment map " + p; return false; }
         } else if (k == "options") {
+            // algorithm names of the reference's command line (src/config.hxx:23-34, 292-318)
             std::string alg; ls >> alg >> s.minPL >> s.maxPL;
-            s.algorithm = (alg == "ptn") ? 6 : 7;
+            const char *names[8] = {"el", "nv", "dbs", "dlsa", "dlss", "dmis", "ptn", "pt"};
+            s.algorithm = -1;
+            for (int a = 0; a < 8; ++a) if (alg == names[a]) s.algorithm = a;
+            if (s.algorithm < 0) { err = "unknown algorithm " + alg; return false; }
         } else if (k == "sampling_material") {
             // sampling overrides of one material: GGX sampling roughness, roulette probability
             // (negative: unchanged); finite differences with the sampling held fixed

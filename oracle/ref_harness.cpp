@@ -3,8 +3,9 @@
 // Compiled by oracle/build_ref.py against a patched copy of the reference
 // headers. It builds a scene from the repository's plain-text scene file
 // directly through the reference's public Scene members
-// (src/scene.hxx:1276-1289), runs K independent reference PathTracer
-// renderers (src/path_tracer.hxx:5-14) with seeds base+i exactly like
+// (src/scene.hxx:1276-1289), runs K independent reference renderers of the
+// requested algorithm (PathTracer, src/path_tracer.hxx:5-14; DirectIllumination,
+// src/direct_illumination.hxx:5-13; EyeLight; NormalVisualiser) with seeds base+i exactly like
 // Render() does (src/pg3render.cxx:65-70, 112-128), and writes
 //   * the mean image over all K*N iterations (double RGB), and
 //   * the per-pixel variance of the K per-renderer means (for z-tests).
@@ -20,8 +21,11 @@
 //   area_light x0 y0 z0 x1 y1 z1 x2 y2 z2 material Lr Lg Lb
 //   background_const r g b
 //   background_em path
-//   options algorithm(pt|ptn) min_path_length max_path_length
+//   options algorithm(el|nv|dbs|dlsa|dlss|dmis|ptn|pt) min_path_length max_path_length
 #include "config.hxx"
+#include "direct_illumination.hxx"
+#include "eye_light.hxx"
+#include "normal_visualiser.hxx"
 #include "path_tracer.hxx"
 
 #include <chrono>
@@ -119,7 +123,10 @@ SceneFile LoadScene(const char *path, const AuxDbgParams &aux)
         } else if (kind == "options") {
             std::string alg;
             ls >> alg >> sf.minPathLength >> sf.maxPathLength;
-            sf.algorithm = (alg == "ptn") ? kPathTracingNaive : kPathTracing;
+            bool known = false;
+            for (int a = 0; a < (int)kAlgorithmCount; ++a)
+                if (alg == Config::GetAcronym((Algorithm)a)) { sf.algorithm = (Algorithm)a; known = true; }
+            if (!known) Fail("unknown algorithm " + alg);
         } else {
             Fail("unknown scene record " + kind);
         }
@@ -179,8 +186,19 @@ int main(int argc, char **argv)
     const uint32_t H = (uint32_t)sf.scene->mCamera.mResolution.y;
     const size_t npx = (size_t)W * H;
 
-    std::vector<PathTracer *> renderers(K);
-    for (int i = 0; i < K; ++i) renderers[i] = new PathTracer(config, seed + i);
+    // the renderer CreateRenderer picks for the algorithm (src/pg3render.cxx:24-50)
+    std::vector<AbstractRenderer *> renderers(K);
+    for (int i = 0; i < K; ++i) {
+        switch (sf.algorithm) {
+        case kEyeLight: renderers[i] = new EyeLight(config, seed + i); break;
+        case kNormalVisualiser: renderers[i] = new NormalVisualiser(config, seed + i); break;
+        case kDirectIllumBsdfSampling:
+        case kDirectIllumLightSamplingAll:
+        case kDirectIllumLightSamplingSingle:
+        case kDirectIllumMis: renderers[i] = new DirectIllumination(config, seed + i); break;
+        default: renderers[i] = new PathTracer(config, seed + i); break;
+        }
+    }
 
     omp_set_num_threads(T);
     const auto t0 = std::chrono::steady_clock::now();

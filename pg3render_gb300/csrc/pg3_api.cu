@@ -124,12 +124,15 @@ void foldTimers(pg3gpu_ctx *ctx)
     ctx->pendingTimers = 0;
 }
 
-int renderChunk(pg3gpu_ctx *ctx, bool naive, uint32_t sample0, uint32_t passes)
+// algorithm: 7 runs on the wavefront pipeline (unless the megakernel was chosen), the others
+// on the megakernel
+int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passes)
 {
     const uint32_t npix = ctx->W * ctx->H;
     const uint64_t paths = (uint64_t)passes * npix;
     int st = ensureOutput(ctx, paths);
-    if (!st && ctx->useWavefront && !naive) st = ensureWave(ctx, paths);
+    const bool wave = ctx->useWavefront && algorithm == PG3GPU_ALG_PATH_TRACING;
+    if (!st && wave) st = ensureWave(ctx, paths);
     if (st) return st;
     if (ctx->pendingTimers == pg3gpu_ctx::kTimerSlots) {
         cudaStreamSynchronize(ctx->stream);
@@ -139,12 +142,12 @@ int renderChunk(pg3gpu_ctx *ctx, bool naive, uint32_t sample0, uint32_t passes)
     cudaEventRecord(ctx->tStart[slot], ctx->stream);
     cudaError_t e;
     uint64_t launches = 1;
-    if (ctx->useWavefront && !naive) {   // the BSDF-only tracer always runs as a megakernel
+    if (wave) {
         launches = 0;
-        e = launchWavefront(ctx->view, naive, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
+        e = launchWavefront(ctx->view, false, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
                             ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->stream, &launches);
     } else
-        e = launchMegakernel(ctx->view, naive, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
+        e = launchMegakernel(ctx->view, algorithm, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
                              ctx->dStats, ctx->megaGrid, ctx->stream);
     if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "path kernel launch: %s", cudaGetErrorString(e));
     cudaEventRecord(ctx->tStop[slot], ctx->stream);
@@ -312,7 +315,7 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
 
     int sms = 0, perSm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (megakernelOccupancy(opts->algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE, &perSm) != cudaSuccess || perSm < 1)
+    if (megakernelOccupancy(opts->algorithm, &perSm) != cudaSuccess || perSm < 1)
         perSm = 1;
     ctx->megaGrid = sms * perSm;
     // the wavefront pipeline is the default for the NEE path tracer (3x the megakernel on the
@@ -348,17 +351,16 @@ int pg3gpu_set_stream(pg3gpu_ctx *ctx, void *stream)
 int pg3gpu_run_iteration(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp)
 {
     if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
-    if (algorithm != PG3GPU_ALG_PATH_TRACING && algorithm != PG3GPU_ALG_PATH_TRACING_NAIVE)
-        return fail(ctx, PG3GPU_ERR_UNSUPPORTED, "algorithm %d is not a path tracer", (int)algorithm);
+    if (algorithm < PG3GPU_ALG_EYE_LIGHT || algorithm > PG3GPU_ALG_PATH_TRACING)
+        return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "unknown algorithm %d", (int)algorithm);
     if (spp == 0) return PG3GPU_OK;
     cudaSetDevice(ctx->device);
-    const bool naive = algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE;
     const uint32_t npix = ctx->W * ctx->H;
     const uint32_t per = passesPerChunk(ctx, spp);
     PG3_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
     for (uint32_t done = 0; done < spp; done += per) {
         const uint32_t passes = std::min(per, spp - done);
-        int st = renderChunk(ctx, naive, iteration + done, passes);
+        int st = renderChunk(ctx, algorithm, iteration + done, passes);
         if (st) return st;
         cudaError_t e = launchAccumulate(npix, passes, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2], ctx->dSum,
                                          ctx->dSumsq, ctx->stream);
@@ -386,15 +388,15 @@ int pg3gpu_synchronize(pg3gpu_ctx *ctx)
 int pg3gpu_render_samples(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp, float *out)
 {
     if (!ctx || !out) return PG3GPU_ERR_INVALID_ARGUMENT;
-    if (algorithm != PG3GPU_ALG_PATH_TRACING && algorithm != PG3GPU_ALG_PATH_TRACING_NAIVE)
-        return fail(ctx, PG3GPU_ERR_UNSUPPORTED, "algorithm %d is not a path tracer", (int)algorithm);
+    if (algorithm < PG3GPU_ALG_EYE_LIGHT || algorithm > PG3GPU_ALG_PATH_TRACING)
+        return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "unknown algorithm %d", (int)algorithm);
     cudaSetDevice(ctx->device);
     const uint32_t npix = ctx->W * ctx->H;
     const uint32_t per = passesPerChunk(ctx, spp);
     std::vector<float> tmp[3];
     for (uint32_t done = 0; done < spp; done += per) {
         const uint32_t passes = std::min(per, spp - done);
-        int st = renderChunk(ctx, algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE, iteration + done, passes);
+        int st = renderChunk(ctx, algorithm, iteration + done, passes);
         if (st) return st;
         const size_t n = (size_t)passes * npix;
         for (int c = 0; c < 3; ++c) {
@@ -533,8 +535,8 @@ extern "C" int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, 
 {
     if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
     if (!sum_rgb || !sumsq_rgb) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "sum_rgb and sumsq_rgb are required");
-    if (algorithm != PG3GPU_ALG_PATH_TRACING && algorithm != PG3GPU_ALG_PATH_TRACING_NAIVE)
-        return fail(ctx, PG3GPU_ERR_UNSUPPORTED, "algorithm %d is not a path tracer", (int)algorithm);
+    if (algorithm < PG3GPU_ALG_EYE_LIGHT || algorithm > PG3GPU_ALG_PATH_TRACING)
+        return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "unknown algorithm %d", (int)algorithm);
     const uint32_t npix = ctx->W * ctx->H;
     if (npix > kNoAllocMaxPaths)
         return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT,
@@ -548,11 +550,10 @@ extern "C" int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, 
     // Every scratch element the accumulation reads is written by the path kernel of the same
     // chunk first, so nothing in the (shared, persistent) scratch has to start at zero.
     float *r = scratch, *g = scratch + kNoAllocMaxPaths, *b = scratch + 2 * (size_t)kNoAllocMaxPaths;
-    const bool naive = algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE;
     const uint32_t per = std::min(spp, kNoAllocMaxPaths / npix);
     for (uint32_t done = 0; done < spp; done += per) {
         const uint32_t passes = std::min(per, spp - done);
-        cudaError_t e = launchMegakernel(ctx->view, naive, iteration + done, (uint64_t)passes * npix, npix, r, g, b,
+        cudaError_t e = launchMegakernel(ctx->view, algorithm, iteration + done, (uint64_t)passes * npix, npix, r, g, b,
                                          ctx->dStats, ctx->megaGrid, ctx->stream);
         if (e == cudaSuccess) e = launchAccumulate(npix, passes, r, g, b, sum_rgb, sumsq_rgb, ctx->stream);
         if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "allocation-free launch: %s", cudaGetErrorString(e));

@@ -240,6 +240,158 @@ PG3_DI float3 tracePath(const SceneView &S, uint32_t pixel, uint32_t sample, Pat
     return L;
 }
 
+// Light sample of light `lid` (area: src/lights.hxx:114-131; background: :424-445).
+PG3_DI void sampleLightAt(const SceneView &S, int lid, float3 pt, const Frame &frame, float3 n, float u0, float u1,
+                          float u2, float3 &wig, float &dist, float3 &smp, float &pdfW)
+{
+    if (lid == S.bgLightId) {
+        bgSample(S, frame, u0, u1, u2, wig, pdfW, smp);
+        dist = kFloatMax;
+    } else {
+        areaSample(S.lights[lid], pt, n, u0, u1, wig, dist, smp, pdfW);
+    }
+}
+
+// GetDirectRadianceFromDirection (src/path_tracer_base.hxx:92-154): radiance arriving along
+// the local direction wil, its light-sampling pdf and the light's id (-1: none).
+PG3_DI float3 directFromDirection(const SceneView &S, float3 pt, const Frame &frame, float3 wil, float &pdfW,
+                                  int &lightId)
+{
+    const float3 wig = toWorld(frame, wil);
+    Hit h;
+    lightId = -1;
+    pdfW = 0.f;
+    if (intersectClosest(S, pt, wig, epsRayCos(wil.z), h)) {
+        float3 lp, ln;
+        int mat;
+        hitAttributes(S, h, pt, wig, lp, ln, mat);
+        const int lid = __ldg(&S.mat2light[mat]);
+        if (lid < 0) return f3(0.f);
+        lightId = lid;
+        return areaEmission(S.lights[lid], lp, toLocal(frameFromZ(ln), -wig).z, pt, pdfW);
+    }
+    if (S.bgKind == kBgNone) return f3(0.f);
+    lightId = S.bgLightId;
+    return bgEmission(S, wig, true, frame, pdfW);
+}
+
+// Direct illumination (algorithms 2-5, src/direct_illumination.hxx:15-156), eye light (0,
+// src/eye_light.hxx:21-60) and normal visualiser (1, src/normal_visualiser.hxx:21-62): one hit.
+// Random numbers: camera jitter (vertex 0, group 0; the visualisers take the pixel centre on
+// sample 0), light pick + sample (vertex 1, group 0), BSDF sample (vertex 1, group 1), light i
+// of the all-lights estimator (vertex 1, group 2 + i).
+PG3_DI float3 traceDirect(const SceneView &S, int alg, uint32_t pixel, uint32_t sample, PathCounters &pc)
+{
+    const uint32_t px = pixel % S.width, py = pixel / S.width;
+    const Rand4 rc = draw(S, pixel, sample, 0, 0);
+    const bool centre = alg <= 1 && sample == 0;
+    const float nx = ((float)px + (centre ? 0.5f : rc.a)) * (2.f / S.width) - 1.f;
+    const float ny = ((float)py + (centre ? 0.5f : rc.b)) * (2.f / S.height) - 1.f;
+    const float3 dir = normalize(S.camFwd + S.camRight * (nx * S.tanX) - S.camUp * (ny * S.tanY));
+    ++pc.ext;
+    Hit h;
+    if (!intersectClosest(S, S.camPos, dir, 0.f, h)) {
+        ++pc.bg;
+        if (alg <= 1 || S.bgKind == kBgNone) return f3(0.f);
+        float pdf;
+        return bgEmission(S, dir, false, frameFromZ(make_float3(0.f, 0.f, 1.f)), pdf);
+    }
+    float3 pt, n;
+    int matId;
+    hitAttributes(S, h, S.camPos, dir, pt, n, matId);
+    if (alg == 0) {
+        const float dotLN = dot(n, -dir);
+        return dotLN > 0.f ? f3(dotLN) : make_float3(-dotLN, 0.f, 0.f);
+    }
+    if (alg == 1)
+        return make_float3(clampf(n.x / 2.f + 0.5f, 0.f, 1.f), clampf(n.y / 2.f + 0.5f, 0.f, 1.f),
+                           clampf(n.z / 2.f + 0.5f, 0.f, 1.f));
+    const Frame frame = frameFromZ(n);
+    const float3 wol = toLocal(frame, -dir);
+    const DevMaterial mat = loadMat(S, matId);
+    const float sum = (S.lightCount > 1) ? estimateSum(S, pt, n) : 0.f;
+    const Rand4 ra = draw(S, pixel, sample, 1, 0);
+    const Rand4 rb = draw(S, pixel, sample, 1, 1);
+    float3 Lo = f3(0.f);
+    if (alg == 3 || alg == 4) {
+        // AddSingleLightSampleContribution (src/path_tracer_base.hxx:315-348)
+        const uint32_t count = (alg == 3) ? S.lightCount : 1u;
+        for (uint32_t k = 0; k < count; ++k) {
+            int lid;
+            float prob;
+            Rand4 rl = ra;
+            if (alg == 3) {
+                lid = (int)k;
+                prob = 1.f;
+                rl = draw(S, pixel, sample, 1, 2 + k);
+            } else {
+                pickLight(S, pt, n, sum, ra.a, lid, prob);
+                if (lid < 0) break;
+            }
+            float3 wig, smp;
+            float dist, pdfW;
+            sampleLightAt(S, lid, pt, frame, n, rl.b, rl.c, rl.d, wig, dist, smp, pdfW);
+            ++pc.shadow;
+            if (!(maxc(smp) > 0.f) || occludedAny(S, pt, wig, dist)) continue;
+            BsdfRec br;
+            evalBsdf(mat, toLocal(frame, wig), wol, br);
+            Lo += smp * br.att / (pdfW * prob);
+        }
+    } else if (alg == 2) {
+        BsdfRec br;
+        sampleBsdf(mat, wol, rb.b, rb.c, rb.d, br);
+        if (!isBlocker(br)) {
+            float pdfL;
+            int lid;
+            ++pc.ext;
+            const float3 Li = directFromDirection(S, pt, frame, br.wil, pdfL, lid);
+            Lo = (br.pdfW != infF()) ? (br.att * fabsf(br.wil.z) * Li) / (br.pdfW * br.compProb)
+                                     : (br.att * Li) / br.compProb;
+        }
+    } else {
+        // kDirectIllumMis: one light sample and one BSDF sample (:99-114)
+        int lid;
+        float lprob = 0.f;
+        pickLight(S, pt, n, sum, ra.a, lid, lprob);
+        if (lid >= 0) {
+            float3 wig, smp;
+            float dist, pdfW;
+            sampleLightAt(S, lid, pt, frame, n, ra.b, ra.c, ra.d, wig, dist, smp, pdfW);
+            ++pc.shadow;
+            if (maxc(smp) > 0.f && !occludedAny(S, pt, wig, dist)) {   // src/path_tracer_base.hxx:350-411
+                BsdfRec br;
+                evalBsdf(mat, toLocal(frame, wig), wol, br);
+                const float lightPdf = pdfW * lprob;
+                Lo += (smp * br.att) * (misPower(lightPdf, br.pdfW * br.compProb) / lightPdf);
+            }
+        }
+        BsdfRec br;   // AddDirectIllumMISBrdfSampleContribution (:427-486)
+        sampleBsdf(mat, wol, rb.b, rb.c, rb.d, br);
+        if (!isBlocker(br)) {
+            float pdfL;
+            int hitLight;
+            ++pc.ext;
+            const float3 Li = directFromDirection(S, pt, frame, br.wil, pdfL, hitLight);
+            if (maxc(Li) > 0.f) {
+                if (br.pdfW != infF()) {
+                    const float bsdfPdf = br.pdfW * br.compProb;
+                    const float pick = pickProb(S, pt, n, sum, hitLight);
+                    Lo += (br.att * fabsf(br.wil.z) * Li) * (misPower(bsdfPdf, pdfL * pick) / bsdfPdf);
+                } else {
+                    Lo += (br.att * Li) / br.compProb;
+                }
+            }
+        }
+    }
+    const int lightId = __ldg(&S.mat2light[matId]);
+    float3 Le = f3(0.f);
+    if (lightId >= 0) {
+        float pdfA;
+        Le = areaEmission(S.lights[lightId], pt, wol.z, make_float3(0.f, 0.f, 0.f), pdfA);
+    }
+    return Le + Lo;
+}
+
 // One camera path of the BSDF-sampling-only tracer (algorithm kPathTracingNaive,
 // src/path_tracer.hxx:45-165).
 PG3_DI float3 tracePathNaive(const SceneView &S, uint32_t pixel, uint32_t sample, PathCounters &pc)

@@ -83,8 +83,8 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "camera resolution must be positive and at most 2^28 pixels");
     if (!finite3(c.position) || !finite3(c.forward) || !finite3(c.up) || !(c.hfov_deg > 0.f && c.hfov_deg < 180.f))
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "camera parameters must be finite, 0 < hfov < 180");
-    if (o.algorithm != PG3GPU_ALG_PATH_TRACING && o.algorithm != PG3GPU_ALG_PATH_TRACING_NAIVE)
-        return bad(PG3GPU_ERR_UNSUPPORTED, "only the path-tracing algorithms (6, 7) are implemented");
+    if (o.algorithm < PG3GPU_ALG_EYE_LIGHT || o.algorithm > PG3GPU_ALG_PATH_TRACING)
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown algorithm (the reference's ids 0-7, src/config.hxx:23-34)");
     if (o.min_path_length < 1) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "min_path_length must be >= 1");
     // the reference rejects these combinations (src/config.hxx:1063-1077)
     if (o.max_path_length == 0 && o.min_path_length != 1)

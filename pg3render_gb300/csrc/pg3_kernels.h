@@ -17,10 +17,11 @@ constexpr int kMegaBlock = 128;
 #endif
 
 // pg3_megakernel.cu
-cudaError_t launchMegakernel(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
+// algorithm: an id of src/config.hxx:23-34 (0-7)
+cudaError_t launchMegakernel(const SceneView &S, int algorithm, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                              float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,
                              cudaStream_t stream);
-cudaError_t megakernelOccupancy(bool naive, int *blocksPerSm);
+cudaError_t megakernelOccupancy(int algorithm, int *blocksPerSm);
 cudaError_t launchAccumulate(uint32_t npix, uint32_t passes, const float *r, const float *g, const float *b,
                              double *sum, double *sumsq, cudaStream_t stream);
 

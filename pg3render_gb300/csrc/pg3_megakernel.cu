@@ -21,11 +21,12 @@ PG3_DI void flushCounters(DevStats *st, const PathCounters &c, uint32_t paths)
     }
 }
 
-template <bool kNaive>
-__global__ void __launch_bounds__(kMegaBlock) megakernel(const __grid_constant__ SceneView S, uint32_t sample0,
-                                                         uint64_t numPaths, uint32_t npix, float *__restrict__ outR,
-                                                         float *__restrict__ outG, float *__restrict__ outB,
-                                                         DevStats *stats)
+// KIND: 0 NEE+MIS path tracer (algorithm 7), 1 naive path tracer (6), 2 one-hit estimators (0-5)
+template <int KIND>
+__global__ void __launch_bounds__(kMegaBlock) megakernel(const __grid_constant__ SceneView S, int alg,
+                                                         uint32_t sample0, uint64_t numPaths, uint32_t npix,
+                                                         float *__restrict__ outR, float *__restrict__ outG,
+                                                         float *__restrict__ outB, DevStats *stats)
 {
     PathCounters pc;
     uint32_t done = 0;
@@ -33,7 +34,9 @@ __global__ void __launch_bounds__(kMegaBlock) megakernel(const __grid_constant__
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < numPaths; i += stride) {
         const uint32_t pixel = (uint32_t)(i % npix);
         const uint32_t sample = sample0 + (uint32_t)(i / npix);
-        const float3 L = kNaive ? tracePathNaive(S, pixel, sample, pc) : tracePath(S, pixel, sample, pc);
+        const float3 L = (KIND == 1)   ? tracePathNaive(S, pixel, sample, pc)
+                         : (KIND == 2) ? traceDirect(S, alg, pixel, sample, pc)
+                                       : tracePath(S, pixel, sample, pc);
         outR[i] = L.x;
         outG[i] = L.y;
         outB[i] = L.z;
@@ -71,21 +74,24 @@ __global__ void __launch_bounds__(256) accumulateKernel(uint32_t npix, uint32_t 
     }
 }
 
-cudaError_t launchMegakernel(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
+cudaError_t launchMegakernel(const SceneView &S, int algorithm, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                              float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,
                              cudaStream_t stream)
 {
-    if (naive)
-        megakernel<true><<<gridBlocks, kMegaBlock, 0, stream>>>(S, sample0, numPaths, npix, outR, outG, outB, stats);
+    if (algorithm == 6)
+        megakernel<1><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats);
+    else if (algorithm == 7)
+        megakernel<0><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats);
     else
-        megakernel<false><<<gridBlocks, kMegaBlock, 0, stream>>>(S, sample0, numPaths, npix, outR, outG, outB, stats);
+        megakernel<2><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats);
     return cudaGetLastError();
 }
 
-cudaError_t megakernelOccupancy(bool naive, int *blocksPerSm)
+cudaError_t megakernelOccupancy(int algorithm, int *blocksPerSm)
 {
-    return naive ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, megakernel<true>, kMegaBlock, 0)
-                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, megakernel<false>, kMegaBlock, 0);
+    if (algorithm == 6) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, megakernel<1>, kMegaBlock, 0);
+    if (algorithm == 7) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, megakernel<0>, kMegaBlock, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSm, megakernel<2>, kMegaBlock, 0);
 }
 
 cudaError_t launchAccumulate(uint32_t npix, uint32_t passes, const float *r, const float *g, const float *b,

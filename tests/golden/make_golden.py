@@ -34,6 +34,16 @@ CASES = {
     "cornell_area_32_rr": (lambda: S.cornell_box(32, 32), 0, "cdf", "pt", 64, 128),
     "cornell_env_32_cdf": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cdf", "pt", 64, 128),
     "cornell_env_32_cos": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cosine", "pt", 64, 128),
+    # direct illumination, eye light, normal visualiser (one hit; src/direct_illumination.hxx,
+    # src/eye_light.hxx, src/normal_visualiser.hxx)
+    "cornell_area_32_dbs": (lambda: S.cornell_box(32, 32), 8, "cdf", "dbs", 64, 128),
+    "cornell_area_32_dlsa": (lambda: S.cornell_box(32, 32), 8, "cdf", "dlsa", 64, 128),
+    "cornell_area_32_dlss": (lambda: S.cornell_box(32, 32), 8, "cdf", "dlss", 64, 128),
+    "cornell_area_32_dmis": (lambda: S.cornell_box(32, 32), 8, "cdf", "dmis", 64, 128),
+    "cornell_env_32_dmis_cdf": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cdf", "dmis", 64, 128),
+    "cornell_env_32_dbs": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cdf", "dbs", 64, 128),
+    "cornell_area_32_el": (lambda: S.cornell_box(32, 32), 8, "cdf", "el", 16, 512),
+    "cornell_area_32_nv": (lambda: S.cornell_box(32, 32), 8, "cdf", "nv", 16, 512),
 }
 
 EM_TOKEN = "@EM@"

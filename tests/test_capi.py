@@ -58,7 +58,7 @@ def _create(scene, **opt):
 @pytest.mark.parametrize("opt,status,msg", [
     (dict(splitting_budget=4), _lib.ERR_UNSUPPORTED, "splitting"),
     (dict(indirect_clipping=16.0), _lib.ERR_UNSUPPORTED, "clipping"),
-    (dict(algorithm=5), _lib.ERR_UNSUPPORTED, "path-tracing"),
+    (dict(algorithm=8), _lib.ERR_INVALID_ARGUMENT, "unknown algorithm"),
     (dict(min_path_length=9), _lib.ERR_INVALID_ARGUMENT, "min path length"),
     (dict(min_path_length=0), _lib.ERR_INVALID_ARGUMENT, "min_path_length"),
     (dict(max_path_length=0, min_path_length=2), _lib.ERR_INVALID_ARGUMENT, "Russian roulette"),

@@ -17,7 +17,12 @@ from _util import load_golden, scene_from_golden, z_ok, zscores
 pytestmark = pytest.mark.gpu
 
 GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr",
-                "cornell_env_32_cdf", "cornell_env_32_cos"]
+                "cornell_env_32_cdf", "cornell_env_32_cos",
+                "cornell_area_32_dbs", "cornell_area_32_dlsa", "cornell_area_32_dlss", "cornell_area_32_dmis",
+                "cornell_env_32_dmis_cdf", "cornell_env_32_dbs", "cornell_area_32_el", "cornell_area_32_nv"]
+VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
+# the reference's acronyms of its algorithm ids (src/config.hxx:147-170)
+ALG_IDS = {"el": 0, "nv": 1, "dbs": 2, "dlsa": 3, "dlss": 4, "dmis": 5, "ptn": 6, "pt": 7}
 SAMPLERS = {"cdf": P.renderer.EM_CDF, "cosine": P.renderer.EM_COSINE}
 
 # Path-by-path tolerance: per sample and channel |gpu - oracle| <= 1e-3 * max(1, |oracle|)
@@ -40,6 +45,26 @@ def _oracle_samples(scene, text, spp, seed, sampler=0, rr=0):
 def _match_fraction(g, o):
     ok = np.abs(g - o) <= REL_TOL * np.maximum(1.0, np.abs(o))
     return float(ok.mean())
+
+
+@pytest.mark.parametrize("alg", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("env", [False, True])
+def test_one_hit_algorithms_path_by_path(alg, env, tmp_path):
+    """Eye light, normal visualiser and the four direct-illumination estimators against the
+    oracle, sample by sample (same Philox numbers), on the area-light and the map scene."""
+    scene = S.cornell_env(24, 24, 64, 32) if env else S.cornell_box(24, 24)
+    em = str(tmp_path / "em.bin")
+    if env:
+        scene.write_env_map(em)
+    names = ["el", "nv", "dbs", "dlsa", "dlss", "dmis"]
+    text = scene.to_text(em_path=em, algorithm=names[alg], max_path_length=8)
+    seed = 31
+    with P.GpuPathTracer(_cfg(scene, 8, alg, P.renderer.EM_CDF), seed=seed) as r:
+        g = r.render_samples(alg, 0, 8)
+    o = _oracle_samples(scene, text, 8, seed, 0)
+    frac = _match_fraction(g, o)
+    assert frac >= MIN_MATCH, "only %.4f of samples match the oracle" % frac
+    assert np.isfinite(g).all() and g.max() > 0
 
 
 @pytest.mark.parametrize("case", ["area", "area_naive", "env_cdf", "env_cos"])
@@ -69,7 +94,7 @@ def test_path_by_path_vs_oracle(case, tmp_path):
 def test_against_reference_golden(name):
     d, text, td = load_golden(name)
     scene = scene_from_golden(d)
-    alg = P.renderer.kPathTracingNaive if str(d["algorithm"]) == "ptn" else P.renderer.kPathTracing
+    alg = ALG_IDS[str(d["algorithm"])]
     cfg = _cfg(scene, int(d["max_path_length"]), alg, SAMPLERS[str(d["em_sampler"])])
     spp = 32768   # heavy-tailed estimators (naive, cosine sky sampling) need many samples
     with P.GpuPathTracer(cfg, seed=2024) as r:
@@ -79,7 +104,8 @@ def test_against_reference_golden(name):
     z = zscores(mean, var / spp, d["mean"], d["var_mean"])
     frac, zm, zs = z_ok(z)
     assert frac >= 0.999, "%s: only %.4f of |z| <= 4 (mean z %.3f, std %.3f)" % (name, frac, zm, zs)
-    assert abs(zm) < 0.25 and 0.7 < zs < 1.3, "%s: z distribution off (mean %.3f, std %.3f)" % (name, zm, zs)
+    if name not in VISUALISERS:   # (deterministic inside a surface: no z distribution there)
+        assert abs(zm) < 0.25 and 0.7 < zs < 1.3, "%s: z distribution off (mean %.3f, std %.3f)" % (name, zm, zs)
 
 
 def test_bvh_and_list_traversal_identical():

@@ -17,7 +17,12 @@ import oracle as O
 from _util import load_golden, z_ok, zscores
 
 GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr",
-                "cornell_env_32_cdf", "cornell_env_32_cos"]
+                "cornell_env_32_cdf", "cornell_env_32_cos",
+                "cornell_area_32_dbs", "cornell_area_32_dlsa", "cornell_area_32_dlss", "cornell_area_32_dmis",
+                "cornell_env_32_dmis_cdf", "cornell_env_32_dbs", "cornell_area_32_el", "cornell_area_32_nv"]
+# the visualisers are deterministic inside a surface (zero variance): only the fraction of
+# |z| <= 4 is a meaningful statistic for them
+VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
 
 
 def test_philox_known_answers():
@@ -33,15 +38,18 @@ def test_philox_known_answers():
 def test_oracle_matches_reference_golden(name):
     d, text, td = load_golden(name)
     sampler = {"cdf": O.EM_CDF, "cosine": O.EM_COSINE}[str(d["em_sampler"])]
-    # BSDF-only sampling of a small light, and cosine sampling of a sky with 1e4 suns, are
-    # heavy-tailed: their sample variances need more samples before the z-test is calibrated
-    spp = {"cornell_area_32_naive": 8192, "cornell_env_32_cos": 16384}.get(name, 1024)
+    # BSDF-only sampling of a small light (naive path tracing, dbs), and cosine sampling of a
+    # sky with 1e4 suns, are heavy-tailed: their sample variances need more samples before
+    # the z-test is calibrated
+    spp = {"cornell_area_32_naive": 8192, "cornell_env_32_cos": 16384, "cornell_area_32_dbs": 8192,
+           "cornell_env_32_dbs": 8192}.get(name, 1024)
     o = O.render(text, 32, 32, seed=99, spp=spp, em_sampler=sampler)
     m = o["sum"] / spp
     v = np.maximum(o["sumsq"] / spp - m * m, 0.0) / spp
     frac, zm, zs = z_ok(zscores(m, v, d["mean"], d["var_mean"]))
     assert frac >= 0.999, "%s: %.4f of |z| <= 4" % (name, frac)
-    assert abs(zm) < 0.25 and 0.7 < zs < 1.3, "%s: z mean %.3f std %.3f" % (name, zm, zs)
+    if name not in VISUALISERS:
+        assert abs(zm) < 0.25 and 0.7 < zs < 1.3, "%s: z mean %.3f std %.3f" % (name, zm, zs)
 
 
 def test_oracle_deterministic_and_sample_indexed():
