@@ -125,8 +125,8 @@ typedef struct pg3gpu_options {
     uint32_t max_path_length;        /* mMaxPathLength; 0 = Russian roulette ends paths */
     uint32_t rr_min_path_length;     /* extension: >0 applies Russian roulette from this path length
                                         on even when max_path_length is set; 0 = reference rule */
-    float indirect_clipping;         /* mIndirectIllumClipping; only 0 is implemented */
-    uint32_t splitting_budget;       /* mSplittingBudget; only 1 is implemented */
+    float indirect_clipping;         /* mIndirectIllumClipping (0: off; the reference's default is 16) */
+    uint32_t splitting_budget;       /* mSplittingBudget, 1..64 (the reference's default is 4) */
     int32_t em_sampler;              /* PG3GPU_EM_* */
     int32_t traversal;               /* PG3GPU_TRAVERSAL_* */
     int32_t pipeline;                /* PG3GPU_PIPELINE_* */
@@ -134,8 +134,14 @@ typedef struct pg3gpu_options {
     uint64_t seed;                   /* mBaseSeed: keys every random stream */
     uint32_t max_paths_in_flight;    /* 0 = automatic; upper bound on paths per launch chunk */
     int32_t ggx_sampler;             /* PG3GPU_GGX_*: visible-normal sampling of the GGX materials */
-    uint32_t reserved[4];
+    float splitting_level;           /* mDbgSplittingLevel in [0, 1] (1: the whole budget at the first vertex) */
+    float light_to_bsdf_ratio;       /* mDbgSplittingLightToBrdfSmplRatio, > 0 */
+    uint32_t reserved[2];
 } pg3gpu_options;
+/* With a splitting budget above 1, indirect clipping, or a light-to-BSDF ratio that gives more
+ * than one light sample per vertex, algorithm 7 runs the reference's recursive estimator with
+ * its tree of sub-paths (src/path_tracer.hxx:167-454) on the megakernel; batches and the
+ * differentiable entry points reject these options. */
 
 /* GGX visible-normal sampling: exact (Heitz 2018, default) or the reference's routine with its
  * rational fit of the slope CDF (src/microfacet.hxx:610-729), which is approximate in its tails. */
@@ -162,7 +168,8 @@ typedef struct pg3gpu_stats {
 typedef struct pg3gpu_ctx pg3gpu_ctx;
 
 /* Fills opts with the reference's unbiased defaults for this path:
- * algorithm PT, min 1, max 0 (RR), clipping 0, splitting 1, CDF sampler. */
+ * algorithm PT, min 1, max 0 (RR), clipping 0, splitting 1 (level 1, light-to-BSDF ratio 1),
+ * CDF sampler. (The reference's command line defaults to -sb 4 -iic 16.) */
 void pg3gpu_default_options(pg3gpu_options *opts);
 
 /* Uploads the scene, builds the acceleration structure and the light-sampling

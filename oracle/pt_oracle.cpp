@@ -842,6 +842,9 @@ struct Scene {
     int bgLightId = -1;
     int algorithm = 7;    // kPathTracing (src/config.hxx:23-34)
     uint32_t minPL = 1, maxPL = 8, rrMinPL = 0;
+    // splitting budget, level, light-to-BSDF sample ratio, indirect clipping (src/config.hxx:1129-1133)
+    uint32_t splitBudget = 1;
+    float splitLevel = 1.f, lightRatio = 1.f, clipping = 0.f;
 
     size_t LightCount() const { return lights.size() + (hasBg ? 1 : 0); }
 
@@ -962,10 +965,29 @@ public:
     // MISWeight2Power (src/path_tracer_base.hxx:522-541), both counts 1
     static float MIS(float a, float b) { const float a2 = a * a, b2 = b * b; return a2 / (a2 + b2) / 1; }
 
-    // EstimateIncomingRadiancePT (src/path_tracer.hxx:167-430) with splitting 1 and no clipping.
-    // 'vertex' is the index of the surface vertex this ray hits (camera ray -> 1).
+    // MISWeight2Power with sample counts (src/path_tracer_base.hxx:522-541)
+    static float MISn(float p1, uint32_t n1, float p2, uint32_t n2)
+    {
+        const float s1 = n1 * p1, s2 = n2 * p2;
+        const float q1 = s1 * s1, q2 = s2 * s2;
+        return q1 / (q1 + q2) / n1;
+    }
+
+    // ComputeSplittingCounts (src/path_tracer.hxx:432-454)
+    void SplittingCounts(float budget, uint32_t &nBsdf, uint32_t &nLight, float &nextBudget) const
+    {
+        nBsdf = (uint32_t)std::lroundf((1.f - S.splitLevel) * 1.f + S.splitLevel * budget);
+        nLight = (uint32_t)std::lroundf(std::max(S.lightRatio * nBsdf, 1.f));
+        nextBudget = 1 + ((budget - nBsdf) / (float)nBsdf);
+    }
+
+    // EstimateIncomingRadiancePT (src/path_tracer.hxx:167-430), with splitting (:240-248,
+    // 432-454) and indirect clipping (:400-402). Random numbers are keyed by the vertex's
+    // preorder index in the path tree (1 for the camera ray's hit; a chain without splitting
+    // gives index = path length): light sample j draws group 2j, BSDF sample i group 2i+1.
     void EstimatePT(const PathKey &key, V3 org, V3 dir, float tmin, uint32_t pathLength, bool computeRefl,
-                    V3 &emitted, V3 &reflected, const Frame *shFrame, bool havePdf, float *emPdf, int *emLight) const
+                    float budget, uint32_t &vid, V3 &emitted, V3 &reflected, const Frame *shFrame, bool havePdf,
+                    float *emPdf, int *emLight) const
     {
         emitted = V3(0.f);
         reflected = V3(0.f);
@@ -991,30 +1013,27 @@ public:
         if (mat.IsReflectanceZero()) return;
         if (S.maxPL > 0 && pathLength >= S.maxPL) return;
         if (pathLength >= 1200) return;   // kMaxPathLengthHard (src/path_tracer.hxx:461-462)
+        const uint32_t me = ++vid;
 
-        const Rand4 ra = Draw(key.seed, key.pixel, key.sample, pathLength, 0);
-        const Rand4 rb = Draw(key.seed, key.pixel, key.sample, pathLength, 1);
+        uint32_t nBsdf, nLight;
+        float nextBudget;
+        SplittingCounts(budget, nBsdf, nLight, nextBudget);
 
         std::vector<float> est;
         if (S.LightCount() > 1) Estimates(pt, frame, est);
 
-        // Light sample + MIS (src/path_tracer.hxx:250-265, src/path_tracer_base.hxx:156-188, 350-411)
+        // Light samples + MIS (src/path_tracer.hxx:250-265, src/path_tracer_base.hxx:156-188, 350-411)
         if (pathLength + 1 >= S.minPL) {
-            int lid = -1;
-            float lprob = 0.f;
-            Pick(est, ra.v[0], lid, lprob);
-            if (lid >= 0) {
+            for (uint32_t j = 0; j < nLight; ++j) {
+                const Rand4 ra = Draw(key.seed, key.pixel, key.sample, me, 2 * j);
+                int lid = -1;
+                float lprob = 0.f;
+                Pick(est, ra.v[0], lid, lprob);
+                if (lid < 0) continue;
                 V3 wig, smp;
                 float dist, pdfW;
                 const float lu[3] = {ra.v[1], ra.v[2], ra.v[3]};
-                if (lid == S.bgLightId) {
-                    S.BgSample(frame, lu, wig, pdfW, smp);
-                    dist = std::numeric_limits<float>::max();
-                } else {
-                    const AreaLight &L = S.lights[lid];
-                    const V3 sp = SampleUniformTriangle(L.p0, L.p0 + L.e1, L.p0 + L.e2, lu[0], lu[1]);
-                    L.ComputeSample(pt, sp, frame, wig, dist, smp, pdfW);
-                }
+                SampleLight(lid, pt, frame, lu, wig, dist, smp, pdfW);
                 if (MaxC(smp) > 0. && !S.Occluded(pt, wig, dist)) {
                     MatRecord mr;
                     mr.wil = frame.ToLocal(wig);
@@ -1022,50 +1041,52 @@ public:
                     mat.Eval(mr);
                     const float bsdfPdf = mr.pdfW * mr.compProb;
                     const float lightPdf = pdfW * lprob;
-                    reflected += (smp * mr.attenuation * MIS(lightPdf, bsdfPdf)) / lightPdf;
+                    reflected += (smp * mr.attenuation * MISn(lightPdf, nLight, bsdfPdf, nBsdf)) / lightPdf;
                 }
             }
         }
 
         // Russian roulette (src/path_tracer.hxx:267-303)
         const bool rrActive = (S.maxPL == 0) || (S.rrMinPL > 0 && pathLength >= S.rrMinPL);
-        float rrProb = 1.0f;
-        bool cut = false;
-        if (rrActive) {
-            rrProb = Clampf(mat.RRContinuationProb(), 0.0f, 0.997f);
-            if (rb.v[0] > rrProb) cut = true;
-        }
+        const float rrProb = rrActive ? Clampf(mat.RRContinuationProb(), 0.0f, 0.997f) : 1.0f;
 
-        // BSDF sample + recursion (src/path_tracer.hxx:305-322)
-        MatRecord mr;
-        mr.wol = wol;
-        const float bu[3] = {rb.v[1], rb.v[2], rb.v[3]};
-        mat.Sample(bu, mr);
-        if (mr.IsBlocker()) return;
-        const V3 wig = frame.ToWorld(mr.wil);
-        const float rayMin = EpsRayCos(mr.CosAbs());
-        V3 bEm, bRefl;
-        float bPdf = 0.f;
-        int bLight = -1;
-        EstimatePT(key, pt, wig, rayMin, pathLength + 1, !cut, bEm, bRefl, &frame, true, &bPdf, &bLight);
-
-        // Direct light hit by the BSDF sample (:327-369)
-        if (!IsZero(bEm) && bLight >= 0) {
-            if (mr.IsFinite()) {
-                const float pp = PickProb(est, bLight);
-                const float lightPdf = bPdf * pp;
-                const float bsdfPdf = mr.pdfW * mr.compProb;
-                reflected += (mr.attenuation * mr.CosAbs() * bEm * MIS(bsdfPdf, lightPdf)) / bsdfPdf;
-            } else {
-                reflected += (mr.attenuation * bEm) / (1.f * mr.compProb);
+        // BSDF samples (src/path_tracer.hxx:305-405)
+        for (uint32_t i = 0; i < nBsdf; ++i) {
+            const Rand4 rb = Draw(key.seed, key.pixel, key.sample, me, 2 * i + 1);
+            const bool cut = rrActive && rb.v[0] > rrProb;
+            MatRecord mr;
+            mr.wol = wol;
+            const float bu[3] = {rb.v[1], rb.v[2], rb.v[3]};
+            mat.Sample(bu, mr);
+            if (mr.IsBlocker()) continue;
+            const V3 wig = frame.ToWorld(mr.wil);
+            const float rayMin = EpsRayCos(mr.CosAbs());
+            V3 bEm, bRefl;
+            float bPdf = 0.f;
+            int bLight = -1;
+            EstimatePT(key, pt, wig, rayMin, pathLength + 1, !cut, nextBudget, vid, bEm, bRefl, &frame, true, &bPdf,
+                       &bLight);
+            // Direct light hit by the BSDF sample (:327-369)
+            if (!IsZero(bEm) && bLight >= 0) {
+                if (mr.IsFinite()) {
+                    const float lightPdf = bPdf * PickProb(est, bLight);
+                    const float bsdfPdf = mr.pdfW * mr.compProb;
+                    reflected += (mr.attenuation * mr.CosAbs() * bEm * MISn(bsdfPdf, nBsdf, lightPdf, nLight)) / bsdfPdf;
+                } else {
+                    reflected += (mr.attenuation * bEm) / ((float)nBsdf * mr.compProb);
+                }
             }
-        }
-        // Indirect light (:372-405)
-        if (!cut && !IsZero(bRefl)) {
-            if (mr.IsFinite())
-                reflected += (mr.attenuation * mr.CosAbs() * bRefl) / (mr.pdfW * 1.f * rrProb * mr.compProb);
-            else
-                reflected += (mr.attenuation * bRefl) / (1.f * rrProb * mr.compProb);
+            // Indirect light (:372-405), clipped proportionally (src/math.hxx:538-549)
+            if (!cut && !IsZero(bRefl)) {
+                V3 ind = mr.IsFinite()
+                             ? (mr.attenuation * mr.CosAbs() * bRefl) / (mr.pdfW * nBsdf * rrProb * mr.compProb)
+                             : (mr.attenuation * bRefl) / (nBsdf * rrProb * mr.compProb);
+                if (S.clipping > 0.f) {
+                    const float mx = MaxC(ind);
+                    if (mx > S.clipping) ind = ind * (S.clipping / mx);
+                }
+                reflected += ind;
+            }
         }
     }
 
@@ -1270,7 +1291,8 @@ public:
         if (S.algorithm <= 5) return EstimateDirect(key, dir);
         if (S.algorithm == 6) return EstimatePTN(key, S.cPos, dir);
         V3 e, r;
-        EstimatePT(key, S.cPos, dir, 0.f, 1, true, e, r, nullptr, false, nullptr, nullptr);
+        uint32_t vid = 0;
+        EstimatePT(key, S.cPos, dir, 0.f, 1, true, (float)S.splitBudget, vid, e, r, nullptr, false, nullptr, nullptr);
         return e + r;
     }
 
@@ -1357,6 +1379,13 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
             s.algorithm = -1;
             for (int a = 0; a < 8; ++a) if (alg == names[a]) s.algorithm = a;
             if (s.algorithm < 0) { err = "unknown algorithm " + alg; return false; }
+            // optional: splitting budget, splitting level, light-to-BSDF ratio, indirect clipping
+            uint32_t sb;
+            float lvl, ratio, clip;
+            if (ls >> sb >> lvl >> ratio >> clip) {
+                if (sb < 1) { err = "splitting budget must be >= 1"; return false; }
+                s.splitBudget = sb; s.splitLevel = lvl; s.lightRatio = ratio; s.clipping = clip;
+            }
         } else if (k == "sampling_material") {
             // sampling overrides of one material: GGX sampling roughness, roulette probability
             // (negative: unchanged); finite differences with the sampling held fixed

@@ -22,6 +22,7 @@
 //   background_const r g b
 //   background_em path
 //   options algorithm(el|nv|dbs|dlsa|dlss|dmis|ptn|pt) min_path_length max_path_length
+//           [splitting_budget splitting_level light_to_bsdf_ratio indirect_clipping]
 #include "config.hxx"
 #include "direct_illumination.hxx"
 #include "eye_light.hxx"
@@ -44,6 +45,8 @@ struct SceneFile {
     Algorithm algorithm = kPathTracing;
     uint32_t minPathLength = 1;
     uint32_t maxPathLength = 0;
+    uint32_t splittingBudget = 1;
+    float splittingLevel = 1.f, lightToBrdfRatio = 1.f, clipping = 0.f;
 };
 
 void Fail(const std::string &msg)
@@ -127,6 +130,14 @@ SceneFile LoadScene(const char *path, const AuxDbgParams &aux)
             for (int a = 0; a < (int)kAlgorithmCount; ++a)
                 if (alg == Config::GetAcronym((Algorithm)a)) { sf.algorithm = (Algorithm)a; known = true; }
             if (!known) Fail("unknown algorithm " + alg);
+            uint32_t sb;
+            float lvl, ratio, clip;
+            if (ls >> sb >> lvl >> ratio >> clip) {
+                sf.splittingBudget = sb;
+                sf.splittingLevel = lvl;
+                sf.lightToBrdfRatio = ratio;
+                sf.clipping = clip;
+            }
         } else {
             Fail("unknown scene record " + kind);
         }
@@ -167,16 +178,17 @@ int main(int argc, char **argv)
 
     SceneFile sf = LoadScene(scenePath, aux);
 
-    // Options as the reference's Config carries them (src/config.hxx:1100-1137); -sb 1 -iic 0.
+    // Options as the reference's Config carries them (src/config.hxx:1100-1137); -sb 1 -iic 0
+    // unless the scene file's options record gives them.
     Config config;
     config.mScene = sf.scene;
     config.mAlgorithm = sf.algorithm;
     config.mMinPathLength = sf.minPathLength;
     config.mMaxPathLength = sf.maxPathLength;
-    config.mIndirectIllumClipping = 0.f;
-    config.mSplittingBudget = 1;
-    config.mDbgSplittingLevel = 1.f;
-    config.mDbgSplittingLightToBrdfSmplRatio = 1.f;
+    config.mIndirectIllumClipping = sf.clipping;
+    config.mSplittingBudget = sf.splittingBudget;
+    config.mDbgSplittingLevel = sf.splittingLevel;
+    config.mDbgSplittingLightToBrdfSmplRatio = sf.lightToBrdfRatio;
     config.mIterations = N;
     config.mNumThreads = T;
     config.mQuietMode = true;

@@ -64,7 +64,8 @@ class Options(ctypes.Structure):
                 ("em_sampler", ctypes.c_int32), ("traversal", ctypes.c_int32), ("pipeline", ctypes.c_int32),
                 ("steer_subdiv_level", ctypes.c_uint32), ("seed", ctypes.c_uint64),
                 ("max_paths_in_flight", ctypes.c_uint32), ("ggx_sampler", ctypes.c_int32),
-                ("reserved", ctypes.c_uint32 * 4)]
+                ("splitting_level", ctypes.c_float), ("light_to_bsdf_ratio", ctypes.c_float),
+                ("reserved", ctypes.c_uint32 * 2)]
 
 
 class Stats(ctypes.Structure):

@@ -105,6 +105,23 @@ int ensureWave(pg3gpu_ctx *ctx, uint64_t paths)
     return PG3GPU_OK;
 }
 
+// Frame stacks of the recursive estimator: one stack of (max path length or the hard limit)
+// frames per thread, at most 2 GiB, so deep roulette paths get fewer resident threads.
+int ensureTree(pg3gpu_ctx *ctx)
+{
+    if (ctx->dTree) return PG3GPU_OK;
+    const uint32_t depth = ctx->view.maxPL > 0 ? ctx->view.maxPL : 1200u;
+    const uint64_t perThread = (uint64_t)depth * sizeof(TreeFrame);
+    uint64_t threads = std::min<uint64_t>((uint64_t)ctx->megaGrid * kMegaBlock, (2ull << 30) / perThread);
+    threads = std::max<uint64_t>(kMegaBlock, threads / kMegaBlock * kMegaBlock);
+    TreeFrame *t = nullptr;
+    if (int st = devAlloc(ctx, &t, threads * depth)) return st;
+    ctx->dTree = t;
+    ctx->treeDepth = depth;
+    ctx->treeGrid = (int)(threads / kMegaBlock);
+    return PG3GPU_OK;
+}
+
 // Paths per launch chunk: whole sample passes, bounded by max_paths_in_flight.
 uint32_t passesPerChunk(const pg3gpu_ctx *ctx, uint32_t spp)
 {
@@ -131,8 +148,10 @@ int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passe
     const uint32_t npix = ctx->W * ctx->H;
     const uint64_t paths = (uint64_t)passes * npix;
     int st = ensureOutput(ctx, paths);
-    const bool wave = ctx->useWavefront && algorithm == PG3GPU_ALG_PATH_TRACING;
+    const bool tree = algorithm == PG3GPU_ALG_PATH_TRACING && ctx->view.treeMode;
+    const bool wave = ctx->useWavefront && algorithm == PG3GPU_ALG_PATH_TRACING && !tree;
     if (!st && wave) st = ensureWave(ctx, paths);
+    if (!st && tree) st = ensureTree(ctx);
     if (st) return st;
     if (ctx->pendingTimers == pg3gpu_ctx::kTimerSlots) {
         cudaStreamSynchronize(ctx->stream);
@@ -148,7 +167,8 @@ int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passe
                             ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->stream, &launches);
     } else
         e = launchMegakernel(ctx->view, algorithm, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
-                             ctx->dStats, ctx->megaGrid, ctx->stream);
+                             ctx->dStats, tree ? ctx->treeGrid : ctx->megaGrid, ctx->stream, ctx->dTree,
+                             ctx->treeDepth);
     if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "path kernel launch: %s", cudaGetErrorString(e));
     cudaEventRecord(ctx->tStop[slot], ctx->stream);
     ctx->kernelLaunches += 1;
@@ -170,6 +190,8 @@ void pg3gpu_default_options(pg3gpu_options *o)
     o->rr_min_path_length = 0;
     o->indirect_clipping = 0.f;
     o->splitting_budget = 1;
+    o->splitting_level = 1.f;
+    o->light_to_bsdf_ratio = 1.f;
     o->em_sampler = PG3GPU_EM_CDF;
     o->traversal = PG3GPU_TRAVERSAL_AUTO;
     o->pipeline = PG3GPU_PIPELINE_AUTO;
@@ -381,7 +403,9 @@ int pg3gpu_synchronize(pg3gpu_ctx *ctx)
     foldTimers(ctx);
     unsigned int flag = 0;
     PG3_CUDA(ctx, cudaMemcpy(&flag, ctx->dErr, sizeof flag, cudaMemcpyDeviceToHost));
-    if (flag) return fail(ctx, PG3GPU_ERR_DEVICE_LIMIT, "kernel limit flag 0x%x (1: BVH stack, 2: queue, 4: steerable descent)", flag);
+    if (flag)
+        return fail(ctx, PG3GPU_ERR_DEVICE_LIMIT,
+                    "kernel limit flag 0x%x (1: BVH stack, 2: queue, 4: steerable descent, 16: estimator tree)", flag);
     return PG3GPU_OK;
 }
 
@@ -542,6 +566,9 @@ extern "C" int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, 
         return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT,
                     "image of %u pixels exceeds the %u-path scratch area of pg3gpu_run_iteration_noalloc", npix,
                     kNoAllocMaxPaths);
+    if (algorithm == PG3GPU_ALG_PATH_TRACING && ctx->view.treeMode)
+        return fail(ctx, PG3GPU_ERR_UNSUPPORTED,
+                    "splitting / clipping keep frame stacks in device memory: use pg3gpu_run_iteration");
     if (spp == 0) return PG3GPU_OK;
     PG3_CUDA(ctx, cudaSetDevice(ctx->device));
     float *scratch = nullptr;

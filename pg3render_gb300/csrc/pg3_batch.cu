@@ -628,6 +628,8 @@ int pg3gpu_batch_create(const pg3gpu_scene *scenes, const pg3gpu_options *opts, 
         if (opts[i].algorithm != PG3GPU_ALG_PATH_TRACING)
             return bail(bfail(b, PG3GPU_ERR_UNSUPPORTED, who + "batches render algorithm 7 (path tracing) only"));
         if (spp[i] == 0) return bail(bfail(b, PG3GPU_ERR_INVALID_ARGUMENT, who + "spp must be positive"));
+        if (opts[i].splitting_budget > 1 || opts[i].indirect_clipping > 0.f || opts[i].light_to_bsdf_ratio >= 1.5f)
+            return bail(bfail(b, PG3GPU_ERR_UNSUPPORTED, who + "batches do not split paths or clip"));
     }
     int emk = -1;
     for (uint32_t i = 0; i < n; ++i) {

@@ -14,6 +14,7 @@
 struct pg3gpu_ctx {
     using SceneView = pg3::SceneView;
     using DevStats = pg3::DevStats;
+    using TreeFrame = pg3::TreeFrame;
     int device = 0;
     cudaStream_t stream = nullptr;
     pg3gpu_options opts{};
@@ -42,6 +43,11 @@ struct pg3gpu_ctx {
     double kernelMs = 0.0;
     uint64_t kernelLaunches = 0, allLaunches = 0;
     std::string lastError;
+
+    // recursive estimator (splitting / clipping): frame stacks of the megakernel's threads
+    TreeFrame *dTree = nullptr;
+    uint32_t treeDepth = 0;
+    int treeGrid = 0;
 
     // differentiable rendering (pg3_diff.cu)
     float *dTot[3] = {nullptr, nullptr, nullptr};   // primal radiance of every path of the last forward

@@ -162,6 +162,8 @@ int diffChecks(pg3gpu_ctx *ctx)
         return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED, "differentiable rendering needs algorithm 7 (path tracing)");
     if (!ctx->useWavefront)
         return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED, "differentiable rendering needs the wavefront pipeline");
+    if (ctx->view.treeMode)
+        return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED, "differentiable rendering does not split paths or clip");
     if (ctx->nmat > kMaxDiffMaterials)
         return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED, "differentiable rendering supports at most 2048 materials");
     return PG3GPU_OK;

@@ -392,6 +392,211 @@ PG3_DI float3 traceDirect(const SceneView &S, int alg, uint32_t pixel, uint32_t 
     return Le + Lo;
 }
 
+// ------------------------------------------------------------------------------------------
+// The recursive estimator with splitting, the light-to-BSDF sample ratio and indirect clipping
+// (src/path_tracer.hxx:167-454). A vertex takes nLight light samples and nBsdf BSDF samples
+// (ComputeSplittingCounts, :432-454); each BSDF sample starts a sub-path whose reflected
+// estimate is clipped proportionally before it is added (:400-402), so the estimator is a tree
+// walked depth first with an explicit stack of vertex frames in device memory. Random numbers
+// are keyed by the vertex's preorder index in the tree (1 for the camera ray's hit; a chain
+// without splitting gives index == path length, the streams of tracePath): light sample j
+// draws group 2j, BSDF sample i group 2i+1.
+// ------------------------------------------------------------------------------------------
+
+// MISWeight2Power with sample counts (src/path_tracer_base.hxx:522-541)
+PG3_DI float misPowerN(float p1, uint32_t n1, float p2, uint32_t n2)
+{
+    const float s1 = n1 * p1, s2 = n2 * p2;
+    const float q1 = s1 * s1, q2 = s2 * s2;
+    return q1 / (q1 + q2) / n1;
+}
+
+PG3_DI void splittingCounts(const SceneView &S, float budget, uint32_t &nB, uint32_t &nL, float &next)
+{
+    nB = (uint32_t)max(lroundf((1.f - S.splitLevel) * 1.f + S.splitLevel * budget), 1l);
+    nL = (uint32_t)lroundf(fmaxf(S.lightRatio * nB, 1.f));
+    next = 1.f + ((budget - nB) / (float)nB);
+}
+
+// A new vertex on the stack: counts, roulette probability, and its light samples
+// (src/path_tracer.hxx:240-265, src/path_tracer_base.hxx:156-188, 350-411).
+PG3_DI void treeVertex(const SceneView &S, TreeFrame *F, float3 pt, float3 n, float3 wol, int mat, uint32_t pl,
+                       float budget, uint32_t vid, uint32_t pixel, uint32_t sample, PathCounters &pc)
+{
+    uint32_t nB, nL;
+    float next;
+    splittingCounts(S, budget, nB, nL, next);
+    const DevMaterial m = loadMat(S, mat);
+    const bool rrActive = S.maxPL == 0 || (S.rrMinPL > 0 && pl >= S.rrMinPL);
+    const float sum = (S.lightCount > 1) ? estimateSum(S, pt, n) : 0.f;
+    const Frame frame = frameFromZ(n);
+    float3 R = f3(0.f);
+    if (pl + 1 >= S.minPL) {
+        for (uint32_t j = 0; j < nL; ++j) {
+            const Rand4 ra = draw(S, pixel, sample, vid, 2 * j);
+            int lid;
+            float lprob = 0.f;
+            pickLight(S, pt, n, sum, ra.a, lid, lprob);
+            if (lid < 0) continue;
+            float3 wig, smp;
+            float dist, pdfW;
+            sampleLightAt(S, lid, pt, frame, n, ra.b, ra.c, ra.d, wig, dist, smp, pdfW);
+            if (!(maxc(smp) > 0.f)) continue;
+            ++pc.shadow;
+            if (occludedAny(S, pt, wig, dist)) continue;
+            BsdfRec br;
+            evalBsdf(m, toLocal(frame, wig), wol, br);
+            const float lightPdf = pdfW * lprob;
+            R += (smp * br.att) * (misPowerN(lightPdf, nL, br.pdfW * br.compProb, nB) / lightPdf);
+        }
+    }
+    F->pt = pt;
+    F->budget = next;
+    F->n = n;
+    F->rr = rrActive ? m.rrProb : 1.0f;
+    F->wol = wol;
+    F->sum = sum;
+    F->R = R;
+    F->vid = vid;
+    F->mat = mat;
+    F->pl = pl;
+    F->i = 0;
+    F->nBsdf = nB;
+    F->nLight = nL;
+    F->flags = rrActive ? 4u : 0u;   // 4: roulette active at this vertex
+}
+
+// Can the vertex reached at path length pl start its own samples? (src/path_tracer.hxx:212-238)
+PG3_DI bool treeReflects(const SceneView &S, const DevMaterial &m, uint32_t pl, PathCounters &pc)
+{
+    if (m.zeroRefl) { ++pc.blocker; return false; }
+    if (S.maxPL > 0 && pl >= S.maxPL) { ++pc.maxl; return false; }
+    if (pl >= kMaxPathLengthHard) { ++pc.safety; return false; }
+    return true;
+}
+
+PG3_DI float3 traceTree(const SceneView &S, uint32_t pixel, uint32_t sample, PathCounters &pc, TreeFrame *stack,
+                        uint32_t maxDepth)
+{
+    const uint32_t px = pixel % S.width, py = pixel / S.width;
+    const Rand4 rc = draw(S, pixel, sample, 0, 0);
+    const float nx = ((float)px + rc.a) * (2.f / S.width) - 1.f;
+    const float ny = ((float)py + rc.b) * (2.f / S.height) - 1.f;
+    const float3 dir = normalize(S.camFwd + S.camRight * (nx * S.tanX) - S.camUp * (ny * S.tanY));
+    ++pc.ext;
+    Hit h;
+    float3 L = f3(0.f);
+    if (!intersectClosest(S, S.camPos, dir, 0.f, h)) {
+        ++pc.bg;
+        if (S.minPL <= 1 && S.bgKind != kBgNone) {
+            float pdf;
+            L = bgEmission(S, dir, false, frameFromZ(make_float3(0.f, 0.f, 1.f)), pdf);
+        }
+        return L;
+    }
+    float3 pt, n;
+    int matId;
+    hitAttributes(S, h, S.camPos, dir, pt, n, matId);
+    const float3 wol0 = toLocal(frameFromZ(n), -dir);
+    const int light0 = __ldg(&S.mat2light[matId]);
+    if (light0 >= 0 && S.minPL <= 1) {
+        float pdfA;
+        L = areaEmission(S.lights[light0], pt, wol0.z, S.camPos, pdfA);
+    }
+    if (!treeReflects(S, loadMat(S, matId), 1, pc)) return L;
+    uint32_t vid = 1;
+    treeVertex(S, &stack[0], pt, n, wol0, matId, 1, S.splitBudget, vid, pixel, sample, pc);
+    int d = 0;
+    for (uint32_t guard = 0; guard < (1u << 26); ++guard) {
+        TreeFrame *F = &stack[d];
+        if (F->i < F->nBsdf) {
+            const uint32_t i = F->i;
+            const Rand4 rb = draw(S, pixel, sample, F->vid, 2 * i + 1);
+            const bool cut = (F->flags & 4u) && rb.a > F->rr;
+            if (cut) ++pc.rr;
+            const DevMaterial m = loadMat(S, F->mat);
+            BsdfRec br;
+            sampleBsdf(m, F->wol, rb.b, rb.c, rb.d, br);
+            if (isBlocker(br)) {
+                ++pc.blocker;
+                F->i = i + 1;
+                continue;
+            }
+            const bool finite = br.pdfW != infF();
+            const float cosAbs = fabsf(br.wil.z);
+            const Frame pf = frameFromZ(F->n);
+            const float3 wig = toWorld(pf, br.wil);
+            const uint32_t pl = F->pl + 1;
+            // the sample's ray: emission found at its end (src/path_tracer.hxx:198-210, 408-429)
+            ++pc.ext;
+            Hit ch;
+            float3 Le = f3(0.f), cpt, cn, cwol;
+            float lpdf = 0.f;
+            int lid = -1, cmat = 0;
+            bool childRefl = false;
+            if (!intersectClosest(S, F->pt, wig, epsRayCos(cosAbs), ch)) {
+                if (pl >= S.minPL && S.bgKind != kBgNone) {
+                    Le = bgEmission(S, wig, finite, pf, lpdf);
+                    lid = S.bgLightId;
+                }
+                if (!cut) ++pc.bg;
+            } else {
+                hitAttributes(S, ch, F->pt, wig, cpt, cn, cmat);
+                cwol = toLocal(frameFromZ(cn), -wig);
+                const int l = __ldg(&S.mat2light[cmat]);
+                if (l >= 0 && pl >= S.minPL) {
+                    Le = areaEmission(S.lights[l], cpt, cwol.z, F->pt, lpdf);
+                    lid = l;
+                }
+                childRefl = !cut && treeReflects(S, loadMat(S, cmat), pl, pc);
+            }
+            // direct light hit by the sample (:324-369)
+            float3 R = F->R;
+            if (!isZero(Le) && lid >= 0) {
+                if (finite) {
+                    const float bsdfPdf = br.pdfW * br.compProb;
+                    const float lightPdf = lpdf * pickProb(S, F->pt, F->n, F->sum, lid);
+                    R += (br.att * cosAbs * Le) * (misPowerN(bsdfPdf, F->nBsdf, lightPdf, F->nLight) / bsdfPdf);
+                } else {
+                    R += (br.att * Le) / ((float)F->nBsdf * br.compProb);
+                }
+            }
+            F->R = R;
+            if (childRefl && (uint32_t)d + 1 < maxDepth) {
+                F->att = br.att;
+                F->cosAbs = cosAbs;
+                F->pdfW = br.pdfW;
+                F->compProb = br.compProb;
+                F->flags = (F->flags & 4u) | (finite ? 1u : 0u);
+                ++vid;
+                treeVertex(S, &stack[d + 1], cpt, cn, cwol, cmat, pl, F->budget, vid, pixel, sample, pc);
+                ++d;
+            } else {
+                if (childRefl) atomicOr(S.errorFlag, kErrTreeStack);
+                F->i = i + 1;
+            }
+            continue;
+        }
+        // this vertex's estimate is complete: hand it to the parent's indirect term (:372-405)
+        const float3 Rv = F->R;
+        if (d == 0) return L + Rv;
+        --d;
+        TreeFrame *P = &stack[d];
+        if (!isZero(Rv)) {
+            const float denom = ((P->flags & 1u) ? P->pdfW : 1.f) * P->nBsdf * P->rr * P->compProb;
+            float3 ind = (P->flags & 1u) ? (P->att * P->cosAbs * Rv) / denom : (P->att * Rv) / denom;
+            if (S.clipping > 0.f) {
+                const float mx = maxc(ind);
+                if (mx > S.clipping) ind = ind * (S.clipping / mx);
+            }
+            P->R = P->R + ind;
+        }
+        P->i = P->i + 1;
+    }
+    atomicOr(S.errorFlag, kErrTreeStack);
+    return L;
+}
+
 // One camera path of the BSDF-sampling-only tracer (algorithm kPathTracingNaive,
 // src/path_tracer.hxx:45-165).
 PG3_DI float3 tracePathNaive(const SceneView &S, uint32_t pixel, uint32_t sample, PathCounters &pc)

@@ -91,8 +91,14 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "min path length != 1 with Russian roulette ending paths");
     if (o.max_path_length != 0 && o.min_path_length > o.max_path_length)
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "min path length larger than max path length");
-    if (o.indirect_clipping != 0.f) return bad(PG3GPU_ERR_UNSUPPORTED, "indirect illumination clipping is not implemented");
-    if (o.splitting_budget != 1) return bad(PG3GPU_ERR_UNSUPPORTED, "splitting budget other than 1 is not implemented");
+    if (!(o.indirect_clipping >= 0.f) || !std::isfinite(o.indirect_clipping))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "indirect clipping must be finite and >= 0");
+    if (o.splitting_budget < 1 || o.splitting_budget > 64)
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "splitting budget must be in 1..64");
+    if (!(o.splitting_level >= 0.f && o.splitting_level <= 1.f))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "splitting level must be in [0, 1]");
+    if (!(o.light_to_bsdf_ratio > 0.f && o.light_to_bsdf_ratio <= 16.f))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "light-to-BSDF sample ratio must be in (0, 16]");
     if (o.em_sampler != PG3GPU_EM_CDF && o.em_sampler != PG3GPU_EM_COSINE && o.em_sampler != PG3GPU_EM_STEERABLE)
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown environment-map sampler");
     if (sc.num_materials == 0 || !sc.materials) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "scene has no materials");
@@ -242,6 +248,18 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
     }
     v.emSampler = o.em_sampler;
     v.algorithm = o.algorithm;
+    v.splitBudget = (float)o.splitting_budget;
+    v.splitLevel = o.splitting_level;
+    v.lightRatio = o.light_to_bsdf_ratio;
+    v.clipping = o.indirect_clipping;
+    // the recursive estimator is needed when a vertex takes more than one BSDF or light sample,
+    // or when indirect estimates are clipped (src/path_tracer.hxx:240-265, 400-402, 432-454)
+    {
+        const float b = (1.f - o.splitting_level) + o.splitting_level * (float)o.splitting_budget;
+        const long nB = std::lround(b);
+        const long nL = std::lround(std::max(o.light_to_bsdf_ratio * (float)nB, 1.f));
+        v.treeMode = (o.splitting_budget > 1 || o.indirect_clipping > 0.f || nB != 1 || nL != 1) ? 1 : 0;
+    }
     v.minPL = o.min_path_length;
     v.maxPL = o.max_path_length;
     v.rrMinPL = o.rr_min_path_length;

@@ -18,9 +18,11 @@ constexpr int kMegaBlock = 128;
 
 // pg3_megakernel.cu
 // algorithm: an id of src/config.hxx:23-34 (0-7)
+// tree / treeDepth: frames of the recursive estimator (algorithm 7 with S.treeMode), treeDepth
+// per thread of the grid (gridBlocks x kMegaBlock threads)
 cudaError_t launchMegakernel(const SceneView &S, int algorithm, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                              float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,
-                             cudaStream_t stream);
+                             cudaStream_t stream, TreeFrame *tree = nullptr, uint32_t treeDepth = 0);
 cudaError_t megakernelOccupancy(int algorithm, int *blocksPerSm);
 cudaError_t launchAccumulate(uint32_t npix, uint32_t passes, const float *r, const float *g, const float *b,
                              double *sum, double *sumsq, cudaStream_t stream);

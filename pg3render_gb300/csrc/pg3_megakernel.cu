@@ -21,13 +21,17 @@ PG3_DI void flushCounters(DevStats *st, const PathCounters &c, uint32_t paths)
     }
 }
 
-// KIND: 0 NEE+MIS path tracer (algorithm 7), 1 naive path tracer (6), 2 one-hit estimators (0-5)
+// KIND: 0 NEE+MIS path tracer (algorithm 7), 1 naive path tracer (6), 2 one-hit estimators (0-5),
+// 3 the recursive estimator with splitting / clipping (algorithm 7; `tree` holds treeDepth
+// frames per thread of the grid)
 template <int KIND>
 __global__ void __launch_bounds__(kMegaBlock) megakernel(const __grid_constant__ SceneView S, int alg,
                                                          uint32_t sample0, uint64_t numPaths, uint32_t npix,
                                                          float *__restrict__ outR, float *__restrict__ outG,
-                                                         float *__restrict__ outB, DevStats *stats)
+                                                         float *__restrict__ outB, DevStats *stats, TreeFrame *tree,
+                                                         uint32_t treeDepth)
 {
+    TreeFrame *myStack = (KIND == 3) ? tree + (size_t)(blockIdx.x * blockDim.x + threadIdx.x) * treeDepth : nullptr;
     PathCounters pc;
     uint32_t done = 0;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -36,6 +40,7 @@ __global__ void __launch_bounds__(kMegaBlock) megakernel(const __grid_constant__
         const uint32_t sample = sample0 + (uint32_t)(i / npix);
         const float3 L = (KIND == 1)   ? tracePathNaive(S, pixel, sample, pc)
                          : (KIND == 2) ? traceDirect(S, alg, pixel, sample, pc)
+                         : (KIND == 3) ? traceTree(S, pixel, sample, pc, myStack, treeDepth)
                                        : tracePath(S, pixel, sample, pc);
         outR[i] = L.x;
         outG[i] = L.y;
@@ -76,14 +81,21 @@ __global__ void __launch_bounds__(256) accumulateKernel(uint32_t npix, uint32_t 
 
 cudaError_t launchMegakernel(const SceneView &S, int algorithm, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                              float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,
-                             cudaStream_t stream)
+                             cudaStream_t stream, TreeFrame *tree, uint32_t treeDepth)
 {
-    if (algorithm == 6)
-        megakernel<1><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats);
+    if (algorithm == 7 && S.treeMode) {
+        if (!tree || treeDepth == 0) return cudaErrorInvalidValue;
+        megakernel<3><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB,
+                                                            stats, tree, treeDepth);
+    } else if (algorithm == 6)
+        megakernel<1><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats,
+                                                            nullptr, 0);
     else if (algorithm == 7)
-        megakernel<0><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats);
+        megakernel<0><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats,
+                                                            nullptr, 0);
     else
-        megakernel<2><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats);
+        megakernel<2><<<gridBlocks, kMegaBlock, 0, stream>>>(S, algorithm, sample0, numPaths, npix, outR, outG, outB, stats,
+                                                            nullptr, 0);
     return cudaGetLastError();
 }
 

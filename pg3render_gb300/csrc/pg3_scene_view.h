@@ -101,6 +101,8 @@ struct SceneView {
     int algorithm;
     uint32_t minPL, maxPL, rrMinPL;
     uint32_t seedLo, seedHi;
+    float splitBudget, splitLevel, lightRatio, clipping;   // splitting and indirect clipping
+    int treeMode;             // 1: the recursive estimator (splitting / clipping) runs algorithm 7
 
     // device error word (bounded loops set bits instead of trapping)
     unsigned int *errorFlag;
@@ -129,6 +131,25 @@ struct GradArgs {
     const uint32_t *sampleOffset;   // device word added to every sample index (null: none)
 };
 
-enum : unsigned int { kErrTraversalStack = 1u, kErrQueueOverflow = 2u, kErrSteerDescent = 4u };
+enum : unsigned int { kErrTraversalStack = 1u, kErrQueueOverflow = 2u, kErrSteerDescent = 4u, kErrTreeStack = 16u };
+
+// One vertex of the recursive estimator's depth-first walk (traceTree, pg3_estimator.cuh).
+struct TreeFrame {
+    float3 pt;
+    float budget;             // splitting budget of this vertex's children
+    float3 n;
+    float rr;                 // roulette continuation probability
+    float3 wol;
+    float sum;                // light-estimate sum for picking
+    float3 R;                 // reflected estimate so far
+    uint32_t vid;             // preorder index
+    float3 att;               // current BSDF sample: attenuation
+    float cosAbs;
+    float pdfW, compProb;
+    int mat;
+    uint32_t pl;
+    uint32_t i, nBsdf, nLight, flags;   // flags: 1 finite sample, 2 roulette cut the sample
+};
+
 
 }  // namespace pg3

@@ -31,8 +31,10 @@ class Config:
     base_seed: int = 1234                # mBaseSeed
     min_path_length: int = 1             # mMinPathLength
     max_path_length: int = 0             # mMaxPathLength (0: Russian roulette)
-    indirect_illum_clipping: float = 0.0  # mIndirectIllumClipping (only 0 implemented)
-    splitting_budget: int = 1            # mSplittingBudget (only 1 implemented)
+    indirect_illum_clipping: float = 0.0  # mIndirectIllumClipping (the reference CLI's default is 16)
+    splitting_budget: int = 1            # mSplittingBudget (the reference CLI's default is 4)
+    splitting_level: float = 1.0         # mDbgSplittingLevel
+    light_to_bsdf_ratio: float = 1.0     # mDbgSplittingLightToBrdfSmplRatio
     em_sampler: int = EM_CDF             # compile-time PG3_USE_ENVMAP_* in the reference
     rr_min_path_length: int = 0          # extension: roulette from this length on with a max length set
     traversal: int = TRAVERSAL_AUTO
@@ -50,6 +52,8 @@ class Config:
         o.rr_min_path_length = self.rr_min_path_length
         o.indirect_clipping = self.indirect_illum_clipping
         o.splitting_budget = self.splitting_budget
+        o.splitting_level = self.splitting_level
+        o.light_to_bsdf_ratio = self.light_to_bsdf_ratio
         o.em_sampler = self.em_sampler
         o.traversal = self.traversal
         o.pipeline = self.pipeline

@@ -100,7 +100,8 @@ class Scene:
 
     # -------------------------------------------------------------- text form
     def to_text(self, em_path: Optional[str] = None, algorithm: str = "pt",
-                min_path_length: int = 1, max_path_length: int = 8) -> str:
+                min_path_length: int = 1, max_path_length: int = 8, splitting=None) -> str:
+        """splitting: optional (budget, level, light_to_bsdf_ratio, indirect_clipping)."""
         c = self.camera
         out = ["# %s" % self.name,
                "camera %r %r %r  %r %r %r  %r %r %r  %d %d %r" % (
@@ -129,7 +130,10 @@ class Scene:
             out.append("background_em %s" % em_path)
         elif self.background_const is not None:
             out.append("background_const %r %r %r" % tuple(self.background_const))
-        out.append("options %s %d %d" % (algorithm, min_path_length, max_path_length))
+        opts = "options %s %d %d" % (algorithm, min_path_length, max_path_length)
+        if splitting is not None:
+            opts += " %d %r %r %r" % (int(splitting[0]), float(splitting[1]), float(splitting[2]), float(splitting[3]))
+        out.append(opts)
         return "\n".join(out) + "\n"
 
     def write_env_map(self, path: str) -> None:

@@ -44,26 +44,33 @@ CASES = {
     "cornell_env_32_dbs": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cdf", "dbs", 64, 128),
     "cornell_area_32_el": (lambda: S.cornell_box(32, 32), 8, "cdf", "el", 16, 512),
     "cornell_area_32_nv": (lambda: S.cornell_box(32, 32), 8, "cdf", "nv", 16, 512),
+    # splitting budget / level / light-to-BSDF ratio and indirect clipping (src/path_tracer.hxx:
+    # 240-265, 400-402, 432-454); the first two are the reference's default options (-sb 4 -iic 16)
+    "cornell_area_32_sb4_iic16": (lambda: S.cornell_box(32, 32), 0, "cdf", "pt", 64, 64, (4, 1.0, 1.0, 16.0)),
+    "cornell_env_32_sb4_iic16": (lambda: S.cornell_env(32, 32, 64, 32), 0, "cdf", "pt", 64, 64, (4, 1.0, 1.0, 16.0)),
+    "cornell_area_32_sb3_lvl05_r2": (lambda: S.cornell_box(32, 32), 8, "cdf", "pt", 64, 64, (3, 0.5, 2.0, 0.0)),
 }
 
 EM_TOKEN = "@EM@"
 
 
 def make(name):
-    build, maxpl, sampler, alg, K, N = CASES[name]
+    build, maxpl, sampler, alg, K, N = CASES[name][:6]
+    splitting = CASES[name][6] if len(CASES[name]) > 6 else None
     scene = build()
     with tempfile.TemporaryDirectory() as td:
         em_path = os.path.join(td, "em.bin")
         if scene.env_map is not None:
             scene.write_env_map(em_path)
-        text = scene.to_text(em_path=em_path, algorithm=alg, max_path_length=maxpl)
+        text = scene.to_text(em_path=em_path, algorithm=alg, max_path_length=maxpl, splitting=splitting)
         r = O.reference_render(text, renderers=K, iters=N, seed=4321, em_sampler=sampler)
     np.savez_compressed(
         os.path.join(HERE, name + ".npz"),
         scene_text=np.array(text.replace(em_path, EM_TOKEN)),
         env_map=(scene.env_map if scene.env_map is not None else np.zeros((0, 0, 3), np.float32)),
         mean=r["mean"], var_mean=r["var_of_renderer_mean"] / K, spp=np.array(K * N),
-        max_path_length=np.array(maxpl), em_sampler=np.array(sampler), algorithm=np.array(alg))
+        max_path_length=np.array(maxpl), em_sampler=np.array(sampler), algorithm=np.array(alg),
+        splitting=np.array(splitting if splitting is not None else (1, 1.0, 1.0, 0.0), np.float64))
     print(name, "done", r["timing"])
 
 

@@ -56,8 +56,11 @@ def _create(scene, **opt):
 
 
 @pytest.mark.parametrize("opt,status,msg", [
-    (dict(splitting_budget=4), _lib.ERR_UNSUPPORTED, "splitting"),
-    (dict(indirect_clipping=16.0), _lib.ERR_UNSUPPORTED, "clipping"),
+    (dict(splitting_budget=0), _lib.ERR_INVALID_ARGUMENT, "splitting budget"),
+    (dict(splitting_budget=65), _lib.ERR_INVALID_ARGUMENT, "splitting budget"),
+    (dict(splitting_level=1.5), _lib.ERR_INVALID_ARGUMENT, "splitting level"),
+    (dict(light_to_bsdf_ratio=0.0), _lib.ERR_INVALID_ARGUMENT, "ratio"),
+    (dict(indirect_clipping=-1.0), _lib.ERR_INVALID_ARGUMENT, "clipping"),
     (dict(algorithm=8), _lib.ERR_INVALID_ARGUMENT, "unknown algorithm"),
     (dict(min_path_length=9), _lib.ERR_INVALID_ARGUMENT, "min path length"),
     (dict(min_path_length=0), _lib.ERR_INVALID_ARGUMENT, "min_path_length"),

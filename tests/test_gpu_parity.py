@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr",
                 "cornell_env_32_cdf", "cornell_env_32_cos",
                 "cornell_area_32_dbs", "cornell_area_32_dlsa", "cornell_area_32_dlss", "cornell_area_32_dmis",
-                "cornell_env_32_dmis_cdf", "cornell_env_32_dbs", "cornell_area_32_el", "cornell_area_32_nv"]
+                "cornell_env_32_dmis_cdf", "cornell_env_32_dbs", "cornell_area_32_el", "cornell_area_32_nv",
+                "cornell_area_32_sb4_iic16", "cornell_env_32_sb4_iic16", "cornell_area_32_sb3_lvl05_r2"]
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
 # the reference's acronyms of its algorithm ids (src/config.hxx:147-170)
 ALG_IDS = {"el": 0, "nv": 1, "dbs": 2, "dlsa": 3, "dlss": 4, "dmis": 5, "ptn": 6, "pt": 7}
@@ -67,6 +68,30 @@ def test_one_hit_algorithms_path_by_path(alg, env, tmp_path):
     assert np.isfinite(g).all() and g.max() > 0
 
 
+@pytest.mark.parametrize("split", [(4, 1.0, 1.0, 16.0, 0), (3, 0.5, 2.0, 0.0, 8), (1, 1.0, 1.0, 2.0, 8),
+                                   (2, 1.0, 1.0, 0.0, 0)])
+@pytest.mark.parametrize("env", [False, True])
+def test_splitting_and_clipping_path_by_path(split, env, tmp_path):
+    """The recursive estimator (splitting budget, level, light-to-BSDF ratio, indirect clipping;
+    roulette when the max path length is 0) against the oracle, sample by sample."""
+    budget, level, ratio, clip, maxpl = split
+    scene = S.cornell_env(24, 24, 64, 32) if env else S.cornell_box(24, 24)
+    em = str(tmp_path / "em.bin")
+    if env:
+        scene.write_env_map(em)
+    text = scene.to_text(em_path=em, max_path_length=maxpl, splitting=(budget, level, ratio, clip))
+    seed = 41
+    cfg = _cfg(scene, maxpl, P.renderer.kPathTracing, P.renderer.EM_CDF, splitting_budget=budget,
+               splitting_level=level, light_to_bsdf_ratio=ratio, indirect_illum_clipping=clip)
+    with P.GpuPathTracer(cfg, seed=seed) as r:
+        g = r.render_samples(P.renderer.kPathTracing, 0, 4)
+        st = r.stats()
+    o = _oracle_samples(scene, text, 4, seed, 0)
+    frac = _match_fraction(g, o)
+    assert frac >= MIN_MATCH, "only %.4f of samples match the oracle" % frac
+    assert st["paths"] == 24 * 24 * 4 and np.isfinite(g).all()
+
+
 @pytest.mark.parametrize("case", ["area", "area_naive", "env_cdf", "env_cos"])
 def test_path_by_path_vs_oracle(case, tmp_path):
     if case.startswith("area"):
@@ -95,7 +120,9 @@ def test_against_reference_golden(name):
     d, text, td = load_golden(name)
     scene = scene_from_golden(d)
     alg = ALG_IDS[str(d["algorithm"])]
-    cfg = _cfg(scene, int(d["max_path_length"]), alg, SAMPLERS[str(d["em_sampler"])])
+    sp = d["splitting"] if "splitting" in d else (1, 1.0, 1.0, 0.0)
+    cfg = _cfg(scene, int(d["max_path_length"]), alg, SAMPLERS[str(d["em_sampler"])], splitting_budget=int(sp[0]),
+               splitting_level=float(sp[1]), light_to_bsdf_ratio=float(sp[2]), indirect_illum_clipping=float(sp[3]))
     spp = 32768   # heavy-tailed estimators (naive, cosine sky sampling) need many samples
     with P.GpuPathTracer(cfg, seed=2024) as r:
         r.RunIteration(alg, 0, spp)
