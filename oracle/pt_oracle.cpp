@@ -847,6 +847,33 @@ struct Scene {
     float splitLevel = 1.f, lightRatio = 1.f, clipping = 0.f;
 
     size_t LightCount() const { return lights.size() + (hasBg ? 1 : 0); }
+    float shL[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};   // SH coefficients of the map's luminance
+    // (texel luminance x basis x texel solid angle, the steerable sampler's basis)
+    void ComputeShL()
+    {
+        double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const double pi = 3.14159265358979323846;
+        for (uint32_t r = 0; r < em.H; ++r) {
+            const double theta = pi * (r + 0.5) / em.H;
+            const double dOmega = (2.0 * pi / em.W) * (pi / em.H) * std::sin(theta);
+            for (uint32_t c = 0; c < em.W; ++c) {
+                const double phi = -((c + 0.5) / em.W - 0.5) * 2.0 * pi;
+                const double x = std::sin(theta) * std::cos(phi), y = std::sin(theta) * std::sin(phi), z = std::cos(theta);
+                const V3 &p = em.At(c, r);
+                const double L = (0.212671 * p.x + 0.715160 * p.y + 0.072169 * p.z) * dOmega;
+                acc[0] += L * 0.282095;
+                acc[1] += L * 0.488603 * y;
+                acc[2] += L * 0.488603 * z;
+                acc[3] += L * 0.488603 * x;
+                acc[4] += L * 1.092548 * x * y;
+                acc[5] += L * 1.092548 * y * z;
+                acc[6] += L * 0.315392 * (3.0 * z * z - 1.0);
+                acc[7] += L * 1.092548 * x * z;
+                acc[8] += L * 0.546274 * (x * x - y * y);
+            }
+        }
+        for (int k = 0; k < 9; ++k) shL[k] = (float)acc[k];
+    }
 
     // src/scene.hxx:42-59, src/scene_graph.hxx:47-57
     bool Intersect(V3 org, V3 dir, float tmin, Hit &h) const
@@ -921,12 +948,29 @@ public:
     explicit Tracer(const Scene &s) : S(s) {}
 
     // Light contribution estimates of the current vertex for every light, in light-id order
-    // (src/path_tracer_base.hxx:22-32, 216-232); only area lights are estimated here, the
-    // environment map is out of scope when other lights are present.
+    // (src/path_tracer_base.hxx:22-32, 216-232). The background's (src/lights.hxx:447-470): pi x
+    // luminance when constant; for a map the clamped-cosine SH estimate of the irradiance, 9 SH
+    // coefficients of the map's luminance (the steerable sampler's estimate,
+    // src/em_steerable_sampler.hxx:2300-2355; the reference's other samplers draw a random MIS
+    // estimate instead, src/em.hxx:130-169 -- either keeps the picking unbiased).
     void Estimates(V3 pt, const Frame &f, std::vector<float> &est) const
     {
-        est.resize(S.lights.size());
+        est.resize(S.LightCount());
         for (size_t i = 0; i < S.lights.size(); ++i) est[i] = S.lights[i].Estimate(pt, f);
+        if (S.hasBg) {
+            if (!S.bgIsEm) {
+                est[S.bgLightId] = Luminance(S.bgConst) * kPiF;
+            } else {
+                const V3 n = f.Normal();
+                const float c1 = .429043f, c2 = .511644f, c3 = .743125f, c4 = .886227f, c5 = .247708f;
+                const float c[9] = {c4 + 0.15f, 2.f * c2 * n.y, 2.f * c2 * n.z, 2.f * c2 * n.x, 2.f * c1 * n.x * n.y,
+                                    2.f * c1 * n.y * n.z, c3 * n.z * n.z - c5, 2.f * c1 * n.x * n.z,
+                                    c1 * (n.x * n.x - n.y * n.y)};
+                float e = 0.f;
+                for (int k = 0; k < 9; ++k) e += S.shL[k] * c[k];
+                est[S.bgLightId] = std::max(e, 0.f);
+            }
+        }
     }
 
     // PickSingleLight (src/path_tracer_base.hxx:191-257)
@@ -1415,10 +1459,7 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
         }
     }
     s.SetupCamera();
-    if (s.hasBg && s.bgIsEm && s.lights.size() > 0) {
-        err = "environment map together with area lights is not restated by the oracle";
-        return false;
-    }
+    if (s.bgIsEm) s.ComputeShL();
     return true;
 }
 

@@ -278,6 +278,7 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
     if ((st = upload(ctx, (float4 **)&v.em, hs.em))) return bail(st);
     if ((st = upload(ctx, (float **)&v.emMarg, hs.emMarg))) return bail(st);
     if ((st = upload(ctx, (float **)&v.emCond, hs.emCond))) return bail(st);
+    if ((st = upload(ctx, (float **)&v.bgShL, hs.bgShL))) return bail(st);
     if (hs.hasSteer) {
         SteerView &sv = v.steer;
         if ((st = upload(ctx, (float4 **)&sv.vdir, hs.steer.vdir))) return bail(st);
@@ -302,7 +303,7 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
         if ((st = upload(ctx, (float4 **)&sv.leafPlane, aux))) return bail(st);
         if ((st = upload(ctx, (int4 **)&sv.faceCells, hs.steer.faceCells))) return bail(st);
         sv.level = hs.steer.level;
-        for (size_t l = 0; l < hs.steer.levelOffset.size() && l < 10; ++l) sv.levelOff[l] = hs.steer.levelOffset[l];
+        for (size_t l = 0; l < hs.steer.levelOffset.size() && l < 8; ++l) sv.levelOff[l] = hs.steer.levelOffset[l];
         sv.root = hs.steer.root;
     }
     if ((st = devAlloc(ctx, &ctx->dErr, 1))) return bail(st);

@@ -32,11 +32,30 @@ PG3_DI float misPower(float a, float b)
     return a2 / (a2 + b2);
 }
 
-// Sum of the area lights' contribution estimates at a vertex (src/path_tracer_base.hxx:216-232).
+// Contribution estimate of the background light (BackgroundLight::EstimateContribution,
+// src/lights.hxx:447-470): a constant background integrates to pi * luminance; for a map the
+// clamped-cosine SH estimate of the irradiance (the steerable sampler's own estimate,
+// src/em_steerable_sampler.hxx:2300-2355; the reference's other samplers estimate it by random
+// MIS samples, em.hxx:130-169 -- any positive estimate keeps the picking unbiased).
+PG3_DI float bgEstimate(const SceneView &S, float3 n)
+{
+    if (S.bgKind == kBgConstant) return luminance(S.bgConst) * kPiF;
+    if (S.bgKind != kBgEnvMap) return 0.f;
+    float c[9];
+    steerCoeffs(n, c);
+    return fmaxf(dot9(S.bgShL, c), 0.f);
+}
+// Estimate of light l (area lights first, the background last; src/scene.hxx:948-953).
+PG3_DI float lightEstimate(const SceneView &S, uint32_t l, float3 pt, float3 n)
+{
+    return (l < S.nArea) ? areaEstimate(S.lights[l], pt, n) : bgEstimate(S, n);
+}
+
+// Sum of the lights' contribution estimates at a vertex (src/path_tracer_base.hxx:216-232).
 PG3_DI float estimateSum(const SceneView &S, float3 pt, float3 n)
 {
     float sum = 0.f;
-    for (uint32_t i = 0; i < S.nArea; ++i) sum += areaEstimate(S.lights[i], pt, n);
+    for (uint32_t i = 0; i < S.lightCount; ++i) sum += lightEstimate(S, i, pt, n);
     return sum;
 }
 
@@ -50,12 +69,12 @@ PG3_DI void pickLight(const SceneView &S, float3 pt, float3 n, float sum, float 
         const float r = u * sum;
         float cum = 0.f, e = 0.f;
         uint32_t l = 0;
-        for (; l < S.nArea; ++l) {
-            e = areaEstimate(S.lights[l], pt, n);
+        for (; l < cnt; ++l) {
+            e = lightEstimate(S, l, pt, n);
             cum += e;
             if (!(r > cum)) break;
         }
-        if (l >= S.nArea) { l = S.nArea - 1; }
+        if (l >= cnt) { l = cnt - 1; e = lightEstimate(S, l, pt, n); }
         id = (int)l;
         prob = e / sum;
     } else {
@@ -69,7 +88,7 @@ PG3_DI float pickProb(const SceneView &S, float3 pt, float3 n, float sum, int id
     const uint32_t cnt = S.lightCount;
     if (cnt <= 1) return cnt == 1 ? 1.f : 0.f;
     if (!(sum > 0.f)) return 1.f / cnt;
-    return areaEstimate(S.lights[id], pt, n) / sum;
+    return lightEstimate(S, (uint32_t)id, pt, n) / sum;
 }
 
 // Background emission and its light-sampling pdf for MIS (src/lights.hxx:379-407,

@@ -74,6 +74,33 @@ void buildEmCdf(const float *rgb, uint32_t W, uint32_t H, std::vector<float> &ma
     computeCdf(rowInt.data(), H, marg.data(), total);
 }
 
+void emShCoefficients(const float *rgb, uint32_t W, uint32_t H, std::vector<float> &out)
+{
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const double pi = 3.14159265358979323846;
+    for (uint32_t r = 0; r < H; ++r) {
+        const double theta = pi * (r + 0.5) / H;
+        const double dOmega = (2.0 * pi / W) * (pi / H) * std::sin(theta);
+        for (uint32_t c = 0; c < W; ++c) {
+            const double phi = -((c + 0.5) / W - 0.5) * 2.0 * pi;   // latLong2Dir
+            const double x = std::sin(theta) * std::cos(phi), y = std::sin(theta) * std::sin(phi), z = std::cos(theta);
+            const float *p = rgb + ((size_t)r * W + c) * 3;
+            const double L = (0.212671 * p[0] + 0.715160 * p[1] + 0.072169 * p[2]) * dOmega;
+            acc[0] += L * 0.282095;
+            acc[1] += L * 0.488603 * y;
+            acc[2] += L * 0.488603 * z;
+            acc[3] += L * 0.488603 * x;
+            acc[4] += L * 1.092548 * x * y;
+            acc[5] += L * 1.092548 * y * z;
+            acc[6] += L * 0.315392 * (3.0 * z * z - 1.0);
+            acc[7] += L * 1.092548 * x * z;
+            acc[8] += L * 0.546274 * (x * x - y * y);
+        }
+    }
+    out.assign(9, 0.f);
+    for (int k = 0; k < 9; ++k) out[k] = (float)acc[k];
+}
+
 int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out, std::string &err)
 {
     char buf[256];
@@ -220,10 +247,6 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
     v.lightCount = v.nArea + (sc.background != PG3GPU_BG_NONE ? 1 : 0);
     v.bgLightId = (sc.background != PG3GPU_BG_NONE) ? (int)v.nArea : -1;
     v.bgConst = make_float3(sc.background_radiance[0], sc.background_radiance[1], sc.background_radiance[2]);
-    if (sc.background != PG3GPU_BG_NONE && sc.num_area_lights > 0)
-        return bad(PG3GPU_ERR_UNSUPPORTED,
-                   "a background light together with area lights needs the environment contribution estimate, "
-                   "which is not implemented");
     if (sc.background == PG3GPU_BG_ENVMAP) {
         if (!sc.env_map || sc.env_width < 2 || sc.env_height < 2 || (uint64_t)sc.env_width * sc.env_height > (1ull << 26))
             return bad(PG3GPU_ERR_INVALID_ARGUMENT, "environment map needs data and 2 <= size <= 2^26 pixels");
@@ -236,12 +259,14 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
             out.em[i] = make_float4(p[0], p[1], p[2], 0.f);
         }
         buildEmCdf(sc.env_map, sc.env_width, sc.env_height, out.emMarg, out.emCond);
+        emShCoefficients(sc.env_map, sc.env_width, sc.env_height, out.bgShL);
         v.emW = sc.env_width;
         v.emH = sc.env_height;
         if (o.em_sampler == PG3GPU_EM_STEERABLE) {
             if (!buildSteerable(sc.env_map, sc.env_width, sc.env_height, o.steer_subdiv_level, out.steer, err))
                 return PG3GPU_ERR_INVALID_ARGUMENT;
             out.hasSteer = true;
+            out.bgShL = out.steer.rootW;   // the steerable sampler's own irradiance estimate (its whole integral)
         }
     } else if (sc.background != PG3GPU_BG_NONE && sc.background != PG3GPU_BG_CONSTANT) {
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown background kind");

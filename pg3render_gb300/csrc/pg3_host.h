@@ -24,6 +24,7 @@ struct HostScene {
     std::vector<DevAreaLight> lights;
     std::vector<float4> em;
     std::vector<float> emMarg, emCond;
+    std::vector<float> bgShL;            // 9 SH coefficients of the map's luminance (picking estimate)
     SteerableHost steer;
     bool hasSteer = false;
 };
@@ -35,5 +36,10 @@ int prepareScene(const pg3gpu_scene &scene, const pg3gpu_options &opts, HostScen
 // (src/em_simple_spherical_sampler.hxx:117-152, src/distribution.hxx:45-74, 484-501):
 // marg has H+1 entries, cond H rows of W+1 entries.
 void buildEmCdf(const float *rgb, uint32_t W, uint32_t H, std::vector<float> &marg, std::vector<float> &cond);
+
+// 9 SH coefficients of the map's texel luminance (basis of the steerable sampler), integrated
+// over the texels' solid angles: with the clamped-cosine coefficients of a normal n, their dot
+// product estimates the irradiance at n (the background's light-picking estimate).
+void emShCoefficients(const float *rgb, uint32_t W, uint32_t H, std::vector<float> &out);
 
 }  // namespace pg3

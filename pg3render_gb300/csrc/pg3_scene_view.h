@@ -56,7 +56,7 @@ struct SteerView {
                               // same allocation by the leaf-locator tables (pg3_steer.cuh)
     const int4 *faceCells;    // cube-map cells: up to 4 candidate level-0 faces (-1 none)
     uint32_t level;           // leaf subdivision level
-    uint32_t levelOff[10];    // first entry of each level in `tri`
+    uint32_t levelOff[8];     // first entry of each level in `tri` (level <= 7)
     int root;
 };
 
@@ -94,6 +94,8 @@ struct SceneView {
     uint32_t emW, emH;
     const float *emMarg;      // marginal CDF over rows (emH + 1)
     const float *emCond;      // conditional CDFs, emH rows of (emW + 1)
+    const float *bgShL;       // 9 SH coefficients of the map's luminance: the background's
+                              // light-picking estimate (with area lights present)
     int emSampler;
     SteerView steer;
 

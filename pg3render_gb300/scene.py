@@ -285,6 +285,25 @@ def cornell_env(width: int = 512, height: int = 512, em_width: int = 1024, em_he
     return s
 
 
+def cornell_env_area(width: int = 512, height: int = 512, em_width: int = 1024, em_height: int = 512,
+                     em_seed: int = 7) -> Scene:
+    """cornell_env with the 0.5x0.5 light quad of radiance 25 under its open top: an environment
+    map and area lights in one scene (light picking includes the background)."""
+    s = cornell_env(width, height, em_width, em_height, em_seed)
+    s.name = "cornell_envarea_%dx%d_em%dx%d" % (width, height, em_width, em_height)
+    _ceiling_light(s)
+    return s
+
+
+def cornell_box_bg(width: int = 256, height: int = 256, background=(0.4, 0.5, 0.7)) -> Scene:
+    """cornell_box with a constant background seen through the open front (area lights and a
+    background light in one scene)."""
+    s = cornell_box(width, height)
+    s.name = "cornell_areabg_%dx%d" % (width, height)
+    s.background_const = tuple(background)
+    return s
+
+
 def cornell_env_diff(width: int = 256, height: int = 256, em_width: int = 512, em_height: int = 256,
                      em_seed: int = 7) -> Scene:
     """The environment-lit box for gradients: four Lambert materials (floor, back wall, red

@@ -43,6 +43,10 @@ def scene_from_golden(d):
     name = text.splitlines()[0][2:].strip()
     if name.startswith("cornell_area_"):
         s = S.cornell_box(32, 32)
+    elif name.startswith("cornell_areabg_"):
+        s = S.cornell_box_bg(32, 32)
+    elif name.startswith("cornell_envarea_"):
+        s = S.cornell_env_area(32, 32, 64, 32)
     else:
         s = S.cornell_env(32, 32, 64, 32)
     if s.env_map is not None:

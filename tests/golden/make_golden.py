@@ -49,6 +49,10 @@ CASES = {
     "cornell_area_32_sb4_iic16": (lambda: S.cornell_box(32, 32), 0, "cdf", "pt", 64, 64, (4, 1.0, 1.0, 16.0)),
     "cornell_env_32_sb4_iic16": (lambda: S.cornell_env(32, 32, 64, 32), 0, "cdf", "pt", 64, 64, (4, 1.0, 1.0, 16.0)),
     "cornell_area_32_sb3_lvl05_r2": (lambda: S.cornell_box(32, 32), 8, "cdf", "pt", 64, 64, (3, 0.5, 2.0, 0.0)),
+    # area lights and a background light in one scene (picking includes the background's estimate)
+    "cornell_envarea_32_cdf": (lambda: S.cornell_env_area(32, 32, 64, 32), 12, "cdf", "pt", 64, 128),
+    "cornell_envarea_32_dmis": (lambda: S.cornell_env_area(32, 32, 64, 32), 12, "cdf", "dmis", 64, 128),
+    "cornell_areabg_32": (lambda: S.cornell_box_bg(32, 32), 8, "cdf", "pt", 64, 128),
 }
 
 EM_TOKEN = "@EM@"

@@ -85,9 +85,9 @@ def test_scene_validation():
     s.triangles[0] = (p, p, p, 0)                            # degenerate
     assert _create(s)[0] == _lib.ERR_INVALID_ARGUMENT
     s = S.cornell_box(8, 8)
-    s.env_map = np.ones((4, 8, 3), np.float32)               # environment map + area lights
+    s.env_map = np.ones((4, 8, 3), np.float32)               # environment map + area lights: valid
     st, err = _create(s)
-    assert st == _lib.ERR_UNSUPPORTED and "area lights" in err
+    assert st == _lib.ERR_CUDA and "device" in err           # (validation passed; no GPU here)
     s = S.cornell_env(8, 8, 16, 8)
     s.env_map[0, 0, 0] = np.nan
     assert _create(s)[0] == _lib.ERR_INVALID_ARGUMENT

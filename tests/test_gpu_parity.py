@@ -20,7 +20,8 @@ GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr"
                 "cornell_env_32_cdf", "cornell_env_32_cos",
                 "cornell_area_32_dbs", "cornell_area_32_dlsa", "cornell_area_32_dlss", "cornell_area_32_dmis",
                 "cornell_env_32_dmis_cdf", "cornell_env_32_dbs", "cornell_area_32_el", "cornell_area_32_nv",
-                "cornell_area_32_sb4_iic16", "cornell_env_32_sb4_iic16", "cornell_area_32_sb3_lvl05_r2"]
+                "cornell_area_32_sb4_iic16", "cornell_env_32_sb4_iic16", "cornell_area_32_sb3_lvl05_r2",
+                "cornell_envarea_32_cdf", "cornell_envarea_32_dmis", "cornell_areabg_32"]
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
 # the reference's acronyms of its algorithm ids (src/config.hxx:147-170)
 ALG_IDS = {"el": 0, "nv": 1, "dbs": 2, "dlsa": 3, "dlss": 4, "dmis": 5, "ptn": 6, "pt": 7}
@@ -92,11 +93,18 @@ def test_splitting_and_clipping_path_by_path(split, env, tmp_path):
     assert st["paths"] == 24 * 24 * 4 and np.isfinite(g).all()
 
 
-@pytest.mark.parametrize("case", ["area", "area_naive", "env_cdf", "env_cos"])
+@pytest.mark.parametrize("case", ["area", "area_naive", "env_cdf", "env_cos", "envarea_cdf", "envarea_cos",
+                                  "areabg", "areabg_naive"])
 def test_path_by_path_vs_oracle(case, tmp_path):
-    if case.startswith("area"):
+    if case.startswith("areabg"):
+        scene = S.cornell_box_bg(24, 24)
+        maxpl, sampler = 8, 0
+    elif case.startswith("area"):
         scene = S.cornell_box(24, 24)
         maxpl, sampler = 8, 0
+    elif case.startswith("envarea"):
+        scene = S.cornell_env_area(24, 24, 64, 32)
+        maxpl, sampler = 12, (0 if case.endswith("cdf") else 1)
     else:
         scene = S.cornell_env(24, 24, 64, 32)
         maxpl, sampler = 12, (0 if case == "env_cdf" else 1)

@@ -20,7 +20,8 @@ GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr"
                 "cornell_env_32_cdf", "cornell_env_32_cos",
                 "cornell_area_32_dbs", "cornell_area_32_dlsa", "cornell_area_32_dlss", "cornell_area_32_dmis",
                 "cornell_env_32_dmis_cdf", "cornell_env_32_dbs", "cornell_area_32_el", "cornell_area_32_nv",
-                "cornell_area_32_sb4_iic16", "cornell_env_32_sb4_iic16", "cornell_area_32_sb3_lvl05_r2"]
+                "cornell_area_32_sb4_iic16", "cornell_env_32_sb4_iic16", "cornell_area_32_sb3_lvl05_r2",
+                "cornell_envarea_32_cdf", "cornell_envarea_32_dmis", "cornell_areabg_32"]
 # the visualisers are deterministic inside a surface (zero variance): only the fraction of
 # |z| <= 4 is a meaningful statistic for them
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
