@@ -60,7 +60,16 @@ enum {
     PG3GPU_ALG_PATH_TRACING = 7
 };
 
-enum { PG3GPU_MAT_LAMBERT = 0, PG3GPU_MAT_GGX_CONDUCTOR = 1, PG3GPU_MAT_GGX_DIELECTRIC = 2 };
+/* Material kinds: LambertMaterial, MicrofacetGGXConductorMaterial, MicrofacetGGXDielectricMaterial,
+   PhongMaterial, SmoothConductorMaterial, SmoothDielectricMaterial (src/materials.hxx:250-1266). */
+enum {
+    PG3GPU_MAT_LAMBERT = 0,
+    PG3GPU_MAT_GGX_CONDUCTOR = 1,
+    PG3GPU_MAT_GGX_DIELECTRIC = 2,
+    PG3GPU_MAT_PHONG = 3,
+    PG3GPU_MAT_SMOOTH_CONDUCTOR = 4,
+    PG3GPU_MAT_SMOOTH_DIELECTRIC = 5
+};
 enum { PG3GPU_BG_NONE = 0, PG3GPU_BG_CONSTANT = 1, PG3GPU_BG_ENVMAP = 2 };
 /* Environment-map light samplers (compile-time choice in src/hard_config.hxx:17-18, run-time here). */
 enum { PG3GPU_EM_CDF = 0, PG3GPU_EM_COSINE = 1, PG3GPU_EM_STEERABLE = 2 };
@@ -78,11 +87,15 @@ typedef struct pg3gpu_camera {       /* Camera::Setup arguments, src/camera.hxx:
 
 typedef struct pg3gpu_material {
     int32_t kind;                    /* PG3GPU_MAT_* */
-    float albedo[3];                 /* Lambert reflectance (src/materials.hxx:262-266) */
+    float albedo[3];                 /* Lambert reflectance (src/materials.hxx:262-266); Phong diffuse
+                                        reflectance as the material holds it, i.e. already halved when
+                                        the glossy lobe is on (src/materials.hxx:366-381) */
     float alpha;                     /* GGX roughness, clamped to [0.001, 1] (src/materials.hxx:805) */
-    float ior;                       /* inner IOR n */
+    float ior;                       /* inner IOR n (GGX and smooth conductor / dielectric) */
     float ior_outer;                 /* outer IOR */
     float absorb;                    /* conductor absorbance k */
+    float glossy[3];                 /* Phong glossy reflectance (mPhongReflectance) */
+    float phong_exponent;            /* Phong lobe exponent (mPhongExponent), >= 0 */
 } pg3gpu_material;
 
 typedef struct pg3gpu_triangle {     /* Triangle(p0, p1, p2, matId), src/scene_graph.hxx:88-101 */
@@ -101,6 +114,11 @@ typedef struct pg3gpu_area_light {   /* AreaLight over one scene triangle, src/l
     float radiance[3];
 } pg3gpu_area_light;
 
+typedef struct pg3gpu_point_light {  /* PointLight, src/lights.hxx:232-343 */
+    float position[3];
+    float power[3];                  /* PointLight::SetPower: intensity = power / (4 pi) */
+} pg3gpu_point_light;
+
 typedef struct pg3gpu_scene {
     pg3gpu_camera camera;
     const pg3gpu_material *materials;
@@ -116,6 +134,8 @@ typedef struct pg3gpu_scene {
     const float *env_map;            /* PG3GPU_BG_ENVMAP: host RGB float32, env_height rows of
                                         env_width pixels, row 0 at theta = 0 (src/em_image.hxx:51-93) */
     uint32_t env_width, env_height;
+    const pg3gpu_point_light *point_lights;   /* light ids after the area lights, before the background */
+    uint32_t num_point_lights;
 } pg3gpu_scene;
 
 /* ---- options (src/config.hxx:1100-1137, src/hard_config.hxx:7-27) ------- */

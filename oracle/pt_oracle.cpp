@@ -195,6 +195,21 @@ static inline V3 SampleCosHemisphereW(float u0, float u1, float *pdf)
 }
 // src/sampling.hxx:308-311
 static inline float CosHemispherePdfW(float z) { return std::max(0.f, z) * kPiInvF; }
+// src/sampling.hxx:250-285
+static inline V3 SamplePowerCosHemisphereW(float u0, float u1, float power)
+{
+    const float term1 = 2.f * kPiF * u0;
+    const float term2 = std::pow(u1, 1.f / (power + 1.f));
+    const float term3 = std::sqrt(1.f - term2 * term2);
+    return V3(std::cos(term1) * term3, std::sin(term1) * term3, term2);
+}
+static inline float PowerCosHemispherePdfW(V3 local, float power)
+{
+    const float cosTheta = std::max(0.f, local.z);
+    return (power + 1.f) * std::pow(cosTheta, power) * (kPiInvF * 0.5f);
+}
+// src/geom.hxx:110-113
+static inline V3 ReflectLocal(V3 v) { return V3(-v.x, -v.y, v.z); }
 
 // src/sampling.hxx:326-343
 static inline V3 SampleCosSphereParamPdfW(float u0, float u1, float u2, bool upper, bool lower, float &pdf)
@@ -403,7 +418,7 @@ static inline float GgxPdfVisibleNormals(V3 wo, V3 h, float D, float a)
 // --------------------------------------------------------------------------------------------
 // Materials (src/materials.hxx)
 // --------------------------------------------------------------------------------------------
-enum { kLambert = 0, kGgxConductor = 1, kGgxDielectric = 2 };
+enum { kLambert = 0, kGgxConductor = 1, kGgxDielectric = 2, kPhong = 3, kSmoothConductor = 4, kSmoothDielectric = 5 };
 
 struct MatRecord {   // src/materials.hxx:48-207 (the fields the path tracer reads)
     V3 wol, wil, attenuation;
@@ -415,7 +430,9 @@ struct MatRecord {   // src/materials.hxx:48-207 (the fields the path tracer rea
 
 struct Material {
     int kind = kLambert;
-    V3 reflectance;
+    V3 reflectance;            // Lambert reflectance; Phong diffuse reflectance (mDiffuseReflectance)
+    V3 glossy;                 // Phong mPhongReflectance
+    float exponent = 1.f;      // Phong mPhongExponent
     float alpha = 0.1f, eta = 1.f, etaInv = 1.f, absorb = 0.f;
     // Sampling overrides (not in the reference): the GGX roughness that sampling and pdfs use and
     // the roulette continuation probability, for finite differences that hold sampling fixed
@@ -441,17 +458,74 @@ struct Material {
         return m;
     }
 
-    bool IsReflectanceZero() const   // :321-324, 873-876, 1110-1113
+    // PhongMaterial (:366-381), with the diffuse part as the material holds it
+    static Material Phong(V3 d, V3 g, float e)
     {
-        return kind == kLambert && IsZero(reflectance);
+        Material m; m.kind = kPhong; m.reflectance = d; m.glossy = g; m.exponent = e;
+        return m;
+    }
+    static Material SmoothConductor(float n, float no, float k)   // :658-668
+    {
+        Material m; m.kind = kSmoothConductor;
+        m.eta = IsTiny(no) ? 1.0f : n / no;
+        m.absorb = k;
+        return m;
+    }
+    static Material SmoothDielectric(float n, float no)   // :713-727
+    {
+        Material m; m.kind = kSmoothDielectric;
+        m.eta = IsTiny(no) ? 1.0f : n / no;
+        m.etaInv = IsTiny(n) ? 1.0f : no / n;
+        return m;
     }
 
-    float RRContinuationProb() const  // :300-319, 853-858, 1102-1108
+    // Light-sampling sides (:36-45): front side for all but the smooth materials, whose Dirac
+    // lobes take no light samples (kBsdfNone, :604-609) -- their light samples are all zero.
+    bool SamplesLights() const { return kind < kSmoothConductor; }
+
+    bool IsReflectanceZero() const   // :321-324, 572-575, 702-705, 777-780, 873-876, 1110-1113
+    {
+        if (kind == kLambert) return IsZero(reflectance);
+        if (kind == kPhong) return IsZero(reflectance) && IsZero(glossy);
+        return false;
+    }
+
+    // :300-319, 542-570, 691-700, 770-775, 853-858, 1102-1108
+    float RRContinuationProb(V3 wol) const
     {
         if (rrOverride >= 0.f) return rrOverride;
-        if (kind != kLambert) return 1.0f;
-        const float p = 0.15f * Luminance(reflectance) + 0.85f * MaxC(reflectance);
-        return Clampf(p, 0.f, 1.f);
+        if (kind == kLambert) {
+            const float p = 0.15f * Luminance(reflectance) + 0.85f * MaxC(reflectance);
+            return Clampf(p, 0.f, 1.f);
+        }
+        if (kind == kPhong) {
+            const float d = 0.15f * Luminance(reflectance) + 0.85f * MaxC(reflectance);
+            const float g = (0.15f * Luminance(glossy) + 0.85f * MaxC(glossy)) * (0.5f + 0.5f * std::max(wol.z, 0.f));
+            return Clampf(d + g, 0.f, 1.f);
+        }
+        if (kind == kSmoothConductor) return FresnelConductor(wol.z, eta, absorb);
+        return 1.0f;
+    }
+
+    // ---- Phong helpers (:383-531)
+    float PhongDiffuseEst() const { return Luminance(reflectance); }
+    float PhongGlossyEst(V3 wol) const { return Luminance(glossy) * (0.5f + 0.5f * std::max(wol.z, 0.f)); }
+    V3 PhongEval(V3 wil, V3 wol) const
+    {
+        if (wil.z <= 0.f || wol.z <= 0.f) return V3(0.f);
+        const float constComponent = (exponent + 2.0f) / (2.0f * kPiF);
+        const V3 wrl = ReflectLocal(wil);
+        const float thetaRCos = std::max(Dot(wrl, wol), 0.f);
+        return reflectance / kPiF + glossy * (constComponent * std::pow(thetaRCos, exponent));
+    }
+    float PhongPdf(V3 wol, V3 wil, float dEst, float gEst) const
+    {
+        const float tot = dEst + gEst;
+        if (tot < 1e-5f) return CosHemispherePdfW(wil.z);
+        Frame lobe;
+        lobe.SetFromZ(ReflectLocal(wol));
+        const V3 wc = lobe.ToLocal(wil);
+        return (dEst / tot) * CosHemispherePdfW(wil.z) + (gEst / tot) * PowerCosHemispherePdfW(wc, exponent);
     }
 
     // ---- GGX conductor helpers (src/materials.hxx:878-989)
@@ -530,11 +604,19 @@ struct Material {
             r.attenuation = CondEval(c);
             r.compProb = 1.0f;
             r.pdfW = CondPdf(c);
-        } else {
+        } else if (kind == kGgxDielectric) {
             DielCtx c = DielInit(r.wil, r.wol);
             r.attenuation = DielEval(c);
             r.compProb = 1.0f;
             r.pdfW = DielPdf(c);
+        } else if (kind == kPhong) {   // :416-431, 577-593
+            r.attenuation = PhongEval(r.wil, r.wol);
+            r.pdfW = PhongPdf(r.wol, r.wil, PhongDiffuseEst(), PhongGlossyEst(r.wol));
+            r.compProb = 1.0f;
+        } else {   // smooth materials (:611-655): no finite component
+            r.attenuation = V3(0.f);
+            r.pdfW = 0.f;
+            r.compProb = 0.f;
         }
     }
 
@@ -559,7 +641,7 @@ struct Material {
             r.pdfW = CondPdf(c);
             if (!above || c.wil.z < 0.0f) r.attenuation = V3(0.f);
             else r.attenuation = CondEval(c);
-        } else {
+        } else if (kind == kGgxDielectric) {
             DielCtx c;
             c.below = r.wol.z < 0.f;
             const float s = c.below ? -1.0f : 1.0f;
@@ -586,6 +668,47 @@ struct Material {
             r.pdfW = DielPdf(c);
             if (!above || cosAbs < 0.0f) r.attenuation = V3(0.f);
             else r.attenuation = DielEval(c);
+        } else if (kind == kPhong) {   // :437-495; u[2] picks the component
+            const float dEst = PhongDiffuseEst(), gEst = PhongGlossyEst(r.wol);
+            const float tot = dEst + gEst;
+            if (tot < 1e-5f) {
+                r.attenuation = V3(0.f);
+                r.wil = SampleCosHemisphereW(u[0], u[1], &r.pdfW);
+                r.compProb = 1.f;
+                return;
+            }
+            if (u[2] * tot < dEst) {
+                r.wil = SampleCosHemisphereW(u[0], u[1], nullptr);
+            } else {
+                const V3 cs = SamplePowerCosHemisphereW(u[0], u[1], exponent);
+                Frame lobe;
+                lobe.SetFromZ(ReflectLocal(r.wol));
+                r.wil = lobe.ToWorld(cs);
+            }
+            r.compProb = 1.f;
+            r.pdfW = PhongPdf(r.wol, r.wil, dEst, gEst);
+            r.attenuation = (r.wil.z > 0.0f) ? PhongEval(r.wil, r.wol) : V3(0.f);
+        } else if (kind == kSmoothConductor) {   // :670-689
+            r.wil = ReflectLocal(r.wol);
+            r.pdfW = kInf;
+            r.compProb = 1.f;
+            r.attenuation = V3(FresnelConductor(r.wil.z, eta, absorb));
+        } else {   // smooth dielectric, :730-767
+            const float F = FresnelDielectric(r.wol.z, eta);
+            float a;
+            if (u[2] <= F) {
+                r.wil = ReflectLocal(r.wol);
+                a = F;
+                r.compProb = F;
+            } else {
+                bool above;
+                r.wil = Refract(above, r.wol, V3(0.f, 0.f, 1.f), eta);
+                a = 1.0f - F;
+                a *= above ? Sqr(eta) : Sqr(etaInv);
+                r.compProb = 1.0f - F;
+            }
+            r.attenuation = V3(a);
+            r.pdfW = kInf;
         }
     }
 };
@@ -825,6 +948,29 @@ struct AreaLight {   // src/lights.hxx:55-229
     }
 };
 
+struct PointLight {   // src/lights.hxx:232-343
+    V3 position, intensity;
+    void SetPower(V3 power) { intensity = power / (4 * kPiF); }   // :244-247
+    // ComputeIllumination (:300-337) for a front-side-sampling material; the pdf is infinite
+    void Sample(V3 pt, const Frame &sf, V3 &wig, float &dist, V3 &sample, float &pdfW) const
+    {
+        wig = position - pt;
+        const float distSqr = Dot(wig, wig);
+        dist = std::sqrt(distSqr);
+        wig = wig / dist;
+        const float cosThetaIn = std::max(Dot(sf.Normal(), wig), 0.0f);
+        sample = (cosThetaIn > 0.f) ? intensity * cosThetaIn / distSqr : V3(0.f);
+        pdfW = kInf;
+    }
+    float Estimate(V3 pt, const Frame &sf) const   // :279-291
+    {
+        V3 w, s;
+        float d, p;
+        Sample(pt, sf, w, d, s, p);
+        return Luminance(s);
+    }
+};
+
 struct Scene {
     float camPos[3]{}, camFwd[3]{}, camUp[3]{};
     uint32_t W = 0, H = 0;
@@ -835,6 +981,7 @@ struct Scene {
     std::vector<Tri> tris;
     std::vector<Sph> sphs;
     std::vector<AreaLight> lights;        // area lights, ids 0..n-1
+    std::vector<PointLight> points;       // point lights, ids n..n+m-1 (src/scene.hxx:817-825)
     std::vector<int> mat2light;
     bool hasBg = false, bgIsEm = false;
     V3 bgConst;
@@ -846,7 +993,7 @@ struct Scene {
     uint32_t splitBudget = 1;
     float splitLevel = 1.f, lightRatio = 1.f, clipping = 0.f;
 
-    size_t LightCount() const { return lights.size() + (hasBg ? 1 : 0); }
+    size_t LightCount() const { return lights.size() + points.size() + (hasBg ? 1 : 0); }
     float shL[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};   // SH coefficients of the map's luminance
     // (texel luminance x basis x texel solid angle, the steerable sampler's basis)
     void ComputeShL()
@@ -957,6 +1104,7 @@ public:
     {
         est.resize(S.LightCount());
         for (size_t i = 0; i < S.lights.size(); ++i) est[i] = S.lights[i].Estimate(pt, f);
+        for (size_t i = 0; i < S.points.size(); ++i) est[S.lights.size() + i] = S.points[i].Estimate(pt, f);
         if (S.hasBg) {
             if (!S.bgIsEm) {
                 est[S.bgLightId] = Luminance(S.bgConst) * kPiF;
@@ -1064,10 +1212,10 @@ public:
         SplittingCounts(budget, nBsdf, nLight, nextBudget);
 
         std::vector<float> est;
-        if (S.LightCount() > 1) Estimates(pt, frame, est);
+        if (S.LightCount() > 1 && mat.SamplesLights()) Estimates(pt, frame, est);
 
-        // Light samples + MIS (src/path_tracer.hxx:250-265, src/path_tracer_base.hxx:156-188, 350-411)
-        if (pathLength + 1 >= S.minPL) {
+        // Light samples + MIS (src/path_tracer.hxx:250-265, src/path_tracer_base.hxx:156-188, 350-423)
+        if (pathLength + 1 >= S.minPL && mat.SamplesLights()) {
             for (uint32_t j = 0; j < nLight; ++j) {
                 const Rand4 ra = Draw(key.seed, key.pixel, key.sample, me, 2 * j);
                 int lid = -1;
@@ -1083,16 +1231,20 @@ public:
                     mr.wil = frame.ToLocal(wig);
                     mr.wol = wol;
                     mat.Eval(mr);
-                    const float bsdfPdf = mr.pdfW * mr.compProb;
-                    const float lightPdf = pdfW * lprob;
-                    reflected += (smp * mr.attenuation * MISn(lightPdf, nLight, bsdfPdf, nBsdf)) / lightPdf;
+                    if (pdfW == kInf) {   // point light: exact contribution, only the picking is estimated
+                        reflected += (smp * mr.attenuation) / (lprob * nLight);
+                    } else {
+                        const float bsdfPdf = mr.pdfW * mr.compProb;
+                        const float lightPdf = pdfW * lprob;
+                        reflected += (smp * mr.attenuation * MISn(lightPdf, nLight, bsdfPdf, nBsdf)) / lightPdf;
+                    }
                 }
             }
         }
 
         // Russian roulette (src/path_tracer.hxx:267-303)
         const bool rrActive = (S.maxPL == 0) || (S.rrMinPL > 0 && pathLength >= S.rrMinPL);
-        const float rrProb = rrActive ? Clampf(mat.RRContinuationProb(), 0.0f, 0.997f) : 1.0f;
+        const float rrProb = rrActive ? Clampf(mat.RRContinuationProb(wol), 0.0f, 0.997f) : 1.0f;
 
         // BSDF samples (src/path_tracer.hxx:305-405)
         for (uint32_t i = 0; i < nBsdf; ++i) {
@@ -1159,7 +1311,7 @@ public:
             const bool rrActive = (S.maxPL == 0) || (S.rrMinPL > 0 && pl >= S.rrMinPL);
             float rr = 1.0f;
             if (rrActive) {
-                rr = Clampf(mat.RRContinuationProb(), 0.0f, 0.997f);
+                rr = Clampf(mat.RRContinuationProb(wol), 0.0f, 0.997f);
                 if (rb.v[0] > rr) return L;
             }
             MatRecord mr;
@@ -1177,14 +1329,16 @@ public:
         }
     }
 
-    // Light sample of light `lid` from the shading point (area: src/lights.hxx:114-131;
-    // background: :424-445); u holds three uniforms.
+    // Light sample of light `lid` from the shading point (area: src/lights.hxx:114-131; point:
+    // :255-266; background: :424-445); u holds three uniforms.
     void SampleLight(int lid, V3 pt, const Frame &frame, const float u[3], V3 &wig, float &dist, V3 &smp,
                      float &pdfW) const
     {
         if (lid == S.bgLightId) {
             S.BgSample(frame, u, wig, pdfW, smp);
             dist = std::numeric_limits<float>::max();
+        } else if (lid >= (int)S.lights.size()) {
+            S.points[lid - S.lights.size()].Sample(pt, frame, wig, dist, smp, pdfW);
         } else {
             const AreaLight &L = S.lights[lid];
             const V3 sp = SampleUniformTriangle(L.p0, L.p0 + L.e1, L.p0 + L.e2, u[0], u[1]);
@@ -1214,7 +1368,8 @@ public:
             L = S.BgEmission(wig, pdfW, &frame);
             lightId = S.bgLightId;
         }
-        if (pickProb && lightId >= 0) *pickProb = PickProb(est, lightId);
+        // (no estimates at a vertex without light samples: its Dirac BSDF samples take no MIS)
+        if (pickProb && lightId >= 0) *pickProb = (S.LightCount() > 1 && est.empty()) ? 0.f : PickProb(est, lightId);
         return L;
     }
 
@@ -1244,7 +1399,8 @@ public:
         const V3 wol = frame.ToLocal(-dir);
         const Material &mat = S.mats[h.mat];
         std::vector<float> est;
-        if (S.LightCount() > 1) Estimates(pt, frame, est);
+        const bool lights = mat.SamplesLights();
+        if (S.LightCount() > 1 && lights) Estimates(pt, frame, est);
         const Rand4 ra = Draw(key.seed, key.pixel, key.sample, 1, 0);
         const Rand4 rb = Draw(key.seed, key.pixel, key.sample, 1, 1);
         V3 Lo(0.f);
@@ -1258,15 +1414,16 @@ public:
             mr.wil = frame.ToLocal(wig);
             mr.wol = wol;
             mat.Eval(mr);
-            Lo += smp * mr.attenuation / (pdfW * prob);
+            if (pdfW == kInf) Lo += smp * mr.attenuation / prob;   // point light (:333-348)
+            else Lo += smp * mr.attenuation / (pdfW * prob);
         };
-        if (alg == 3) {
+        if (alg == 3 && lights) {
             for (size_t i = 0; i < S.LightCount(); ++i) {
                 const Rand4 rl = Draw(key.seed, key.pixel, key.sample, 1, 2 + (uint32_t)i);
                 const float lu[3] = {rl.v[1], rl.v[2], rl.v[3]};
                 single((int)i, 1.f, lu);
             }
-        } else if (alg == 4) {
+        } else if (alg == 4 && lights) {
             int lid = -1;
             float lprob = 0.f;
             Pick(est, ra.v[0], lid, lprob);
@@ -1282,11 +1439,11 @@ public:
                 Lo = mr.IsFinite() ? (mr.attenuation * mr.CosAbs() * Li) / (mr.pdfW * mr.compProb)
                                    : (mr.attenuation * Li) / mr.compProb;
             }
-        } else {
+        } else if (alg == 5) {
             // kDirectIllumMis: one light sample and one BSDF sample (:99-114), power heuristic
             int lid = -1;
             float lprob = 0.f;
-            Pick(est, ra.v[0], lid, lprob);
+            if (lights) Pick(est, ra.v[0], lid, lprob);
             if (lid >= 0) {
                 V3 wig, smp;
                 float dist, pdfW;
@@ -1297,8 +1454,12 @@ public:
                     mr.wil = frame.ToLocal(wig);
                     mr.wol = wol;
                     mat.Eval(mr);
-                    const float lightPdf = pdfW * lprob;
-                    Lo += (smp * mr.attenuation * MIS(lightPdf, mr.pdfW * mr.compProb)) / lightPdf;
+                    if (pdfW == kInf) {
+                        Lo += (smp * mr.attenuation) / lprob;
+                    } else {
+                        const float lightPdf = pdfW * lprob;
+                        Lo += (smp * mr.attenuation * MIS(lightPdf, mr.pdfW * mr.compProb)) / lightPdf;
+                    }
                 }
             }
             MatRecord mr;   // AddDirectIllumMISBrdfSampleContribution (:427-486)
@@ -1389,6 +1550,23 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
         } else if (k == "ggx_dielectric") {
             float a, n, no; ls >> a >> n >> no;
             s.mats.push_back(Material::Dielectric(a, n, no));
+        } else if (k == "phong") {
+            float d[3], g[3], e;
+            ls >> d[0] >> d[1] >> d[2] >> g[0] >> g[1] >> g[2] >> e;
+            s.mats.push_back(Material::Phong(V3(d[0], d[1], d[2]), V3(g[0], g[1], g[2]), e));
+        } else if (k == "smooth_conductor") {
+            float n, no, kk; ls >> n >> no >> kk;
+            s.mats.push_back(Material::SmoothConductor(n, no, kk));
+        } else if (k == "smooth_dielectric") {
+            float n, no; ls >> n >> no;
+            s.mats.push_back(Material::SmoothDielectric(n, no));
+        } else if (k == "point_light") {
+            float p[3], w[3];
+            ls >> p[0] >> p[1] >> p[2] >> w[0] >> w[1] >> w[2];
+            PointLight pl;
+            pl.position = V3(p[0], p[1], p[2]);
+            pl.SetPower(V3(w[0], w[1], w[2]));
+            s.points.push_back(pl);
         } else if (k == "triangle" || k == "area_light") {
             float v[9]; int mat;
             for (float &x : v) ls >> x;
@@ -1448,7 +1626,7 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
         }
     }
     s.mat2light.resize(std::max(s.mat2light.size(), s.mats.size()), -1);
-    if (s.hasBg) s.bgLightId = (int)s.lights.size();   // the background is pushed last (src/scene.hxx:948-953)
+    if (s.hasBg) s.bgLightId = (int)(s.lights.size() + s.points.size());   // pushed last (src/scene.hxx:948-953)
     if (s.bgIsEm) {
         s.em.BuildCdf();
         if (hasSamplingEm) {

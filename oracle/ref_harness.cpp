@@ -16,9 +16,13 @@
 //   lambert r g b
 //   ggx_conductor alpha n_inner n_outer k
 //   ggx_dielectric alpha n_inner n_outer
+//   phong dr dg db gr gg gb exponent         (diffuse part as the material holds it)
+//   smooth_conductor n_inner n_outer k
+//   smooth_dielectric n_inner n_outer
 //   triangle x0 y0 z0 x1 y1 z1 x2 y2 z2 material
 //   sphere cx cy cz radius material
 //   area_light x0 y0 z0 x1 y1 z1 x2 y2 z2 material Lr Lg Lb
+//   point_light x y z power_r power_g power_b
 //   background_const r g b
 //   background_em path
 //   options algorithm(el|nv|dbs|dlsa|dlss|dmis|ptn|pt) min_path_length max_path_length
@@ -87,6 +91,33 @@ SceneFile LoadScene(const char *path, const AuxDbgParams &aux)
             float a, n, no;
             ls >> a >> n >> no;
             s->mMaterials.push_back(new MicrofacetGGXDielectricMaterial(a, n, no));
+        } else if (kind == "phong") {
+            // PhongMaterial halves the diffuse part when the glossy lobe is on: hand it twice
+            // the held value (exact in binary floating point)
+            float d[3], g[3], e;
+            ls >> d[0] >> d[1] >> d[2] >> g[0] >> g[1] >> g[2] >> e;
+            const bool glossy = g[0] != 0.f || g[1] != 0.f || g[2] != 0.f;
+            const float k = glossy ? 2.f : 1.f;
+            SpectrumF dr, gr;
+            dr.SetSRGBAttenuation(k * d[0], k * d[1], k * d[2]);
+            gr.SetSRGBAttenuation(g[0], g[1], g[2]);
+            s->mMaterials.push_back(new PhongMaterial(dr, gr, e, 1u, glossy ? 1u : 0u));
+        } else if (kind == "smooth_conductor") {
+            float n, no, k;
+            ls >> n >> no >> k;
+            s->mMaterials.push_back(new SmoothConductorMaterial(n, no, k));
+        } else if (kind == "smooth_dielectric") {
+            float n, no;
+            ls >> n >> no;
+            s->mMaterials.push_back(new SmoothDielectricMaterial(n, no));
+        } else if (kind == "point_light") {
+            float p[3], w[3];
+            ls >> p[0] >> p[1] >> p[2] >> w[0] >> w[1] >> w[2];
+            PointLight *light = new PointLight(Vec3f(p[0], p[1], p[2]));
+            SpectrumF power;
+            power.SetSRGBLight(w[0], w[1], w[2]);
+            light->SetPower(power);
+            s->mLights.push_back(Scene::TLightSharedPtr(light));
         } else if (kind == "triangle" || kind == "area_light") {
             float v[9];
             int mat;

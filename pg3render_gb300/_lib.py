@@ -31,7 +31,8 @@ class Camera(ctypes.Structure):
 
 class Material(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("albedo", c_float3), ("alpha", ctypes.c_float),
-                ("ior", ctypes.c_float), ("ior_outer", ctypes.c_float), ("absorb", ctypes.c_float)]
+                ("ior", ctypes.c_float), ("ior_outer", ctypes.c_float), ("absorb", ctypes.c_float),
+                ("glossy", c_float3), ("phong_exponent", ctypes.c_float)]
 
 
 class Triangle(ctypes.Structure):
@@ -46,6 +47,10 @@ class AreaLight(ctypes.Structure):
     _fields_ = [("triangle", ctypes.c_uint32), ("radiance", c_float3)]
 
 
+class PointLight(ctypes.Structure):
+    _fields_ = [("position", c_float3), ("power", c_float3)]
+
+
 class SceneDesc(ctypes.Structure):
     _fields_ = [("camera", Camera),
                 ("materials", ctypes.POINTER(Material)), ("num_materials", ctypes.c_uint32),
@@ -54,7 +59,8 @@ class SceneDesc(ctypes.Structure):
                 ("area_lights", ctypes.POINTER(AreaLight)), ("num_area_lights", ctypes.c_uint32),
                 ("background", ctypes.c_int32), ("background_radiance", c_float3),
                 ("env_map", ctypes.POINTER(ctypes.c_float)),
-                ("env_width", ctypes.c_uint32), ("env_height", ctypes.c_uint32)]
+                ("env_width", ctypes.c_uint32), ("env_height", ctypes.c_uint32),
+                ("point_lights", ctypes.POINTER(PointLight)), ("num_point_lights", ctypes.c_uint32)]
 
 
 class Options(ctypes.Structure):
@@ -175,7 +181,8 @@ def scene_desc(scene):
     d.camera = Camera(c_float3(*c.position), c_float3(*c.forward), c_float3(*c.up), c.width, c.height, c.hfov_deg)
     mats = (Material * max(1, len(scene.materials)))()
     for i, m in enumerate(scene.materials):
-        mats[i] = Material(m.kind, c_float3(*m.albedo), m.alpha, m.ior, m.ior_outer, m.absorb)
+        mats[i] = Material(m.kind, c_float3(*m.albedo), m.alpha, m.ior, m.ior_outer, m.absorb,
+                           c_float3(*m.glossy), m.phong_exponent)
     tris = (Triangle * max(1, len(scene.triangles)))()
     for i, (p0, p1, p2, mat) in enumerate(scene.triangles):
         tris[i] = Triangle((ctypes.c_float * 9)(*p0, *p1, *p2), mat)
@@ -189,7 +196,11 @@ def scene_desc(scene):
     d.triangles, d.num_triangles = tris, len(scene.triangles)
     d.spheres, d.num_spheres = sphs, len(scene.spheres)
     d.area_lights, d.num_area_lights = lights, len(scene.area_lights)
-    keep = [mats, tris, sphs, lights]
+    points = (PointLight * max(1, len(scene.point_lights)))()
+    for i, (pos, power) in enumerate(scene.point_lights):
+        points[i] = PointLight(c_float3(*pos), c_float3(*power))
+    d.point_lights, d.num_point_lights = points, len(scene.point_lights)
+    keep = [mats, tris, sphs, lights, points]
     if scene.env_map is not None:
         em = np.ascontiguousarray(scene.env_map, dtype=np.float32)
         d.background = BG_ENVMAP

@@ -163,7 +163,7 @@ int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passe
     uint64_t launches = 1;
     if (wave) {
         launches = 0;
-        e = launchWavefront(ctx->view, false, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
+        e = launchWavefront(ctx->view, ctx->kindMask, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
                             ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->stream, &launches);
     } else
         e = launchMegakernel(ctx->view, algorithm, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
@@ -259,6 +259,8 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
     ctx->W = scene->camera.width;
     ctx->H = scene->camera.height;
     ctx->nmat = scene->num_materials;
+    ctx->kindMask = hs.kindMask;
+    ctx->numPointLights = hs.numPointLights;
     auto bail = [&](int s) {
         g_createError = ctx->lastError;
         pg3gpu_destroy(ctx);

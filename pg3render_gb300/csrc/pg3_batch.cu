@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const SceneView *sv = stageViews(views, ninst, smem);
-    constexpr int kBucket = (K < 0) ? kBucketMiss : 1 + K;
+    constexpr int kBucket = bucketOfShade(K);
     const int cur = (int)ctl->cur;
     const uint32_t n = B.q.cnt->bucket[kBucket];
     const float4 *rq = B.q.ray[cur];
@@ -354,6 +354,7 @@ struct pg3gpu_batch {
     uint64_t totalPaths = 0;
     uint32_t maxLen = 0;
     int emk = kEmCosine;
+    uint32_t kindMask = 0;           // material kinds of all instances (bit per kind)
     int sms = 0;
     SceneView *dViews = nullptr;
     BatchInst *dInst = nullptr;
@@ -445,17 +446,34 @@ StepShape stepShape(const pg3gpu_batch *b)
     return s;
 }
 
+// Shade kernels of the miss bucket and of the material kinds present in the batch.
+int shadeLaunches(uint32_t kindMask)
+{
+    int n = 1;
+    for (int k = kMatLambert; k <= kMatPhong; ++k) n += (kindMask >> k) & 1u;
+    return n + ((kindMask & ((1u << kMatSmoothConductor) | (1u << kMatSmoothDielectric))) ? 1 : 0);
+}
+int stepLaunches(const pg3gpu_batch *b) { return 4 + shadeLaunches(b->kindMask); }
+
 template <int EMK>
 void launchShadeBatch(const pg3gpu_batch *b, const StepShape &s, cudaStream_t st)
 {
     const uint32_t n = (uint32_t)b->inst.size();
+    const uint32_t m = b->kindMask;
     batchShade<-1, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
-    batchShade<kMatLambert, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
-    batchShade<kMatGgxConductor, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
-    batchShade<kMatGgxDielectric, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
+    if (m & (1u << kMatLambert))
+        batchShade<kMatLambert, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
+    if (m & (1u << kMatGgxConductor))
+        batchShade<kMatGgxConductor, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
+    if (m & (1u << kMatGgxDielectric))
+        batchShade<kMatGgxDielectric, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
+    if (m & (1u << kMatPhong))
+        batchShade<kMatPhong, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
+    if (m & ((1u << kMatSmoothConductor) | (1u << kMatSmoothDielectric)))
+        batchShade<kShadeSmooth, EMK><<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
 }
 
-// One step of the loop (7 launches).
+// One step of the loop (regen, extend, the shade kernels, shadow, advance).
 void launchStep(const pg3gpu_batch *b, const StepShape &s, cudaStream_t st, int useGraph)
 {
     const uint32_t n = (uint32_t)b->inst.size();
@@ -538,7 +556,7 @@ void collectSteps(pg3gpu_batch *b)
     if (!b->stepsPending || !b->dCtl) return;
     uint32_t steps = 0;
     if (cudaMemcpy(&steps, &b->dCtl->steps, sizeof steps, cudaMemcpyDeviceToHost) == cudaSuccess)
-        b->launches += 1 + 8ull * steps;
+        b->launches += 1 + (uint64_t)stepLaunches(b) * steps;
     b->stepsPending = false;
 }
 
@@ -569,7 +587,7 @@ int runOnce(pg3gpu_batch *b)
         uint32_t done = 0;
         for (uint64_t c = 0; c < maxChecks && !done; ++c) {
             for (int k = 0; k < 8; ++k) launchStep(b, s, b->stream, 0);
-            b->launches += 64;
+            b->launches += 8ull * stepLaunches(b);
             if (int st = bcuda(b, cudaMemcpyAsync(&done, &b->dCtl->done, sizeof done, cudaMemcpyDeviceToHost, b->stream),
                                "done flag"))
                 return st;
@@ -639,6 +657,7 @@ int pg3gpu_batch_create(const pg3gpu_scene *scenes, const pg3gpu_options *opts, 
         if (st) return bail(bfail(b, st, who + pg3gpu_last_error(nullptr)));
         b->inst.push_back(c);
         b->spp.push_back(spp[i]);
+        b->kindMask |= c->kindMask;
         if (c->view.bgKind == kBgEnvMap) {
             if (emk >= 0 && emk != c->view.emSampler)
                 return bail(bfail(b, PG3GPU_ERR_UNSUPPORTED, who + "all environment-map instances must use one sampler"));

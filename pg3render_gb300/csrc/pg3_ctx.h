@@ -22,6 +22,8 @@ struct pg3gpu_ctx {
     std::vector<void *> allocs;
     uint32_t W = 0, H = 0;
     uint32_t nmat = 0;
+    uint32_t kindMask = 0;               // material kinds of the scene (bit per kind)
+    uint32_t numPointLights = 0;
     uint32_t *dBvhCodes = nullptr, *dBvhIds = nullptr;   // sorted Morton codes / primitive ids of the LBVH
     double *dSum = nullptr, *dSumsq = nullptr;
     float *dOut[3] = {nullptr, nullptr, nullptr};

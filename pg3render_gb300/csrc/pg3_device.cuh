@@ -4,7 +4,7 @@
 // (file:line given per function, paths relative to the reference project) in
 // a form suited to a GPU thread: float3 registers instead of Vec3f objects,
 // a counter-based random stream instead of a per-renderer mt19937_64, and no
-// virtual dispatch (materials are a switch over a 48-byte record).
+// virtual dispatch (materials are a switch over a 64-byte record).
 #pragma once
 
 #include <cstdint>
@@ -159,6 +159,22 @@ PG3_DI float3 sampleCosHemisphere(float u0, float u1, float &pdf)
     return r;
 }
 PG3_DI float cosHemispherePdf(float z) { return fmaxf(0.f, z) * kPiInvF; }
+// SamplePowerCosHemisphereW / PowerCosHemispherePdfW (src/sampling.hxx:250-285): density
+// (n + 1) cos^n / (2 pi) around +z
+PG3_DI float3 samplePowerCosHemisphere(float u0, float u1, float power)
+{
+    const float t2 = powf(u1, 1.f / (power + 1.f));
+    const float t3 = sqrtf(1.f - t2 * t2);
+    float s, c;
+    sincosf(2.f * kPiF * u0, &s, &c);
+    return make_float3(c * t3, s * t3, t2);
+}
+PG3_DI float powerCosHemispherePdf(float z, float power)
+{
+    return (power + 1.f) * powf(fmaxf(0.f, z), power) * (kPiInvF * 0.5f);
+}
+// ReflectLocal (src/geom.hxx:110-113): mirror direction about the local normal
+PG3_DI float3 reflectLocal(float3 v) { return make_float3(-v.x, -v.y, v.z); }
 // upper hemisphere only: every material on this path samples lights from the front side
 // (kBsdfFrontSideLightSampling, src/materials.hxx:253-266, 788-806, 992-1021)
 PG3_DI float cosSpherePdfFront(float3 local) { return (local.z < 0.f) ? 0.f : cosHemispherePdf(fabsf(local.z)); }
@@ -380,6 +396,32 @@ PG3_DI float dielPdf(const DevMaterial &mt, const DielCtx &c)
     return vn * J * (c.refl ? c.F : (1.f - c.F));
 }
 
+// Phong: src/materials.hxx:353-602. Diffuse plus a power-cosine lobe around the mirror direction;
+// sampling picks the component by the luminance estimates below (the glossy one attenuated to
+// half at grazing angles) and the pdf is the whole mixture.
+PG3_DI float3 phongGlossy(const DevMaterial &m) { return make_float3(m.gr, m.gg, m.gb); }
+PG3_DI float phongDiffuseEst(const DevMaterial &m) { return luminance(make_float3(m.r, m.g, m.b)); }
+PG3_DI float phongGlossyEst(const DevMaterial &m, float3 wol)
+{
+    return luminance(phongGlossy(m)) * (0.5f + 0.5f * fmaxf(wol.z, 0.f));
+}
+PG3_DI float3 phongEval(const DevMaterial &m, float3 wil, float3 wol)      // :404-414
+{
+    if (wil.z <= 0.f || wol.z <= 0.f) return f3(0.f);
+    const float cc = (m.exponent + 2.0f) / (2.0f * kPiF);
+    const float c = fmaxf(dot(reflectLocal(wil), wol), 0.f);
+    return make_float3(m.r, m.g, m.b) * kPiInvF + phongGlossy(m) * (cc * powf(c, m.exponent));
+}
+PG3_DI float phongPdf(const DevMaterial &m, float3 wol, float3 wil, float dEst, float gEst)   // :497-531
+{
+    const float tot = dEst + gEst;
+    if (tot < 1e-5f) return cosHemispherePdf(wil.z);   // diffuse fallback of blockers
+    // the lobe frame's z axis is the mirror direction: the canonical cosine is dot(wil, wrl)
+    const float cz = dot(wil, reflectLocal(wol));
+    return (dEst / tot) * cosHemispherePdf(wil.z) + (gEst / tot) * powerCosHemispherePdf(cz, m.exponent);
+}
+PG3_DI float smoothDielectricFresnel(const DevMaterial &m, float3 wol) { return fresnelDielectric(wol.z, m.eta); }
+
 // EvalBsdf + GetOptData(kOptSamplingProbs) per material kind: :277-283 (Lambert),
 // :809-817 (conductor), :1023-1031 with InitEvalContext :1123-1160 (dielectric)
 // DA: also compute BsdfRec::dAtt
@@ -400,7 +442,7 @@ PG3_DI void evalBsdfK(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
         r.att = condEval(m, wil, wol, h, F, D);
         r.pdfW = condPdf(m, wol, h, ggxDp(m, h, D));
         if (DA) r.dAtt = ggxDlnDGda(wil, wol, h, m.alpha);
-    } else {
+    } else if (K == kMatGgxDielectric) {
         DielCtx c;
         const bool below = wol.z < 0.f;
         c.refl = (wil.z > 0.f) == (wol.z > 0.f);
@@ -416,13 +458,27 @@ PG3_DI void evalBsdfK(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
         r.att = dielEval(m, c);
         r.pdfW = dielPdf(m, c);
         if (DA) r.dAtt = ggxDlnDGda(c.wi, c.wo, c.m, m.alpha);
+    } else if (K == kMatPhong) {
+        r.att = phongEval(m, wil, wol);
+        r.pdfW = phongPdf(m, wol, wil, phongDiffuseEst(m), phongGlossyEst(m, wol));
+        if (DA) r.dAtt = 0.f;
+    } else {
+        // smooth conductor / dielectric (:611-655): Dirac lobes only, no finite component
+        r.att = f3(0.f);
+        r.pdfW = 0.f;
+        r.compProb = 0.f;
+        if (DA) r.dAtt = 0.f;
     }
 }
 PG3_DI void evalBsdf(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
 {
-    if (m.kind == kMatLambert) evalBsdfK<kMatLambert>(m, wil, wol, r);
-    else if (m.kind == kMatGgxConductor) evalBsdfK<kMatGgxConductor>(m, wil, wol, r);
-    else evalBsdfK<kMatGgxDielectric>(m, wil, wol, r);
+    switch (m.kind) {
+    case kMatLambert: evalBsdfK<kMatLambert>(m, wil, wol, r); break;
+    case kMatGgxConductor: evalBsdfK<kMatGgxConductor>(m, wil, wol, r); break;
+    case kMatGgxDielectric: evalBsdfK<kMatGgxDielectric>(m, wil, wol, r); break;
+    case kMatPhong: evalBsdfK<kMatPhong>(m, wil, wol, r); break;
+    default: evalBsdfK<kMatSmoothConductor>(m, wil, wol, r); break;
+    }
 }
 
 // SampleBsdf per material kind: :285-292 (Lambert), :819-851 (conductor), :1033-1100 (dielectric)
@@ -444,7 +500,7 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         const float3 wil = reflect(above, wol, h);
         evalBsdfK<K, DA>(m, wil, wol, r);
         if (!above || wil.z < 0.0f) r.att = f3(0.f);
-    } else {
+    } else if (K == kMatGgxDielectric) {
         DielCtx c;
         const bool below = wol.z < 0.f;
         const float s = below ? -1.0f : 1.0f;
@@ -466,13 +522,90 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         const float3 wil = c.wi * s;
         evalBsdfK<K, DA>(m, wil, wol, r);
         if (!above || cosAbs < 0.0f) r.att = f3(0.f);
+    } else if (K == kMatPhong) {
+        // :437-495; u2 picks the component, (u0, u1) the direction
+        if (DA) r.dAtt = 0.f;
+        const float dEst = phongDiffuseEst(m), gEst = phongGlossyEst(m, wol);
+        const float tot = dEst + gEst;
+        if (tot < 1e-5f) {   // diffuse fallback of blockers
+            r.att = f3(0.f);
+            r.wil = sampleCosHemisphere(u0, u1, r.pdfW);
+            return;
+        }
+        float pdfDummy;
+        if (u2 * tot < dEst) {
+            r.wil = sampleCosHemisphere(u0, u1, pdfDummy);
+        } else {
+            const float3 cs = samplePowerCosHemisphere(u0, u1, m.exponent);
+            r.wil = toWorld(frameFromZ(reflectLocal(wol)), cs);
+        }
+        r.pdfW = phongPdf(m, wol, r.wil, dEst, gEst);
+        r.att = (r.wil.z > 0.f) ? phongEval(m, r.wil, wol) : f3(0.f);
+    } else if (K == kMatSmoothConductor) {
+        // :670-689: mirror direction, grey conductor Fresnel
+        if (DA) r.dAtt = 0.f;
+        r.wil = reflectLocal(wol);
+        r.pdfW = infF();
+        r.att = f3(fresnelConductor(r.wil.z, m.eta, m.absorb));
+    } else {
+        // :725-767: reflection with probability F (total internal reflection included), else
+        // refraction with the radiance scaled by eta^2 or 1/eta^2
+        if (DA) r.dAtt = 0.f;
+        const float F = smoothDielectricFresnel(m, wol);
+        float a;
+        if (u2 <= F) {
+            r.wil = reflectLocal(wol);
+            a = F;
+            r.compProb = F;
+        } else {
+            bool above;
+            r.wil = refract(above, wol, make_float3(0.f, 0.f, 1.f), m.eta);
+            a = (1.0f - F) * (above ? sqr(m.eta) : sqr(m.etaInv));
+            r.compProb = 1.0f - F;
+        }
+        r.att = f3(a);
+        r.pdfW = infF();
     }
 }
 PG3_DI void sampleBsdf(const DevMaterial &m, float3 wol, float u0, float u1, float u2, BsdfRec &r)
 {
-    if (m.kind == kMatLambert) sampleBsdfK<kMatLambert>(m, wol, u0, u1, u2, r);
-    else if (m.kind == kMatGgxConductor) sampleBsdfK<kMatGgxConductor>(m, wol, u0, u1, u2, r);
-    else sampleBsdfK<kMatGgxDielectric>(m, wol, u0, u1, u2, r);
+    switch (m.kind) {
+    case kMatLambert: sampleBsdfK<kMatLambert>(m, wol, u0, u1, u2, r); break;
+    case kMatGgxConductor: sampleBsdfK<kMatGgxConductor>(m, wol, u0, u1, u2, r); break;
+    case kMatGgxDielectric: sampleBsdfK<kMatGgxDielectric>(m, wol, u0, u1, u2, r); break;
+    case kMatPhong: sampleBsdfK<kMatPhong>(m, wol, u0, u1, u2, r); break;
+    case kMatSmoothConductor: sampleBsdfK<kMatSmoothConductor>(m, wol, u0, u1, u2, r); break;
+    default: sampleBsdfK<kMatSmoothDielectric>(m, wol, u0, u1, u2, r); break;
+    }
+}
+// The two Dirac materials share one wavefront bucket (kind read at run time).
+template <bool DA = false>
+PG3_DI void sampleBsdfSmooth(const DevMaterial &m, float3 wol, float u2, BsdfRec &r)
+{
+    if (m.kind == kMatSmoothConductor) sampleBsdfK<kMatSmoothConductor, DA>(m, wol, 0.f, 0.f, u2, r);
+    else sampleBsdfK<kMatSmoothDielectric, DA>(m, wol, 0.f, 0.f, u2, r);
+}
+
+// Does the material take light samples? Every kind but the Dirac ones samples lights from its
+// front side (kBsdfFrontSideLightSampling); smooth materials have no finite component
+// (kBsdfNone, src/materials.hxx:604-609), so their light samples are always zero.
+PG3_DI bool takesLightSamples(const DevMaterial &m) { return m.kind < kMatSmoothConductor; }
+
+// GetRRContinuationProb (src/materials.hxx:301-322, 542-570, 691-700, 770-775, 853-869, 1093-1098)
+// clamped to [0, 0.997] (src/path_tracer.hxx:281-283). Phong and the smooth conductor depend on
+// the outgoing direction; the others are constants of the record. KS: the kinds the caller can
+// see (-1 any, 0-3 that kind, 4 the smooth pair).
+template <int KS = -1>
+PG3_DI float rrContinuation(const DevMaterial &m, float3 wol)
+{
+    if ((KS < 0 || KS == kMatPhong) && m.kind == kMatPhong) {
+        const float3 gl = phongGlossy(m);
+        const float g = (0.15f * luminance(gl) + 0.85f * maxc(gl)) * (0.5f + 0.5f * fmaxf(wol.z, 0.f));
+        return fminf(clampf(m.rrProb + g, 0.f, 1.f), 0.997f);
+    }
+    if ((KS < 0 || KS == kMatSmoothConductor) && m.kind == kMatSmoothConductor)
+        return clampf(fresnelConductor(wol.z, m.eta, m.absorb), 0.f, 0.997f);
+    return m.rrProb;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -617,6 +750,41 @@ PG3_DI float3 areaEmission(const DevAreaLight &L, float3 lightPt, float wolZ, fl
     w = w / sqrtf(d2);
     pdf = fmaxf(L.p0_invArea.w * (d2 / fabsf(dot(xyz(L.n_b), w))), kEpsDist);
     return (wolZ <= 0.f) ? f3(0.f) : lightRadiance(L);
+}
+
+// ------------------------------------------------------------------------------------------
+// Point lights (src/lights.hxx:232-343): entries of the light table marked by a negative 1/area
+// ------------------------------------------------------------------------------------------
+PG3_DI bool isPointLight(const DevAreaLight &L) { return L.p0_invArea.w < 0.f; }
+// ComputeIllumination (:300-337) for a front-side-sampling material: I cos / d^2, pdf infinite
+PG3_DI void pointSample(const DevAreaLight &L, float3 pt, float3 sn, float3 &wig, float &dist, float3 &smp,
+                        float &pdfW)
+{
+    wig = xyz(L.p0_invArea) - pt;
+    const float d2 = dot(wig, wig);
+    dist = sqrtf(d2);
+    wig = wig / dist;
+    const float cosIn = fmaxf(dot(sn, wig), 0.0f);
+    smp = (cosIn > 0.f) ? lightRadiance(L) * cosIn / d2 : f3(0.f);
+    pdfW = infF();
+}
+// A light-table entry: sample (area: :114-131) and contribution estimate (area: :133-167,
+// point: the luminance of its only sample, :279-291)
+PG3_DI void tableSample(const DevAreaLight &L, float3 pt, float3 sn, float u0, float u1, float3 &wig, float &dist,
+                        float3 &smp, float &pdfW)
+{
+    if (isPointLight(L)) pointSample(L, pt, sn, wig, dist, smp, pdfW);
+    else areaSample(L, pt, sn, u0, u1, wig, dist, smp, pdfW);
+}
+PG3_DI float tableEstimate(const DevAreaLight &L, float3 pt, float3 sn)
+{
+    if (isPointLight(L)) {
+        float3 w, s;
+        float d, p;
+        pointSample(L, pt, sn, w, d, s, p);
+        return luminance(s);
+    }
+    return areaEstimate(L, pt, sn);
 }
 
 // ------------------------------------------------------------------------------------------

@@ -166,6 +166,11 @@ int diffChecks(pg3gpu_ctx *ctx)
         return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED, "differentiable rendering does not split paths or clip");
     if (ctx->nmat > kMaxDiffMaterials)
         return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED, "differentiable rendering supports at most 2048 materials");
+    if (ctx->kindMask & ~((1u << kMatLambert) | (1u << kMatGgxConductor) | (1u << kMatGgxDielectric)))
+        return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED,
+                        "differentiable rendering supports Lambert and GGX materials only (no Phong or smooth materials)");
+    if (ctx->numPointLights)
+        return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED, "differentiable rendering does not support point lights");
     return PG3GPU_OK;
 }
 
@@ -304,7 +309,7 @@ extern "C" int pg3gpu_diff_forward(pg3gpu_ctx *ctx, uint32_t iteration, uint32_t
     G.adjoint = 0;
     G.sampleOffset = ctx->dSampleOffset;
     uint64_t launches = 0;
-    cudaError_t e = launchWavefront(ctx->view, false, iteration, paths, npix, ctx->dTot[0], ctx->dTot[1], ctx->dTot[2],
+    cudaError_t e = launchWavefront(ctx->view, ctx->kindMask, iteration, paths, npix, ctx->dTot[0], ctx->dTot[1], ctx->dTot[2],
                                     ctx->dStats, ctx->dWaveGrad, ctx->waveGradCapacity, ctx->waveGrid, ctx->stream,
                                     &launches, &G);
     if (e == cudaSuccess) {
@@ -341,7 +346,7 @@ extern "C" int pg3gpu_diff_adjoint(pg3gpu_ctx *ctx, const float *dLdI, float *gM
     G.adjoint = 1;
     G.sampleOffset = ctx->dSampleOffset;
     uint64_t launches = 0;
-    const cudaError_t e = launchWavefront(ctx->view, false, ctx->diffIteration, paths, npix, ctx->dAdj[0],
+    const cudaError_t e = launchWavefront(ctx->view, ctx->kindMask, ctx->diffIteration, paths, npix, ctx->dAdj[0],
                                           ctx->dAdj[1], ctx->dAdj[2], ctx->dStats, ctx->dWaveGrad,
                                           ctx->waveGradCapacity, ctx->waveGrid, ctx->stream, &launches, &G);
     if (int st = cudaStatus(ctx, e, "adjoint")) return st;

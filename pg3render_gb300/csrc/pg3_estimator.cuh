@@ -32,6 +32,14 @@ PG3_DI float misPower(float a, float b)
     return a2 / (a2 + b2);
 }
 
+// MISWeight2Power with sample counts (src/path_tracer_base.hxx:522-541)
+PG3_DI float misPowerN(float p1, uint32_t n1, float p2, uint32_t n2)
+{
+    const float s1 = n1 * p1, s2 = n2 * p2;
+    const float q1 = s1 * s1, q2 = s2 * s2;
+    return q1 / (q1 + q2) / n1;
+}
+
 // Contribution estimate of the background light (BackgroundLight::EstimateContribution,
 // src/lights.hxx:447-470): a constant background integrates to pi * luminance; for a map the
 // clamped-cosine SH estimate of the irradiance (the steerable sampler's own estimate,
@@ -45,10 +53,22 @@ PG3_DI float bgEstimate(const SceneView &S, float3 n)
     steerCoeffs(n, c);
     return fmaxf(dot9(S.bgShL, c), 0.f);
 }
-// Estimate of light l (area lights first, the background last; src/scene.hxx:948-953).
+// Estimate of light l (area lights first, then point lights, the background last;
+// src/scene.hxx:767-825, 948-953).
 PG3_DI float lightEstimate(const SceneView &S, uint32_t l, float3 pt, float3 n)
 {
-    return (l < S.nArea) ? areaEstimate(S.lights[l], pt, n) : bgEstimate(S, n);
+    return (l < S.nArea) ? tableEstimate(S.lights[l], pt, n) : bgEstimate(S, n);
+}
+
+// Weight of one of nL light samples against nB BSDF samples (AddMISLightSampleContribution,
+// src/path_tracer_base.hxx:350-423): area and background samples are MIS-weighted with the
+// BSDF's pdf of the same direction; a point light's sample is its exact contribution, left to
+// the estimate of the sum over lights (divided by the picking probability and the count).
+PG3_DI float lightSampleWeight(float pdfW, float lprob, uint32_t nL, float bsdfPdf, uint32_t nB)
+{
+    if (pdfW == infF()) return 1.f / (lprob * (float)nL);
+    const float lightPdf = pdfW * lprob;
+    return misPowerN(lightPdf, nL, bsdfPdf, nB) / lightPdf;
 }
 
 // Sum of the lights' contribution estimates at a vertex (src/path_tracer_base.hxx:216-232).
@@ -200,10 +220,11 @@ PG3_DI float3 tracePath(const SceneView &S, uint32_t pixel, uint32_t sample, Pat
 
         const Rand4 ra = draw(S, pixel, sample, pl, 0);
         const Rand4 rb = draw(S, pixel, sample, pl, 1);
-        const float sum = (S.lightCount > 1) ? estimateSum(S, pt, n) : 0.f;
+        const bool lights = takesLightSamples(mat);
+        const float sum = (S.lightCount > 1 && lights) ? estimateSum(S, pt, n) : 0.f;
 
         // light sample with MIS (src/path_tracer.hxx:250-265, src/path_tracer_base.hxx:350-411)
-        if (pl + 1 >= S.minPL) {
+        if (pl + 1 >= S.minPL && lights) {
             int lid;
             float lprob = 0.f;
             pickLight(S, pt, n, sum, ra.a, lid, lprob);
@@ -214,15 +235,14 @@ PG3_DI float3 tracePath(const SceneView &S, uint32_t pixel, uint32_t sample, Pat
                     bgSample(S, frame, ra.b, ra.c, ra.d, wig, pdfW, smp);
                     dist = kFloatMax;
                 } else {
-                    areaSample(S.lights[lid], pt, n, ra.b, ra.c, wig, dist, smp, pdfW);
+                    tableSample(S.lights[lid], pt, n, ra.b, ra.c, wig, dist, smp, pdfW);
                 }
                 if (maxc(smp) > 0.f) {
                     ++pc.shadow;
                     if (!occludedAny(S, pt, wig, dist)) {
                         BsdfRec br;
                         evalBsdf(mat, toLocal(frame, wig), wol, br);
-                        const float lightPdf = pdfW * lprob;
-                        L += beta * (smp * br.att) * (misPower(lightPdf, br.pdfW * br.compProb) / lightPdf);
+                        L += beta * (smp * br.att) * lightSampleWeight(pdfW, lprob, 1u, br.pdfW * br.compProb, 1u);
                     }
                 }
             }
@@ -232,7 +252,7 @@ PG3_DI float3 tracePath(const SceneView &S, uint32_t pixel, uint32_t sample, Pat
         float rrProb = 1.0f;
         bool cut = false;
         if (S.maxPL == 0 || (S.rrMinPL > 0 && pl >= S.rrMinPL)) {
-            rrProb = mat.rrProb;
+            rrProb = rrContinuation(mat, wol);
             cut = rb.a > rrProb;
         }
 
@@ -259,7 +279,7 @@ PG3_DI float3 tracePath(const SceneView &S, uint32_t pixel, uint32_t sample, Pat
     return L;
 }
 
-// Light sample of light `lid` (area: src/lights.hxx:114-131; background: :424-445).
+// Light sample of light `lid` (area: src/lights.hxx:114-131; point: :255-266; background: :424-445).
 PG3_DI void sampleLightAt(const SceneView &S, int lid, float3 pt, const Frame &frame, float3 n, float u0, float u1,
                           float u2, float3 &wig, float &dist, float3 &smp, float &pdfW)
 {
@@ -267,7 +287,7 @@ PG3_DI void sampleLightAt(const SceneView &S, int lid, float3 pt, const Frame &f
         bgSample(S, frame, u0, u1, u2, wig, pdfW, smp);
         dist = kFloatMax;
     } else {
-        areaSample(S.lights[lid], pt, n, u0, u1, wig, dist, smp, pdfW);
+        tableSample(S.lights[lid], pt, n, u0, u1, wig, dist, smp, pdfW);
     }
 }
 
@@ -328,11 +348,12 @@ PG3_DI float3 traceDirect(const SceneView &S, int alg, uint32_t pixel, uint32_t 
     const Frame frame = frameFromZ(n);
     const float3 wol = toLocal(frame, -dir);
     const DevMaterial mat = loadMat(S, matId);
-    const float sum = (S.lightCount > 1) ? estimateSum(S, pt, n) : 0.f;
+    const bool lights = takesLightSamples(mat);
+    const float sum = (S.lightCount > 1 && lights) ? estimateSum(S, pt, n) : 0.f;
     const Rand4 ra = draw(S, pixel, sample, 1, 0);
     const Rand4 rb = draw(S, pixel, sample, 1, 1);
     float3 Lo = f3(0.f);
-    if (alg == 3 || alg == 4) {
+    if ((alg == 3 || alg == 4) && lights) {
         // AddSingleLightSampleContribution (src/path_tracer_base.hxx:315-348)
         const uint32_t count = (alg == 3) ? S.lightCount : 1u;
         for (uint32_t k = 0; k < count; ++k) {
@@ -354,7 +375,8 @@ PG3_DI float3 traceDirect(const SceneView &S, int alg, uint32_t pixel, uint32_t 
             if (!(maxc(smp) > 0.f) || occludedAny(S, pt, wig, dist)) continue;
             BsdfRec br;
             evalBsdf(mat, toLocal(frame, wig), wol, br);
-            Lo += smp * br.att / (pdfW * prob);
+            // a point light's sample is exact: only the picking is estimated (:333-348)
+            Lo += smp * br.att / ((pdfW == infF()) ? prob : pdfW * prob);
         }
     } else if (alg == 2) {
         BsdfRec br;
@@ -367,11 +389,11 @@ PG3_DI float3 traceDirect(const SceneView &S, int alg, uint32_t pixel, uint32_t 
             Lo = (br.pdfW != infF()) ? (br.att * fabsf(br.wil.z) * Li) / (br.pdfW * br.compProb)
                                      : (br.att * Li) / br.compProb;
         }
-    } else {
+    } else if (alg == 5) {
         // kDirectIllumMis: one light sample and one BSDF sample (:99-114)
-        int lid;
+        int lid = -1;
         float lprob = 0.f;
-        pickLight(S, pt, n, sum, ra.a, lid, lprob);
+        if (lights) pickLight(S, pt, n, sum, ra.a, lid, lprob);
         if (lid >= 0) {
             float3 wig, smp;
             float dist, pdfW;
@@ -380,8 +402,7 @@ PG3_DI float3 traceDirect(const SceneView &S, int alg, uint32_t pixel, uint32_t 
             if (maxc(smp) > 0.f && !occludedAny(S, pt, wig, dist)) {   // src/path_tracer_base.hxx:350-411
                 BsdfRec br;
                 evalBsdf(mat, toLocal(frame, wig), wol, br);
-                const float lightPdf = pdfW * lprob;
-                Lo += (smp * br.att) * (misPower(lightPdf, br.pdfW * br.compProb) / lightPdf);
+                Lo += (smp * br.att) * lightSampleWeight(pdfW, lprob, 1u, br.pdfW * br.compProb, 1u);
             }
         }
         BsdfRec br;   // AddDirectIllumMISBrdfSampleContribution (:427-486)
@@ -422,13 +443,6 @@ PG3_DI float3 traceDirect(const SceneView &S, int alg, uint32_t pixel, uint32_t 
 // draws group 2j, BSDF sample i group 2i+1.
 // ------------------------------------------------------------------------------------------
 
-// MISWeight2Power with sample counts (src/path_tracer_base.hxx:522-541)
-PG3_DI float misPowerN(float p1, uint32_t n1, float p2, uint32_t n2)
-{
-    const float s1 = n1 * p1, s2 = n2 * p2;
-    const float q1 = s1 * s1, q2 = s2 * s2;
-    return q1 / (q1 + q2) / n1;
-}
 
 PG3_DI void splittingCounts(const SceneView &S, float budget, uint32_t &nB, uint32_t &nL, float &next)
 {
@@ -447,10 +461,11 @@ PG3_DI void treeVertex(const SceneView &S, TreeFrame *F, float3 pt, float3 n, fl
     splittingCounts(S, budget, nB, nL, next);
     const DevMaterial m = loadMat(S, mat);
     const bool rrActive = S.maxPL == 0 || (S.rrMinPL > 0 && pl >= S.rrMinPL);
-    const float sum = (S.lightCount > 1) ? estimateSum(S, pt, n) : 0.f;
+    const bool lights = takesLightSamples(m);
+    const float sum = (S.lightCount > 1 && lights) ? estimateSum(S, pt, n) : 0.f;
     const Frame frame = frameFromZ(n);
     float3 R = f3(0.f);
-    if (pl + 1 >= S.minPL) {
+    if (pl + 1 >= S.minPL && lights) {
         for (uint32_t j = 0; j < nL; ++j) {
             const Rand4 ra = draw(S, pixel, sample, vid, 2 * j);
             int lid;
@@ -465,14 +480,13 @@ PG3_DI void treeVertex(const SceneView &S, TreeFrame *F, float3 pt, float3 n, fl
             if (occludedAny(S, pt, wig, dist)) continue;
             BsdfRec br;
             evalBsdf(m, toLocal(frame, wig), wol, br);
-            const float lightPdf = pdfW * lprob;
-            R += (smp * br.att) * (misPowerN(lightPdf, nL, br.pdfW * br.compProb, nB) / lightPdf);
+            R += (smp * br.att) * lightSampleWeight(pdfW, lprob, nL, br.pdfW * br.compProb, nB);
         }
     }
     F->pt = pt;
     F->budget = next;
     F->n = n;
-    F->rr = rrActive ? m.rrProb : 1.0f;
+    F->rr = rrActive ? rrContinuation(m, wol) : 1.0f;
     F->wol = wol;
     F->sum = sum;
     F->R = R;
@@ -657,7 +671,7 @@ PG3_DI float3 tracePathNaive(const SceneView &S, uint32_t pixel, uint32_t sample
         const Rand4 rb = draw(S, pixel, sample, pl, 1);
         float rr = 1.0f;
         if (S.maxPL == 0 || (S.rrMinPL > 0 && pl >= S.rrMinPL)) {
-            rr = mat.rrProb;
+            rr = rrContinuation(mat, wol);
             if (rb.a > rr) { ++pc.rr; break; }
         }
         BsdfRec br;

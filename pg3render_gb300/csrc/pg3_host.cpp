@@ -130,7 +130,7 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown environment-map sampler");
     if (sc.num_materials == 0 || !sc.materials) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "scene has no materials");
     if ((sc.num_triangles && !sc.triangles) || (sc.num_spheres && !sc.spheres) ||
-        (sc.num_area_lights && !sc.area_lights))
+        (sc.num_area_lights && !sc.area_lights) || (sc.num_point_lights && !sc.point_lights))
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "NULL array with a nonzero count");
     if (sc.num_triangles + (uint64_t)sc.num_spheres > (1u << 30))
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "too many primitives");
@@ -154,7 +154,7 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         v.height = c.height;
     }
 
-    // materials (src/materials.hxx:262-266, 791-806, 996-1021)
+    // materials (src/materials.hxx:262-266, 366-381, 658-668, 713-727, 791-806, 996-1021)
     v.nmat = sc.num_materials;
     out.mats.resize(sc.num_materials);
     for (uint32_t i = 0; i < sc.num_materials; ++i) {
@@ -179,15 +179,39 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         } else if (m.kind == PG3GPU_MAT_GGX_DIELECTRIC) {
             if (std::fabs(m.ior_outer) >= kTiny) { d.eta = m.ior / m.ior_outer; d.etaInv = m.ior_outer / m.ior; }
             d.rrProb = 0.997f;
+        } else if (m.kind == PG3GPU_MAT_PHONG) {
+            if (!finite3(m.albedo) || !finite3(m.glossy) || m.albedo[0] < 0.f || m.albedo[1] < 0.f ||
+                m.albedo[2] < 0.f || m.glossy[0] < 0.f || m.glossy[1] < 0.f || m.glossy[2] < 0.f)
+                return bad(PG3GPU_ERR_INVALID_ARGUMENT, "Phong reflectances must be finite and non-negative");
+            if (!(m.phong_exponent >= 0.f) || !std::isfinite(m.phong_exponent))
+                return bad(PG3GPU_ERR_INVALID_ARGUMENT, "Phong exponent must be finite and >= 0");
+            d.gr = m.glossy[0]; d.gg = m.glossy[1]; d.gb = m.glossy[2];
+            d.exponent = m.phong_exponent;
+            // the diffuse part of GetRRContinuationProb (:542-570); the glossy part depends on wo
+            d.rrProb = 0.15f * lum(d.r, d.g, d.b) + 0.85f * std::max(d.r, std::max(d.g, d.b));
+            d.zeroRefl = (d.r == 0.f && d.g == 0.f && d.b == 0.f && d.gr == 0.f && d.gg == 0.f && d.gb == 0.f) ? 1 : 0;
+        } else if (m.kind == PG3GPU_MAT_SMOOTH_CONDUCTOR) {
+            d.eta = (std::fabs(m.ior_outer) < kTiny) ? 1.0f : m.ior / m.ior_outer;
+            d.absorb = m.absorb;
+            d.rrProb = 0.997f;   // unused: the roulette probability is the Fresnel reflectance of wo
+        } else if (m.kind == PG3GPU_MAT_SMOOTH_DIELECTRIC) {
+            d.eta = (std::fabs(m.ior_outer) < kTiny) ? 1.0f : m.ior / m.ior_outer;
+            d.etaInv = (std::fabs(m.ior) < kTiny) ? 1.0f : m.ior_outer / m.ior;
+            d.rrProb = 0.997f;
         } else {
             std::snprintf(buf, sizeof buf, "material %u: unknown kind %d", i, m.kind);
             err = buf;
             return PG3GPU_ERR_INVALID_ARGUMENT;
         }
-        if (!(m.alpha >= 0.f) && m.kind != PG3GPU_MAT_LAMBERT)
+        if (!(m.alpha >= 0.f) && (m.kind == PG3GPU_MAT_GGX_CONDUCTOR || m.kind == PG3GPU_MAT_GGX_DIELECTRIC))
             return bad(PG3GPU_ERR_INVALID_ARGUMENT, "GGX roughness must be >= 0");
+        if ((m.kind == PG3GPU_MAT_GGX_CONDUCTOR || m.kind == PG3GPU_MAT_GGX_DIELECTRIC ||
+             m.kind == PG3GPU_MAT_SMOOTH_CONDUCTOR || m.kind == PG3GPU_MAT_SMOOTH_DIELECTRIC) &&
+            !(std::isfinite(m.ior) && std::isfinite(m.ior_outer) && std::isfinite(m.absorb)))
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "indices of refraction and absorbance must be finite");
         d.vndfExact = (o.ggx_sampler == PG3GPU_GGX_VNDF_REFERENCE_FIT) ? 0 : 1;
         out.mats[i] = d;
+        out.kindMask |= 1u << m.kind;
     }
 
     // geometry
@@ -220,9 +244,12 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
     v.ntri = sc.num_triangles;
     v.nsph = sc.num_spheres;
 
-    // lights: area lights keep their order, the background comes last (src/scene.hxx:948-953)
+    // lights: area lights keep their order, point lights follow, the background comes last
+    // (src/scene.hxx:767-825, 948-953)
+    if (sc.num_area_lights + (uint64_t)sc.num_point_lights > (1u << 20))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "too many lights");
     out.mat2light.assign(sc.num_materials, -1);
-    out.lights.resize(sc.num_area_lights);
+    out.lights.resize(sc.num_area_lights + sc.num_point_lights);
     for (uint32_t i = 0; i < sc.num_area_lights; ++i) {
         const pg3gpu_area_light &a = sc.area_lights[i];
         if (a.triangle >= sc.num_triangles) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "area light triangle out of range");
@@ -242,7 +269,20 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
             return bad(PG3GPU_ERR_INVALID_ARGUMENT, "two area lights share one emitting material");
         out.mat2light[t.material] = (int)i;
     }
-    v.nArea = sc.num_area_lights;
+    for (uint32_t i = 0; i < sc.num_point_lights; ++i) {
+        const pg3gpu_point_light &p = sc.point_lights[i];
+        if (!finite3(p.position) || !finite3(p.power))
+            return bad(PG3GPU_ERR_INVALID_ARGUMENT, "point light position and power must be finite");
+        // PointLight::SetPower (src/lights.hxx:244-247): intensity = power / (4 pi)
+        DevAreaLight L;
+        L.p0_invArea = make_float4(p.position[0], p.position[1], p.position[2], -1.f);
+        L.e1_r = make_float4(0.f, 0.f, 0.f, p.power[0] / (4 * kPi));
+        L.e2_g = make_float4(0.f, 0.f, 0.f, p.power[1] / (4 * kPi));
+        L.n_b = make_float4(0.f, 0.f, 0.f, p.power[2] / (4 * kPi));
+        out.lights[sc.num_area_lights + i] = L;
+    }
+    out.numPointLights = sc.num_point_lights;
+    v.nArea = sc.num_area_lights + sc.num_point_lights;
     v.bgKind = sc.background;
     v.lightCount = v.nArea + (sc.background != PG3GPU_BG_NONE ? 1 : 0);
     v.bgLightId = (sc.background != PG3GPU_BG_NONE) ? (int)v.nArea : -1;

@@ -27,6 +27,8 @@ struct HostScene {
     std::vector<float> bgShL;            // 9 SH coefficients of the map's luminance (picking estimate)
     SteerableHost steer;
     bool hasSteer = false;
+    uint32_t kindMask = 0;               // material kinds present (bit per PG3GPU_MAT_* kind)
+    uint32_t numPointLights = 0;
 };
 
 // Returns PG3GPU_OK or an error status with a message in err.

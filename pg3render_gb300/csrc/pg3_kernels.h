@@ -33,9 +33,11 @@ cudaError_t buildLbvh(const SceneView &S, BvhNode *nodes, void *scratch, uint32_
                       uint32_t *sortedIdsOut, cudaStream_t stream);
 
 // pg3_wavefront.cu
-// grad: null renders; otherwise a primal replay (grad->adjoint == 0) or the adjoint pass
+// kindMask: bit k set when the scene has a material of kind k (shade kernels of absent kinds are
+// not launched); grad: null renders; otherwise a primal replay (grad->adjoint == 0) or the
+// adjoint pass
 size_t wavefrontBytes(uint64_t capacity, bool grad);
-cudaError_t launchWavefront(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
+cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch,
                             uint64_t capacity, int gridBlocks, cudaStream_t stream, uint64_t *launches,
                             const GradArgs *grad = nullptr);

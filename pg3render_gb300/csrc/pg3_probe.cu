@@ -49,6 +49,7 @@ __device__ float lightPdfAlong(const SceneView &S, int light, float3 pt, float3 
         return pdf;
     }
     const DevAreaLight &L = S.lights[light];
+    if (isPointLight(L)) return infF();   // a point light is reached by light sampling only
     const float3 p0 = xyz(L.p0_invArea), e1 = xyz(L.e1_r), e2 = xyz(L.e2_g);
     float t = 1e36f;
     const float3 nrmT = normalize(cross(e1, e2));
@@ -72,7 +73,7 @@ __global__ void probeLightKernel(const __grid_constant__ SceneView S, int light,
     float3 wig, smp;
     float pdf = 0.f, dist;
     if (light == S.bgLightId) bgSample(S, f, r.b, r.c, r.d, wig, pdf, smp);
-    else areaSample(S.lights[light], pt, nrm, r.b, r.c, wig, dist, smp, pdf);
+    else tableSample(S.lights[light], pt, nrm, r.b, r.c, wig, dist, smp, pdf);
     dirs[3 * i] = wig.x; dirs[3 * i + 1] = wig.y; dirs[3 * i + 2] = wig.z;
     pdfS[i] = pdf;
     pdfE[i] = lightPdfAlong(S, light, pt, nrm, wig);

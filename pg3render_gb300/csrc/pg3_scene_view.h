@@ -12,27 +12,36 @@
 
 namespace pg3 {
 
-enum : int { kMatLambert = 0, kMatGgxConductor = 1, kMatGgxDielectric = 2 };
+enum : int {
+    kMatLambert = 0, kMatGgxConductor = 1, kMatGgxDielectric = 2,
+    kMatPhong = 3, kMatSmoothConductor = 4, kMatSmoothDielectric = 5, kNumMatKinds = 6
+};
 enum : int { kBgNone = 0, kBgConstant = 1, kBgEnvMap = 2 };
 enum : int { kEmCdf = 0, kEmCosine = 1, kEmSteerable = 2 };
 
-struct DevMaterial {          // 48 bytes
+struct DevMaterial {          // 64 bytes
     int kind;
-    float r, g, b;            // Lambert reflectance
+    float r, g, b;            // Lambert reflectance; Phong diffuse reflectance
     float alpha;              // GGX roughness (already clamped)
     float eta, etaInv;        // inner/outer, outer/inner
     float absorb;             // conductor k
-    float rrProb;             // Russian-roulette continuation probability (clamped to 0.997)
-    int zeroRefl;             // Lambert with zero reflectance: paths end here (lights)
+    float rrProb;             // Russian-roulette continuation probability (clamped to 0.997); Phong: the
+                              // diffuse part of its view-dependent estimate
+    int zeroRefl;             // zero reflectance (IsReflectanceZero): paths end here (lights)
     int vndfExact;            // GGX: exact visible-normal sampling (1) or the reference's fitted routine (0)
     float alphaS;             // GGX roughness the sampling routines and pdfs use (normally == alpha)
+    float gr, gg, gb;         // Phong glossy reflectance
+    float exponent;           // Phong lobe exponent
 };
+static_assert(sizeof(DevMaterial) == 64, "DevMaterial is one 64-byte record");
 
+// One entry of the light table: area lights first, then point lights (the background light is
+// the id after the table).
 struct DevAreaLight {         // 64 bytes; radiance rides in the w lanes
-    float4 p0_invArea;        // p0.xyz, 1/area
-    float4 e1_r;              // edge p1 - p0, radiance r
-    float4 e2_g;              // edge p2 - p0, radiance g
-    float4 n_b;               // frame normal xyz, radiance b
+    float4 p0_invArea;        // p0.xyz, 1/area; a point light: position xyz, -1
+    float4 e1_r;              // edge p1 - p0, radiance r (point light: intensity r)
+    float4 e2_g;              // edge p2 - p0, radiance g (intensity g)
+    float4 n_b;               // frame normal xyz, radiance b (intensity b)
 };
 
 // Linear BVH node (Karras 2012 layout, children as signed ids: >= 0 inner node,
@@ -83,8 +92,8 @@ struct SceneView {
     const int *mat2light;     // material id -> light id or -1
     uint32_t nmat;
     const DevAreaLight *lights;
-    uint32_t nArea;
-    uint32_t lightCount;      // area lights + background
+    uint32_t nArea;           // entries of the light table (area and point lights)
+    uint32_t lightCount;      // light table + background
     int bgKind;
     int bgLightId;
     float3 bgConst;

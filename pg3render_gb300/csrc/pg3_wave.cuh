@@ -32,7 +32,15 @@ namespace pg3 {
 namespace cg = cooperative_groups;
 
 constexpr int kWaveBlock = PG3_WAVE_BLOCK;
-enum : int { kBucketMiss = 0, kBucketLambert = 1, kBucketConductor = 2, kBucketDielectric = 3, kNumBuckets = 4 };
+// Material buckets: one per kind, the two Dirac materials share one (their kernels are short).
+// A shade kernel's K is its kind, kShadeSmooth the shared Dirac bucket, -1 the miss bucket.
+enum : int {
+    kBucketMiss = 0, kBucketLambert = 1, kBucketConductor = 2, kBucketDielectric = 3, kBucketPhong = 4,
+    kBucketSmooth = 5, kNumBuckets = 6
+};
+constexpr int kShadeSmooth = kMatSmoothConductor;
+PG3_DI constexpr int bucketOfShade(int K) { return (K < 0) ? kBucketMiss : 1 + K; }
+PG3_DI int bucketOfKind(int kind) { return min(1 + kind, (int)kBucketSmooth); }
 constexpr uint32_t kFlagFinite = 1u << 16, kFlagRefl = 1u << 17;
 constexpr uint32_t kSlotBits = 24, kSlotMask = (1u << kSlotBits) - 1u;
 constexpr uint32_t kMaxSlots = 1u << kSlotBits;
@@ -234,10 +242,11 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
     if (go && S.maxPL > 0 && pl >= S.maxPL) { ++pc.maxl; go = false; }
     if (go && pl >= kMaxPathLengthHard) { ++pc.safety; go = false; }
     if (!go) return;
+    constexpr bool kLights = K != kShadeSmooth;   // Dirac materials take no light samples
     const Rand4 ra = draw(S, pixel, sample, pl, 0);
     const Rand4 rb = draw(S, pixel, sample, pl, 1);
-    const float sum = (S.lightCount > 1) ? estimateSum(S, pt, nrm) : 0.f;
-    if (pl + 1 >= S.minPL) {
+    const float sum = (kLights && S.lightCount > 1) ? estimateSum(S, pt, nrm) : 0.f;
+    if (kLights && pl + 1 >= S.minPL) {
         int lid;
         float lprob = 0.f;
         pickLight(S, pt, nrm, sum, ra.a, lid, lprob);
@@ -248,14 +257,13 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
                 bgSample<EMK>(S, frame, ra.b, ra.c, ra.d, wig, pdfW, smp);
                 dist = kFloatMax;
             } else {
-                areaSample(S.lights[lid], pt, nrm, ra.b, ra.c, wig, dist, smp, pdfW);
+                tableSample(S.lights[lid], pt, nrm, ra.b, ra.c, wig, dist, smp, pdfW);
             }
             if (maxc(smp) > 0.f) {
                 BsdfRec br;
                 evalBsdfK<K, GRAD>(mat, toLocal(frame, wig), wol, br);
-                const float lightPdf = pdfW * lprob;
-                const float mis = misPower(lightPdf, br.pdfW * br.compProb);
-                const float3 c = beta * (smp * br.att) * (mis / lightPdf);
+                const float w = lightSampleWeight(pdfW, lprob, 1u, br.pdfW * br.compProb, 1u);
+                const float3 c = beta * (smp * br.att) * w;
                 o.shadow = true;
                 o.s0 = make_float4(pt.x, pt.y, pt.z, dist);
                 o.s1 = make_float4(wig.x, wig.y, wig.z, __uint_as_float(tag));
@@ -265,14 +273,14 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
                     o.s4 = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
                     if (adj) {
                         if (K == kMatLambert) {
-                            const float3 g = delta * beta * smp * ((mis / lightPdf) * br.dAtt);
+                            const float3 g = delta * beta * smp * (w * br.dAtt);
                             o.s3 = make_float4(g.x, g.y, g.z, 0.f);
                         } else {
                             o.s3 = make_float4(0.f, 0.f, 0.f, dot(delta, c) * br.dAtt);
                         }
                         float3 e = f3(0.f);
                         if (lid == S.bgLightId && S.bgKind == kBgEnvMap && G.gEm)
-                            e = delta * beta * br.att * (fabsf(dot(wig, nrm)) * mis / lightPdf);
+                            e = delta * beta * br.att * (fabsf(dot(wig, nrm)) * w);
                         o.s4 = make_float4(e.x, e.y, e.z, __int_as_float(matId));
                     }
                 }
@@ -283,12 +291,13 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
     float rrProb = 1.0f;
     bool cut = false;
     if (S.maxPL == 0 || (S.rrMinPL > 0 && pl >= S.rrMinPL)) {
-        rrProb = mat.rrProb;
+        rrProb = rrContinuation<K>(mat, wol);
         cut = rb.a > rrProb;
     }
     // BSDF sample (src/path_tracer.hxx:305-322)
     BsdfRec br;
-    sampleBsdfK<K, GRAD>(mat, wol, rb.b, rb.c, rb.d, br);
+    if (K == kShadeSmooth) sampleBsdfSmooth<GRAD>(mat, wol, rb.d, br);
+    else sampleBsdfK<K, GRAD>(mat, wol, rb.b, rb.c, rb.d, br);
     if (isBlocker(br)) {
         ++pc.blocker;
         return;
@@ -374,18 +383,23 @@ PG3_DI int extendOne(const SceneView &S, const Queues &Q, const float4 *rq, uint
     Q.hit[i] = make_float2(h.t, __int_as_float(h.prim));
     if (!hit) return kBucketMiss;
     const int mat = ((uint32_t)h.prim < S.ntri) ? __ldg(&S.triMat[h.prim]) : __ldg(&S.sphMat[h.prim - S.ntri]);
-    return 1 + __ldg(&S.mats[mat].kind);
+    return bucketOfKind(__ldg(&S.mats[mat].kind));
 }
 
+// Appends queue index i to its bucket (-1: none); all lanes of the warp call this. Lanes of the
+// same bucket are grouped with one match, and each group's leader reserves its slots.
 PG3_DI void bucketAppend(const Queues &Q, int bucket, uint32_t i)
 {
-#pragma unroll
-    for (int b = 0; b < kNumBuckets; ++b) {
-        const uint32_t pos = warpAppend(&Q.cnt->bucket[b], bucket == b);
-        if (bucket == b) {
-            if (pos < Q.cap) Q.bucket[b][pos] = i;
-            else atomicOr(Q.err, kErrQueueOverflow);
-        }
+    const unsigned peers = __match_any_sync(0xffffffffu, bucket);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (bucket >= 0 && lane == leader) base = atomicAdd(&Q.cnt->bucket[bucket], (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (bucket >= 0) {
+        const uint32_t pos = base + __popc(peers & ((1u << lane) - 1u));
+        if (pos < Q.cap) Q.bucket[bucket][pos] = i;
+        else atomicOr(Q.err, kErrQueueOverflow);
     }
 }
 

@@ -5,9 +5,11 @@
 //   raygen            camera rays of all slots -> ray queue A; path state init
 //   per bounce:
 //     extend          closest hit of every queued ray; the ray's queue index is
-//                     appended to one of four buckets (miss, Lambert, GGX
-//                     conductor, GGX dielectric) with warp-aggregated atomics
-//     shade<kind>     one kernel per bucket: emitter MIS, light sample (the BSDF
+//                     appended to one of six buckets (miss, Lambert, GGX
+//                     conductor, GGX dielectric, Phong, smooth conductor or
+//                     dielectric) with warp-aggregated atomics
+//     shade<kind>     one kernel per bucket (kinds the scene has): emitter MIS,
+//                     light sample (the BSDF
 //                     value and MIS weight are folded into a shadow record),
 //                     Russian roulette, BSDF sample -> next ray queue
 //     shadow          any-hit test of every shadow record; unoccluded records
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
     extern __shared__ float sGrad[];
     initBlockGrad<GRAD>(sGrad, S.nmat);
     sample0 = sampleBase<GRAD>(sample0, G);
-    constexpr int kBucket = (K < 0) ? kBucketMiss : 1 + K;
+    constexpr int kBucket = bucketOfShade(K);
     const uint32_t n = Q.cnt->bucket[kBucket];
     const float4 *rq = Q.ray[cur];
     PathCounters pc;
@@ -189,20 +191,40 @@ Queues carve(void *scratch, uint64_t cap, bool grad)
     return q;
 }
 
-// The four shade kernels of one bounce, specialised on the environment-map sampler.
+// The shade kernels of one bounce (the miss bucket and the material kinds of the scene),
+// specialised on the environment-map sampler. Returns the number of launches.
 template <int EMK, bool GRAD>
-void launchShade(const SceneView &S, const Queues &Q, int cur, uint32_t base, uint32_t npix, uint32_t sample0,
-                 float *r, float *g, float *b, DevStats *stats, int grid, size_t smem, const GradArgs &G,
-                 cudaStream_t st)
+int launchShade(const SceneView &S, uint32_t kindMask, const Queues &Q, int cur, uint32_t base, uint32_t npix,
+                uint32_t sample0, float *r, float *g, float *b, DevStats *stats, int grid, size_t smem,
+                const GradArgs &G, cudaStream_t st)
 {
+    int n = 1;
     shadeKernel<-1, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-    shadeKernel<kMatLambert, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-    shadeKernel<kMatGgxConductor, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-    shadeKernel<kMatGgxDielectric, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+    if (kindMask & (1u << kMatLambert)) {
+        shadeKernel<kMatLambert, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+        ++n;
+    }
+    if (kindMask & (1u << kMatGgxConductor)) {
+        shadeKernel<kMatGgxConductor, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+        ++n;
+    }
+    if (kindMask & (1u << kMatGgxDielectric)) {
+        shadeKernel<kMatGgxDielectric, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+        ++n;
+    }
+    if (kindMask & (1u << kMatPhong)) {
+        shadeKernel<kMatPhong, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+        ++n;
+    }
+    if (kindMask & ((1u << kMatSmoothConductor) | (1u << kMatSmoothDielectric))) {
+        shadeKernel<kShadeSmooth, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+        ++n;
+    }
+    return n;
 }
 
 template <bool GRAD>
-cudaError_t runWavefront(const SceneView &S, uint32_t sample0, uint64_t numPaths, uint32_t npix, float *outR,
+cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix, float *outR,
                          float *outG, float *outB, DevStats *stats, void *scratch, uint64_t capacity, int gridBlocks,
                          cudaStream_t stream, uint64_t *launches, const GradArgs &G0)
 {
@@ -230,13 +252,16 @@ cudaError_t runWavefront(const SceneView &S, uint32_t sample0, uint64_t numPaths
             extendKernel<<<gridBlocks, kWaveBlock, 0, stream>>>(S, Q, cur, stats);
             const int emk = (S.bgKind == kBgEnvMap) ? S.emSampler : kEmCosine;   // no map: constant/area paths
             const uint32_t b32 = (uint32_t)base;
-            if (emk == kEmCdf) launchShade<kEmCdf, GRAD>(S, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
+            int shades;
+            if (emk == kEmCdf)
+                shades = launchShade<kEmCdf, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
             else if (emk == kEmSteerable)
-                launchShade<kEmSteerable, GRAD>(S, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
-            else launchShade<kEmCosine, GRAD>(S, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
+                shades = launchShade<kEmSteerable, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
+            else
+                shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
             shadowKernel<GRAD><<<gridBlocks, kWaveBlock, smem, stream>>>(S, Q, r, g, b, stats, G);
             advanceKernel<<<1, 1, 0, stream>>>(Q.cnt, cur);
-            *launches += 7;
+            *launches += 3 + shades;
             if (S.maxPL == 0 && (bounce & 7) == 7 && capturing == cudaStreamCaptureStatusNone) {
                 // roulette-ended paths: stop once the queue is empty (checked every 8 bounces)
                 uint32_t left = 0;
@@ -257,18 +282,17 @@ size_t wavefrontBytes(uint64_t cap, bool grad)
            3 * align256(16 * cap) + align256((grad ? 80 : 48) * cap) + (grad ? align256(8 * cap) : 0);
 }
 
-cudaError_t launchWavefront(const SceneView &S, bool naive, uint32_t sample0, uint64_t numPaths, uint32_t npix,
+cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch, uint64_t capacity,
                             int gridBlocks, cudaStream_t stream, uint64_t *launches, const GradArgs *grad)
 {
-    if (naive) return cudaErrorNotSupported;   // the BSDF-only tracer runs as a megakernel
     if (capacity > kMaxSlots || numPaths > 0xffffffffull) return cudaErrorInvalidValue;
     if (grad)
-        return runWavefront<true>(S, sample0, numPaths, npix, outR, outG, outB, stats, scratch, capacity, gridBlocks,
-                                  stream, launches, *grad);
+        return runWavefront<true>(S, kindMask, sample0, numPaths, npix, outR, outG, outB, stats, scratch, capacity,
+                                  gridBlocks, stream, launches, *grad);
     GradArgs none{};
-    return runWavefront<false>(S, sample0, numPaths, npix, outR, outG, outB, stats, scratch, capacity, gridBlocks,
-                               stream, launches, none);
+    return runWavefront<false>(S, kindMask, sample0, numPaths, npix, outR, outG, outB, stats, scratch, capacity,
+                               gridBlocks, stream, launches, none);
 }
 
 }  // namespace pg3

@@ -30,22 +30,43 @@ Vec3 = Tuple[float, float, float]
 MAT_LAMBERT = 0
 MAT_GGX_CONDUCTOR = 1
 MAT_GGX_DIELECTRIC = 2
+MAT_PHONG = 3
+MAT_SMOOTH_CONDUCTOR = 4
+MAT_SMOOTH_DIELECTRIC = 5
 
 # Copper IOR and absorbance at ~590 nm, and the IOR of air, as the reference
 # defines them (src/materials.hxx:22-27).
 AIR_IOR = 1.000277
+GLASS_IOR = 1.51
 COPPER_IOR = 0.468
 COPPER_ABSORB = 2.81
+SILVER_IOR = 0.121
+SILVER_ABSORB = 3.66
+GOLD_IOR = 0.236
+GOLD_ABSORB = 2.960089
 
 
 @dataclasses.dataclass
 class Material:
     kind: int
-    albedo: Vec3 = (0.0, 0.0, 0.0)     # Lambert reflectance
+    albedo: Vec3 = (0.0, 0.0, 0.0)     # Lambert reflectance; Phong diffuse reflectance (as held)
     alpha: float = 0.1                 # GGX roughness (clamped to [0.001, 1] by the renderer)
     ior: float = 1.5                   # inner IOR
     ior_outer: float = 1.0             # outer IOR
     absorb: float = 0.0                # conductor k
+    glossy: Vec3 = (0.0, 0.0, 0.0)     # Phong glossy reflectance
+    phong_exponent: float = 1.0        # Phong lobe exponent
+
+
+def phong(diffuse: Vec3, glossy: Vec3, exponent: float, use_diffuse: bool = True, use_glossy: bool = True) -> Material:
+    """PhongMaterial(aDiffuseReflectance, aGlossyReflectance, aPhongExponent, aDiffuse, aGlossy)
+    (src/materials.hxx:366-381): a disabled component is zero, and the diffuse part is halved
+    when the glossy lobe is on."""
+    d = tuple(float(x) for x in diffuse) if use_diffuse else (0.0, 0.0, 0.0)
+    g = tuple(float(x) for x in glossy) if use_glossy else (0.0, 0.0, 0.0)
+    if use_glossy:
+        d = tuple(x / 2.0 for x in d)   # (equal to halving the float32 value: the ABI stores float32)
+    return Material(MAT_PHONG, albedo=d, glossy=g, phong_exponent=float(exponent))
 
 
 @dataclasses.dataclass
@@ -68,6 +89,8 @@ class Scene:
     spheres: List[Tuple[Vec3, float, int]] = dataclasses.field(default_factory=list)
     # (triangle index, radiance rgb); the triangle's material is the light's emitter
     area_lights: List[Tuple[int, Vec3]] = dataclasses.field(default_factory=list)
+    # (position, power rgb): point lights, light ids after the area lights
+    point_lights: List[Tuple[Vec3, Vec3]] = dataclasses.field(default_factory=list)
     background_const: Optional[Vec3] = None
     env_map: Optional[np.ndarray] = None   # float32 [H, W, 3], row 0 = theta 0 (+z)
     name: str = "scene"
@@ -92,7 +115,7 @@ class Scene:
 
     @property
     def num_lights(self) -> int:
-        return len(self.area_lights) + (1 if self.has_background else 0)
+        return len(self.area_lights) + len(self.point_lights) + (1 if self.has_background else 0)
 
     @property
     def has_background(self) -> bool:
@@ -113,6 +136,12 @@ class Scene:
                 out.append("ggx_conductor %r %r %r %r" % (m.alpha, m.ior, m.ior_outer, m.absorb))
             elif m.kind == MAT_GGX_DIELECTRIC:
                 out.append("ggx_dielectric %r %r %r" % (m.alpha, m.ior, m.ior_outer))
+            elif m.kind == MAT_PHONG:
+                out.append("phong %r %r %r %r %r %r %r" % (*m.albedo, *m.glossy, m.phong_exponent))
+            elif m.kind == MAT_SMOOTH_CONDUCTOR:
+                out.append("smooth_conductor %r %r %r" % (m.ior, m.ior_outer, m.absorb))
+            elif m.kind == MAT_SMOOTH_DIELECTRIC:
+                out.append("smooth_dielectric %r %r" % (m.ior, m.ior_outer))
             else:
                 raise ValueError("unknown material kind %d" % m.kind)
         light_of = {ti: rad for ti, rad in self.area_lights}
@@ -124,6 +153,8 @@ class Scene:
                 out.append("triangle %s %d" % (coords, mat))
         for (cc, r, mat) in self.spheres:
             out.append("sphere %r %r %r %r %d" % (*cc, r, mat))
+        for (pos, power) in self.point_lights:
+            out.append("point_light %r %r %r %r %r %r" % (*pos, *power))
         if self.env_map is not None:
             if em_path is None:
                 raise ValueError("environment map scenes need em_path")
@@ -301,6 +332,51 @@ def cornell_box_bg(width: int = 256, height: int = 256, background=(0.4, 0.5, 0.
     s = cornell_box(width, height)
     s.name = "cornell_areabg_%dx%d" % (width, height)
     s.background_const = tuple(background)
+    return s
+
+
+def _mixed_materials_box(s: Scene, ceiling: bool) -> None:
+    # Phong walls: the box's reflectances as the diffuse part (halved by the glossy lobe) and a
+    # grey glossy lobe of 0.5, exponent 90, like the reference's glossy-walls box
+    mw = s.add_material(phong(WHITE, (0.5, 0.5, 0.5), 90))
+    ml = s.add_material(phong(RED, (0.5, 0.5, 0.5), 90))
+    mr = s.add_material(phong(GREEN, (0.5, 0.5, 0.5), 90))
+    s.add_quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), mw, (0, 0, 1))
+    if ceiling:
+        s.add_quad((-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1), mw, (0, 0, -1))
+    s.add_quad((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), mw, (0, -1, 0))
+    s.add_quad((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), ml, (1, 0, 0))
+    s.add_quad((1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1), mr, (-1, 0, 0))
+    m_phong = s.add_material(phong((0.803922, 0.803922, 0.152941), (0.7, 0.7, 0.7), 200))
+    m_metal = s.add_material(Material(MAT_SMOOTH_CONDUCTOR, ior=COPPER_IOR, ior_outer=AIR_IOR, absorb=COPPER_ABSORB))
+    m_glass = s.add_material(Material(MAT_SMOOTH_DIELECTRIC, ior=GLASS_IOR, ior_outer=AIR_IOR))
+    s.spheres.append(((-0.45, 0.25, -0.65), 0.35, m_phong))
+    s.spheres.append(((0.45, -0.25, -0.65), 0.35, m_metal))
+    s.spheres.append(((-0.35, -0.5, -0.75), 0.25, m_glass))
+
+
+def cornell_mixed(width: int = 256, height: int = 256, area: bool = True, point: bool = True) -> Scene:
+    """The closed box with the reference's other materials and a point light: Phong walls
+    (diffuse + grey glossy 0.5, exponent 90), a Phong sphere (yellow diffuse, glossy 0.7, exponent
+    200), a smooth copper sphere and a smooth glass sphere (IOR 1.51 in air), lit by the ceiling
+    quad light and/or a 20 W point light under the ceiling."""
+    s = Scene(_camera_for_box(width, height),
+              name="cornell_mixed%s%s_%dx%d" % ("_area" if area else "", "_point" if point else "", width, height))
+    _mixed_materials_box(s, ceiling=True)
+    if area:
+        _ceiling_light(s)
+    if point:
+        s.point_lights.append(((0.0, 0.0, 0.6), (20.0, 20.0, 20.0)))
+    return s
+
+
+def cornell_env_mixed(width: int = 256, height: int = 256, em_width: int = 512, em_height: int = 256,
+                      em_seed: int = 7) -> Scene:
+    """cornell_mixed with the ceiling removed, lit by the synthetic sky and the point light."""
+    s = Scene(_camera_for_box(width, height), name="cornell_envmixed_%dx%d_em%dx%d" % (width, height, em_width, em_height))
+    _mixed_materials_box(s, ceiling=False)
+    s.point_lights.append(((0.0, 0.0, 0.6), (20.0, 20.0, 20.0)))
+    s.env_map = synthetic_sky(em_width, em_height, seed=em_seed)
     return s
 
 

@@ -41,7 +41,13 @@ def scene_from_golden(d):
     from pg3render_gb300 import scene as S
     text = str(d["scene_text"])
     name = text.splitlines()[0][2:].strip()
-    if name.startswith("cornell_area_"):
+    if name.startswith("cornell_mixed_area_point_"):
+        s = S.cornell_mixed(32, 32)
+    elif name.startswith("cornell_mixed_point_"):
+        s = S.cornell_mixed(32, 32, area=False)
+    elif name.startswith("cornell_envmixed_"):
+        s = S.cornell_env_mixed(32, 32, 64, 32)
+    elif name.startswith("cornell_area_"):
         s = S.cornell_box(32, 32)
     elif name.startswith("cornell_areabg_"):
         s = S.cornell_box_bg(32, 32)

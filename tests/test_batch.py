@@ -91,6 +91,22 @@ def test_batch_matches_single_scene_contexts(use_graph):
 
 
 @pytest.mark.gpu
+def test_batch_with_phong_smooth_materials_and_point_lights():
+    # instances of different material kinds: the batch launches the shade kernels of every kind
+    # that any instance holds (Phong, the smooth pair) next to the Lambert/GGX ones
+    cfgs, spps = _variants(2, base_seed=500)
+    cfgs.append(P.Config(scene=S.cornell_mixed(20, 20), max_path_length=0, base_seed=11))
+    cfgs.append(P.Config(scene=S.cornell_mixed(24, 16, area=False), max_path_length=8, base_seed=12))
+    spps += [3, 4]
+    refs = _reference_images(cfgs, spps)
+    with P.GpuBatch(cfgs, spps) as b:
+        b.run()
+        b.synchronize()
+        for i in range(len(cfgs)):
+            _assert_same(b.framebuffer(i, with_variance=True), refs[i])
+
+
+@pytest.mark.gpu
 def test_batch_slot_reuse_with_tiny_capacity():
     # 1024 slots for tens of thousands of paths: every slot is refilled many times and
     # instances of different sizes share the slots within one step

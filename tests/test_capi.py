@@ -95,6 +95,38 @@ def test_scene_validation():
     assert _create(s)[0] == _lib.ERR_INVALID_ARGUMENT
 
 
+def test_phong_smooth_and_point_light_validation():
+    s = S.cornell_mixed(8, 8)
+    st, err = _create(s)
+    assert st == _lib.ERR_CUDA and "device" in err           # valid (no GPU here)
+    for kind, field, value, msg in [(S.MAT_PHONG, "phong_exponent", -1.0, "exponent"),
+                                    (S.MAT_PHONG, "glossy", (0.1, -0.2, 0.1), "Phong reflectances"),
+                                    (S.MAT_PHONG, "albedo", (np.inf, 0.2, 0.1), "Phong reflectances"),
+                                    (S.MAT_SMOOTH_DIELECTRIC, "ior", np.nan, "refraction")]:
+        s = S.cornell_mixed(8, 8)
+        i = next(k for k, m in enumerate(s.materials) if m.kind == kind)
+        setattr(s.materials[i], field, value)
+        st, err = _create(s)
+        assert st == _lib.ERR_INVALID_ARGUMENT and msg in err, (field, st, err)
+    s = S.cornell_mixed(8, 8)
+    s.point_lights[0] = ((0.0, np.nan, 0.5), (1.0, 1.0, 1.0))
+    st, err = _create(s)
+    assert st == _lib.ERR_INVALID_ARGUMENT and "point light" in err
+    s = S.cornell_mixed(8, 8)
+    s.materials[0].kind = 6
+    st, err = _create(s)
+    assert st == _lib.ERR_INVALID_ARGUMENT and "unknown kind" in err
+
+
+def test_phong_constructor_halves_diffuse_with_glossy_lobe():
+    m = S.phong((0.8, 0.6, 0.4), (0.5, 0.5, 0.5), 90)
+    assert m.albedo == (0.4, 0.3, 0.2) and m.glossy == (0.5, 0.5, 0.5) and m.phong_exponent == 90
+    m = S.phong((0.8, 0.6, 0.4), (0.5, 0.5, 0.5), 90, use_glossy=False)
+    assert m.albedo == (0.8, 0.6, 0.4) and m.glossy == (0.0, 0.0, 0.0)
+    s = S.cornell_mixed(8, 8)
+    assert s.num_lights == 3 and "point_light 0.0 0.0 0.6 20.0 20.0 20.0" in s.to_text()
+
+
 def test_null_arguments():
     L = _lib.load()
     h = ctypes.c_void_p()

@@ -21,7 +21,10 @@ GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr"
                 "cornell_area_32_dbs", "cornell_area_32_dlsa", "cornell_area_32_dlss", "cornell_area_32_dmis",
                 "cornell_env_32_dmis_cdf", "cornell_env_32_dbs", "cornell_area_32_el", "cornell_area_32_nv",
                 "cornell_area_32_sb4_iic16", "cornell_env_32_sb4_iic16", "cornell_area_32_sb3_lvl05_r2",
-                "cornell_envarea_32_cdf", "cornell_envarea_32_dmis", "cornell_areabg_32"]
+                "cornell_envarea_32_cdf", "cornell_envarea_32_dmis", "cornell_areabg_32",
+                "cornell_mixed_32", "cornell_mixed_32_rr", "cornell_mixed_32_point", "cornell_mixed_32_naive",
+                "cornell_mixed_32_dmis", "cornell_mixed_32_dlsa", "cornell_mixed_32_dlss", "cornell_mixed_32_dbs",
+                "cornell_mixed_32_sb4_iic16", "cornell_envmixed_32_cdf"]
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
 # the reference's acronyms of its algorithm ids (src/config.hxx:147-170)
 ALG_IDS = {"el": 0, "nv": 1, "dbs": 2, "dlsa": 3, "dlss": 4, "dmis": 5, "ptn": 6, "pt": 7}
@@ -121,6 +124,61 @@ def test_path_by_path_vs_oracle(case, tmp_path):
     assert frac >= MIN_MATCH, "only %.4f of samples match the oracle" % frac
     # the sample means agree much tighter than the per-pixel noise
     assert np.allclose(g.mean(axis=(0, 1, 2)), o.mean(axis=(0, 1, 2)), rtol=2e-2)
+
+
+# (algorithm, max path length, splitting, scene variant, pipeline)
+MIXED_CASES = {
+    "pt": ("pt", 8, None, "mixed", P.renderer.PIPELINE_WAVEFRONT),
+    "pt_megakernel": ("pt", 8, None, "mixed", P.renderer.PIPELINE_MEGAKERNEL),
+    "rr": ("pt", 0, None, "mixed", P.renderer.PIPELINE_WAVEFRONT),
+    "point_only": ("pt", 8, None, "point", P.renderer.PIPELINE_WAVEFRONT),
+    "naive": ("ptn", 8, None, "mixed", P.renderer.PIPELINE_AUTO),
+    "dbs": ("dbs", 8, None, "mixed", P.renderer.PIPELINE_AUTO),
+    "dlsa": ("dlsa", 8, None, "mixed", P.renderer.PIPELINE_AUTO),
+    "dlss": ("dlss", 8, None, "mixed", P.renderer.PIPELINE_AUTO),
+    "dmis": ("dmis", 8, None, "mixed", P.renderer.PIPELINE_AUTO),
+    "sb4_iic16": ("pt", 0, (4, 1.0, 1.0, 16.0), "mixed", P.renderer.PIPELINE_AUTO),
+    "env": ("pt", 12, None, "env", P.renderer.PIPELINE_WAVEFRONT),
+    "env_steerable": ("pt", 12, None, "env", P.renderer.PIPELINE_WAVEFRONT),
+}
+
+
+@pytest.mark.parametrize("case", list(MIXED_CASES))
+def test_mixed_materials_and_point_light_path_by_path(case, tmp_path):
+    """Phong, smooth conductor and smooth dielectric materials and a point light, through every
+    estimator and both pipelines, against the oracle sample by sample."""
+    alg_name, maxpl, split, variant, pipeline = MIXED_CASES[case]
+    if variant == "env":
+        scene = S.cornell_env_mixed(24, 24, 64, 32)
+    else:
+        scene = S.cornell_mixed(24, 24, area=(variant == "mixed"))
+    em = str(tmp_path / "em.bin")
+    if scene.env_map is not None:
+        scene.write_env_map(em)
+    text = scene.to_text(em_path=em, algorithm=alg_name, max_path_length=maxpl, splitting=split)
+    alg = ALG_IDS[alg_name]
+    sampler = P.renderer.EM_STEERABLE if case == "env_steerable" else P.renderer.EM_CDF
+    kw = {}
+    if split is not None:
+        kw = dict(splitting_budget=split[0], splitting_level=split[1], light_to_bsdf_ratio=split[2],
+                  indirect_illum_clipping=split[3])
+    seed = 53
+    with P.GpuPathTracer(_cfg(scene, maxpl, alg, sampler, pipeline=pipeline, **kw), seed=seed) as r:
+        g = r.render_samples(alg, 0, 8)
+    if case == "env_steerable":
+        # the oracle has no steerable sampler: the image means of the two samplers agree within
+        # their standard errors
+        o = _oracle_samples(scene, text, 256, seed, 0).reshape(-1, 3).astype(np.float64)
+        with P.GpuPathTracer(_cfg(scene, maxpl, alg, sampler, pipeline=pipeline), seed=seed) as r:
+            g = r.render_samples(alg, 0, 1024).reshape(-1, 3).astype(np.float64)
+        assert np.isfinite(g).all()
+        se = np.sqrt(g.var(axis=0) / len(g) + o.var(axis=0) / len(o))
+        assert np.all(np.abs(g.mean(axis=0) - o.mean(axis=0)) <= 5 * se), (g.mean(axis=0), o.mean(axis=0), se)
+        return
+    o = _oracle_samples(scene, text, 8, seed, 0)
+    frac = _match_fraction(g, o)
+    assert frac >= MIN_MATCH, "only %.4f of samples match the oracle" % frac
+    assert np.isfinite(g).all() and g.max() > 0
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)

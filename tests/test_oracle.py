@@ -21,7 +21,10 @@ GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr"
                 "cornell_area_32_dbs", "cornell_area_32_dlsa", "cornell_area_32_dlss", "cornell_area_32_dmis",
                 "cornell_env_32_dmis_cdf", "cornell_env_32_dbs", "cornell_area_32_el", "cornell_area_32_nv",
                 "cornell_area_32_sb4_iic16", "cornell_env_32_sb4_iic16", "cornell_area_32_sb3_lvl05_r2",
-                "cornell_envarea_32_cdf", "cornell_envarea_32_dmis", "cornell_areabg_32"]
+                "cornell_envarea_32_cdf", "cornell_envarea_32_dmis", "cornell_areabg_32",
+                "cornell_mixed_32", "cornell_mixed_32_rr", "cornell_mixed_32_point", "cornell_mixed_32_naive",
+                "cornell_mixed_32_dmis", "cornell_mixed_32_dlsa", "cornell_mixed_32_dlss", "cornell_mixed_32_dbs",
+                "cornell_mixed_32_sb4_iic16", "cornell_envmixed_32_cdf"]
 # the visualisers are deterministic inside a surface (zero variance): only the fraction of
 # |z| <= 4 is a meaningful statistic for them
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
@@ -44,7 +47,10 @@ def test_oracle_matches_reference_golden(name):
     # sky with 1e4 suns, are heavy-tailed: their sample variances need more samples before
     # the z-test is calibrated
     spp = {"cornell_area_32_naive": 8192, "cornell_env_32_cos": 16384, "cornell_area_32_dbs": 8192,
-           "cornell_env_32_dbs": 8192}.get(name, 1024)
+           "cornell_env_32_dbs": 8192, "cornell_mixed_32_naive": 8192, "cornell_mixed_32_dbs": 8192,
+           # glossy Phong lobes lit by a point light, caustics through smooth glass: heavy tails
+           "cornell_mixed_32": 8192, "cornell_mixed_32_rr": 8192, "cornell_mixed_32_point": 8192,
+           "cornell_envmixed_32_cdf": 8192}.get(name, 1024)
     o = O.render(text, 32, 32, seed=99, spp=spp, em_sampler=sampler)
     m = o["sum"] / spp
     v = np.maximum(o["sumsq"] / spp - m * m, 0.0) / spp
