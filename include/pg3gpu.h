@@ -304,12 +304,12 @@ int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t it
  * CUDA graph together with the caller's loss and optimiser. */
 #define PG3GPU_PARAMS_DEVICE 1u          /* pointers are device memory (else host memory) */
 #define PG3GPU_PARAMS_KEEP_SAMPLING 2u   /* keep the sampling data (roulette probabilities, GGX sampling
-                                            roughness, environment-map CDF) of the current parameters */
+                                            roughness, environment-map sampler tables) of the current
+                                            parameters */
 /* Replaces the parameters; either pointer may be NULL. Clamps albedo to >= 0, alpha to
  * [0.001, 1] and texels to >= 0. Unless KEEP_SAMPLING, the sampling data follow the new
- * values: the environment-map CDF is rebuilt on the device (CDF and cosine samplers; the
- * steerable sampler's tables are built on the host at create time, so it needs KEEP_SAMPLING
- * when texels change). */
+ * values: the environment-map CDF and the steerable sampler's weights are rebuilt on the
+ * device. */
 int pg3gpu_set_params(pg3gpu_ctx *ctx, const float *material_params, const float *env_texels, uint32_t flags);
 /* Current parameters into host arrays (either may be NULL). */
 int pg3gpu_get_params(pg3gpu_ctx *ctx, float *material_params, float *env_texels);

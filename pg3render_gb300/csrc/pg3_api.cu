@@ -282,31 +282,52 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
     if ((st = upload(ctx, (float **)&v.emCond, hs.emCond))) return bail(st);
     if ((st = upload(ctx, (float **)&v.bgShL, hs.bgShL))) return bail(st);
     if (hs.hasSteer) {
+        // geometry from the shared host build; the map-dependent weights are built on the device
+        const SteerGeom &g = *hs.steer;
         SteerView &sv = v.steer;
-        if ((st = upload(ctx, (float4 **)&sv.vdir, hs.steer.vdir))) return bail(st);
-        if ((st = upload(ctx, (float **)&sv.vw, hs.steer.vw))) return bail(st);
-        if ((st = upload(ctx, (int4 **)&sv.tri, hs.steer.tri))) return bail(st);
-        if ((st = upload(ctx, (float **)&sv.nodeW, hs.steer.nodeW))) return bail(st);
-        if ((st = upload(ctx, (int **)&sv.nodeChild, hs.steer.nodeChild))) return bail(st);
+        if ((st = upload(ctx, (float4 **)&sv.vdir, g.vdir))) return bail(st);
+        if ((st = upload(ctx, (int4 **)&sv.tri, g.tri))) return bail(st);
+        if ((st = upload(ctx, (int **)&sv.nodeChild, g.nodeChild))) return bail(st);
         // leaf planes, then (pg3_steer.cuh) edge normals, leaf-locator cells, whole-sphere weights
-        std::vector<float4> aux = hs.steer.leafPlane;
-        aux.insert(aux.end(), hs.steer.leafEdge.begin(), hs.steer.leafEdge.end());
-        for (const uint4 &c : hs.steer.leafCells) {
+        std::vector<float4> aux = g.leafPlane;
+        aux.insert(aux.end(), g.leafEdge.begin(), g.leafEdge.end());
+        for (const uint4 &c : g.leafCells) {
             float4 f;
             std::memcpy(&f, &c, sizeof f);
             aux.push_back(f);
         }
-        for (int k = 0; k < 9; k += 4)
-            aux.push_back(make_float4(hs.steer.rootW[k], k + 1 < 9 ? hs.steer.rootW[k + 1] : 0.f,
-                                      k + 2 < 9 ? hs.steer.rootW[k + 2] : 0.f, k + 3 < 9 ? hs.steer.rootW[k + 3] : 0.f));
-        if (hs.steer.leafPlane.size() != (20ull << (2 * hs.steer.level)) ||
-            hs.steer.leafGrid != (4u << hs.steer.level))
-            return bail(fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: unexpected leaf count or grid"));
+        const size_t rootAt = aux.size();
+        aux.resize(rootAt + 3, make_float4(0.f, 0.f, 0.f, 0.f));
+        if (g.leafPlane.size() != (20ull << (2 * g.level)) || g.leafGrid != (4u << g.level) ||
+            g.layerStart.size() < 2 || g.layerStart.size() > kSteerMaxLayers + 1)
+            return bail(fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: unexpected leaf count, grid or tree depth"));
         if ((st = upload(ctx, (float4 **)&sv.leafPlane, aux))) return bail(st);
-        if ((st = upload(ctx, (int4 **)&sv.faceCells, hs.steer.faceCells))) return bail(st);
-        sv.level = hs.steer.level;
-        for (size_t l = 0; l < hs.steer.levelOffset.size() && l < 8; ++l) sv.levelOff[l] = hs.steer.levelOffset[l];
-        sv.root = hs.steer.root;
+        if ((st = upload(ctx, (int4 **)&sv.faceCells, g.faceCells))) return bail(st);
+        sv.level = g.level;
+        for (size_t l = 0; l < g.levelOffset.size() && l < 8; ++l) sv.levelOff[l] = g.levelOffset[l];
+        sv.root = g.root;
+        SteerWeightArgs &a = ctx->steerArgs;
+        a.em = v.em;
+        a.emW = v.emW;
+        a.emH = v.emH;
+        a.vdir = sv.vdir;
+        a.numVertices = (uint32_t)g.vdir.size();
+        a.leafTri = sv.tri + g.levelOffset[g.level];
+        a.numLeaves = g.numLeaves();
+        if ((st = upload(ctx, (float **)&a.leafArea, g.leafArea))) return bail(st);
+        a.nodeChild = sv.nodeChild;
+        a.numLayers = (uint32_t)g.layerStart.size() - 1;
+        for (uint32_t l = 0; l <= a.numLayers; ++l) a.layerStart[l] = g.layerStart[l];
+        if ((st = devAlloc(ctx, &a.vw, 9 * (size_t)a.numVertices))) return bail(st);
+        if ((st = devAlloc(ctx, &a.leafW, 9 * (size_t)a.numLeaves))) return bail(st);
+        if ((st = devAlloc(ctx, &a.nodeW, 54 * (size_t)g.numNodes()))) return bail(st);
+        a.rootW = reinterpret_cast<float *>(const_cast<float4 *>(sv.leafPlane) + rootAt);
+        sv.vw = a.vw;
+        sv.nodeW = a.nodeW;
+        v.bgShL = a.rootW;   // the background's picking estimate: the sampler's whole integral
+        const cudaError_t e = launchSteerWeights(a, nullptr);
+        if (e != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "steerable build: %s", cudaGetErrorString(e)));
+        ctx->hasSteer = true;
     }
     if ((st = devAlloc(ctx, &ctx->dErr, 1))) return bail(st);
     if (cudaMemset(ctx->dErr, 0, sizeof(unsigned int)) != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "memset"));

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/pg3gpu.h"
+#include "pg3_kernels.h"
 #include "pg3_scene_view.h"
 
 struct pg3gpu_ctx {
@@ -58,6 +59,8 @@ struct pg3gpu_ctx {
     void *dWaveGrad = nullptr;                      // queues with gradient records
     uint64_t waveGradCapacity = 0;
     float *dRowInt = nullptr;                       // environment-map CDF build: per-row integrals
+    bool hasSteer = false;                          // steerable sampler: its device build inputs/outputs
+    pg3::SteerWeightArgs steerArgs{};
     uint32_t diffIteration = 0, diffSpp = 0;        // samples the stored radiance belongs to
     const uint32_t *dSampleOffset = nullptr;        // caller's device word added to sample indices
     bool diffValid = false;

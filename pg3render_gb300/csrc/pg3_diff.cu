@@ -214,9 +214,6 @@ extern "C" int pg3gpu_set_params(pg3gpu_ctx *ctx, const float *mp, const float *
     const bool hasEm = v.bgKind == kBgEnvMap;
     if (et && !hasEm) return ctxError(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "the scene has no environment map");
     const bool rebuild = et && !keep;
-    if (rebuild && v.emSampler == kEmSteerable)
-        return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED,
-                        "the steerable sampler's tables are built on the host: pass PG3GPU_PARAMS_KEEP_SAMPLING");
     if (rebuild && (v.emW > kMaxCdfSide || v.emH > kMaxCdfSide))
         return ctxError(ctx, PG3GPU_ERR_UNSUPPORTED, "device CDF rebuild supports maps up to 8192 texels a side");
     if (int st = cudaStatus(ctx, cudaSetDevice(ctx->device), "cudaSetDevice")) return st;
@@ -249,6 +246,8 @@ extern "C" int pg3gpu_set_params(pg3gpu_ctx *ctx, const float *mp, const float *
                 cdfMarginalKernel<<<1, kCdfBlock, v.emH * sizeof(float), ctx->stream>>>(
                     ctx->dRowInt, v.emH, const_cast<float *>(v.emMarg));
             }
+            // the steerable sampler's weights (and with them the background's picking estimate)
+            if (!st && ctx->hasSteer) st = cudaStatus(ctx, launchSteerWeights(ctx->steerArgs, ctx->stream), "steerable build");
         }
     }
     if (!st) st = cudaStatus(ctx, cudaGetLastError(), "parameter update");

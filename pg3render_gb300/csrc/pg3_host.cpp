@@ -41,15 +41,18 @@ void computeCdf(const float *f, uint32_t n, float *cdf, float &integral)
 
 void buildEmCdf(const float *rgb, uint32_t W, uint32_t H, std::vector<float> &marg, std::vector<float> &cond)
 {
+    // texel luminances once; the filter below reads them through the wrap rule at the border
+    std::vector<float> lumImg((size_t)W * H);
+    for (size_t i = 0; i < lumImg.size(); ++i) lumImg[i] = lum(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
     auto L = [&](int x, int y) {
+        if (x >= 0 && x < (int)W && y >= 0 && y < (int)H) return lumImg[(size_t)y * W + (size_t)x];
         // NormalizeImgCoords (src/em_image.hxx:269-302)
         int rx = x, ry = y;
         if (y >= (int)H) { rx = x + (int)W / 2; ry = (int)H - 1; }
         else if (y < 0) { rx = x + (int)W / 2; ry = 0; }
         int m = rx % (int)W;
         if (m < 0) m += (int)W;
-        const float *p = rgb + ((size_t)ry * W + (size_t)m) * 3;
-        return lum(p[0], p[1], p[2]);
+        return lumImg[(size_t)ry * W + (size_t)m];
     };
     std::vector<float> f((size_t)W);
     cond.assign((size_t)H * (W + 1), 0.f);
@@ -78,12 +81,18 @@ void emShCoefficients(const float *rgb, uint32_t W, uint32_t H, std::vector<floa
 {
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const double pi = 3.14159265358979323846;
+    std::vector<double> cosPhi(W), sinPhi(W);
+    for (uint32_t c = 0; c < W; ++c) {
+        const double phi = -((c + 0.5) / W - 0.5) * 2.0 * pi;   // latLong2Dir
+        cosPhi[c] = std::cos(phi);
+        sinPhi[c] = std::sin(phi);
+    }
     for (uint32_t r = 0; r < H; ++r) {
         const double theta = pi * (r + 0.5) / H;
-        const double dOmega = (2.0 * pi / W) * (pi / H) * std::sin(theta);
+        const double sinT = std::sin(theta), z = std::cos(theta);
+        const double dOmega = (2.0 * pi / W) * (pi / H) * sinT;
         for (uint32_t c = 0; c < W; ++c) {
-            const double phi = -((c + 0.5) / W - 0.5) * 2.0 * pi;   // latLong2Dir
-            const double x = std::sin(theta) * std::cos(phi), y = std::sin(theta) * std::sin(phi), z = std::cos(theta);
+            const double x = sinT * cosPhi[c], y = sinT * sinPhi[c];
             const float *p = rgb + ((size_t)r * W + c) * 3;
             const double L = (0.212671 * p[0] + 0.715160 * p[1] + 0.072169 * p[2]) * dOmega;
             acc[0] += L * 0.282095;
@@ -299,14 +308,14 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
             out.em[i] = make_float4(p[0], p[1], p[2], 0.f);
         }
         buildEmCdf(sc.env_map, sc.env_width, sc.env_height, out.emMarg, out.emCond);
-        emShCoefficients(sc.env_map, sc.env_width, sc.env_height, out.bgShL);
         v.emW = sc.env_width;
         v.emH = sc.env_height;
         if (o.em_sampler == PG3GPU_EM_STEERABLE) {
-            if (!buildSteerable(sc.env_map, sc.env_width, sc.env_height, o.steer_subdiv_level, out.steer, err))
-                return PG3GPU_ERR_INVALID_ARGUMENT;
-            out.hasSteer = true;
-            out.bgShL = out.steer.rootW;   // the steerable sampler's own irradiance estimate (its whole integral)
+            out.steer = steerGeometry(o.steer_subdiv_level, err);
+            if (!out.steer) return PG3GPU_ERR_INVALID_ARGUMENT;
+            out.hasSteer = true;   // the picking estimate is the sampler's own whole integral (device)
+        } else {
+            emShCoefficients(sc.env_map, sc.env_width, sc.env_height, out.bgShL);
         }
     } else if (sc.background != PG3GPU_BG_NONE && sc.background != PG3GPU_BG_CONSTANT) {
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown background kind");

@@ -25,7 +25,8 @@ struct HostScene {
     std::vector<float4> em;
     std::vector<float> emMarg, emCond;
     std::vector<float> bgShL;            // 9 SH coefficients of the map's luminance (picking estimate)
-    SteerableHost steer;
+    const SteerGeom *steer = nullptr;    // steerable sampler geometry (shared, process lifetime); its
+                                         // weights are built on the device
     bool hasSteer = false;
     uint32_t kindMask = 0;               // material kinds present (bit per PG3GPU_MAT_* kind)
     uint32_t numPointLights = 0;

@@ -42,6 +42,23 @@ cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t samp
                             uint64_t capacity, int gridBlocks, cudaStream_t stream, uint64_t *launches,
                             const GradArgs *grad = nullptr);
 
+// pg3_steer_build.cu: the steerable sampler's map-dependent tables from the device texels
+constexpr uint32_t kSteerMaxLayers = 16;
+struct SteerWeightArgs {
+    const float4 *em;
+    uint32_t emW, emH;
+    const float4 *vdir;                          // geometry (pg3_steerable.cpp)
+    uint32_t numVertices;
+    const int4 *leafTri;
+    const float *leafArea;
+    uint32_t numLeaves;
+    const int *nodeChild;
+    uint32_t layerStart[kSteerMaxLayers + 1];    // tree layers bottom-up, node ranges
+    uint32_t numLayers;
+    float *vw, *leafW, *nodeW, *rootW;           // outputs (9 / 9 / 54 floats per item, 9)
+};
+cudaError_t launchSteerWeights(const SteerWeightArgs &args, cudaStream_t stream);
+
 // pg3_probe.cu (sampler probes for tests)
 cudaError_t launchProbeBsdf(const SceneView &S, int mat, uint32_t n, const float *wol, uint32_t seed, float *wil,
                             float *pdfS, float *pdfE, float *attS, float *attE, cudaStream_t st);

@@ -1,0 +1,140 @@
+// Device build of the steerable sampler's map-dependent tables (the geometry comes from the
+// host, pg3_steerable.cpp): vertex weights, leaf weights, the 6-ary tree's node weights and the
+// whole-sphere integral. It runs at context creation and whenever the environment map changes
+// (differentiable rendering), so neither waits for a host pass over the map.
+//
+// vertex weight   vw[v][k]  = Y_k(d_v) * L(d_v)         (src/em_steerable_sampler.hxx:181-202, 3084-3095)
+// leaf weight     lw[t][k]  = area_t * mean of its three vertex weights           (:1277-1296)
+// node weight     nodeW[n][c][k] = the summed weight of child c                    (:3755-3793)
+// whole sphere    rootW[k]  = sum over all leaves of lw[t][k]
+// with Y the 9 real SH basis functions (Ramamoorthi & Hanrahan 2001) and L the luminance of
+// the map's bilinear (tent) lookup in the vertex direction (src/em_image.hxx:95-143).
+#include <climits>
+
+#include "pg3_kernels.h"
+
+namespace pg3 {
+
+namespace {
+
+__device__ float texelLum(const float4 *em, uint32_t W, uint32_t H, int x, int y)
+{
+    // NormalizeImgCoords (src/em_image.hxx:269-302)
+    int rx = x, ry = y;
+    if (y >= (int)H) { rx = x + (int)W / 2; ry = (int)H - 1; }
+    else if (y < 0) { rx = x + (int)W / 2; ry = 0; }
+    int m = rx % (int)W;
+    if (m < 0) m += (int)W;
+    const float4 p = em[(size_t)ry * W + (size_t)m];
+    return 0.212671f * p.x + 0.715160f * p.y + 0.072169f * p.z;
+}
+
+__global__ void vertexWeightsKernel(const float4 *em, uint32_t W, uint32_t H, const float4 *vdir, uint32_t nv,
+                                    float *vw)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float4 d = vdir[i];
+    const float kPi = 3.14159265358979f;
+    const float phi = -atan2f(d.y, d.x);
+    const float theta = acosf(fminf(fmaxf(d.z, -1.f), 1.f));
+    const float u = fminf(fmaxf(0.5f + phi * 0.5f * (1.f / kPi), 0.f), 1.f);
+    const float v = fminf(fmaxf(theta * (1.f / kPi), 0.f), 1.f);
+    const float xf = u * (float)W, yf = v * (float)H;
+    const int cx = (int)(xf + 0.5f), cy = (int)(yf + 0.5f);
+    const int x0 = cx - 1, y0 = cy - 1;
+    const float xl = xf - ((float)x0 + 0.5f), yl = yf - ((float)y0 + 0.5f);
+    const float top = (1.f - xl) * texelLum(em, W, H, x0, y0) + xl * texelLum(em, W, H, cx, y0);
+    const float bot = (1.f - xl) * texelLum(em, W, H, x0, cy) + xl * texelLum(em, W, H, cx, cy);
+    const float L = (1.f - yl) * top + yl * bot;
+    const float x = d.x, y = d.y, z = d.z;
+    float *o = vw + 9 * (size_t)i;
+    o[0] = L * 0.282095f;
+    o[1] = L * 0.488603f * y;
+    o[2] = L * 0.488603f * z;
+    o[3] = L * 0.488603f * x;
+    o[4] = L * 1.092548f * x * y;
+    o[5] = L * 1.092548f * y * z;
+    o[6] = L * 0.315392f * (3.f * z * z - 1.f);
+    o[7] = L * 1.092548f * x * z;
+    o[8] = L * 0.546274f * (x * x - y * y);
+}
+
+__global__ void leafWeightsKernel(const int4 *leafTri, const float *leafArea, uint32_t nLeaf, const float *vw,
+                                  float *lw)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nLeaf) return;
+    const int4 t = leafTri[i];
+    const float a = leafArea[i] * (1.f / 3.f);
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+        lw[9 * (size_t)i + k] = a * (vw[9 * (size_t)t.x + k] + vw[9 * (size_t)t.y + k] + vw[9 * (size_t)t.z + k]);
+}
+
+// One tree layer: every child slot of nodes [n0, n1) gets its child's summed weight (a leaf's
+// weight, or the sum of a lower node's six child slots, written by the previous launch).
+__global__ void treeLayerKernel(const int *nodeChild, uint32_t n0, uint32_t n1, const float *lw, float *nodeW)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= 6 * (n1 - n0)) return;
+    const uint32_t n = n0 + j / 6, c = j % 6;
+    const int ch = nodeChild[6 * (size_t)n + c];
+    float w[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) w[k] = 0.f;
+    if (ch != INT_MIN) {
+        if (ch < 0) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) w[k] = lw[9 * (size_t)(~ch) + k];
+        } else {
+            for (int cc = 0; cc < 6; ++cc)
+#pragma unroll
+                for (int k = 0; k < 9; ++k) w[k] += nodeW[54 * (size_t)ch + 9 * cc + k];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) nodeW[54 * (size_t)n + 9 * c + k] = w[k];
+}
+
+// Whole-sphere weights: one block, fp64 partial sums over all leaves.
+__global__ void rootWeightsKernel(const float *lw, uint32_t nLeaf, float *rootW)
+{
+    __shared__ double part[9][256];
+    double acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+    for (uint32_t i = threadIdx.x; i < nLeaf; i += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] += lw[9 * (size_t)i + k];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) part[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (uint32_t s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) part[k][threadIdx.x] += part[k][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x < 9) rootW[threadIdx.x] = (float)part[threadIdx.x][0];
+}
+
+}  // namespace
+
+cudaError_t launchSteerWeights(const SteerWeightArgs &a, cudaStream_t st)
+{
+    if (!a.em || !a.vdir || !a.leafTri || !a.leafArea || !a.nodeChild || !a.vw || !a.leafW || !a.nodeW ||
+        !a.rootW || a.numLayers == 0 || a.numLayers > kSteerMaxLayers)
+        return cudaErrorInvalidValue;
+    vertexWeightsKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.em, a.emW, a.emH, a.vdir, a.numVertices, a.vw);
+    leafWeightsKernel<<<(a.numLeaves + 127) / 128, 128, 0, st>>>(a.leafTri, a.leafArea, a.numLeaves, a.vw, a.leafW);
+    for (uint32_t l = 0; l < a.numLayers; ++l) {
+        const uint32_t n0 = a.layerStart[l], n1 = a.layerStart[l + 1];
+        if (n1 <= n0) return cudaErrorInvalidValue;
+        treeLayerKernel<<<(6 * (n1 - n0) + 127) / 128, 128, 0, st>>>(a.nodeChild, n0, n1, a.leafW, a.nodeW);
+    }
+    rootWeightsKernel<<<1, 256, 0, st>>>(a.leafW, a.numLeaves, a.rootW);
+    return cudaGetLastError();
+}
+
+}  // namespace pg3

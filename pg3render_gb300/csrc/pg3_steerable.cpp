@@ -1,9 +1,14 @@
-// Host-side build of the steerable sampler tables (see pg3_steerable.h).
+// Host-side build of the steerable sampler's geometry (see pg3_steerable.h).
 #include "pg3_steerable.h"
 
+#include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
 #include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
 #include <utility>
 
 namespace pg3 {
@@ -17,59 +22,33 @@ D3 crs(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x *
 double dt(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 D3 nrm(D3 a) { const double l = std::sqrt(dt(a, a)); return {a.x / l, a.y / l, a.z / l}; }
 
-const float kPi = 3.14159265358979f;
-
-// Bilinear (tent) lookup of the lat-long map, as the kernels do (src/em_image.hxx:95-143).
-float emLuminanceAt(const float *rgb, uint32_t W, uint32_t H, float dx, float dy, float dz)
+// Runs body(i) for i in [0, n) on up to 16 host threads.
+template <class F>
+void parallelFor(uint32_t n, F body)
 {
-    const float phi = -std::atan2(dy, dx);
-    const float theta = std::acos(std::fmin(std::fmax(dz, -1.f), 1.f));
-    const float u = std::fmin(std::fmax(0.5f + phi * 0.5f * (1.f / kPi), 0.f), 1.f);
-    const float v = std::fmin(std::fmax(theta * (1.f / kPi), 0.f), 1.f);
-    const float xf = u * (float)W, yf = v * (float)H;
-    const int cx = (int)(xf + 0.5f), cy = (int)(yf + 0.5f);
-    const int x0 = cx - 1, y0 = cy - 1;
-    const float xl = xf - ((float)x0 + 0.5f), yl = yf - ((float)y0 + 0.5f);
-    auto wrap = [&](int x, int y, int &ox, int &oy) {
-        int rx = x, ry = y;
-        if (y >= (int)H) { rx = x + (int)W / 2; ry = (int)H - 1; }
-        else if (y < 0) { rx = x + (int)W / 2; ry = 0; }
-        int m = rx % (int)W;
-        if (m < 0) m += (int)W;
-        ox = m; oy = ry;
-    };
-    auto lum = [&](int x, int y) {
-        const float *p = rgb + ((size_t)y * W + (size_t)x) * 3;
-        return 0.212671f * p[0] + 0.715160f * p[1] + 0.072169f * p[2];
-    };
-    int ax, ay, bx, by;
-    wrap(x0, y0, ax, ay);
-    wrap(cx, cy, bx, by);
-    const float top = (1.f - xl) * lum(ax, ay) + xl * lum(bx, ay);
-    const float bot = (1.f - xl) * lum(ax, by) + xl * lum(bx, by);
-    return (1.f - yl) * top + yl * bot;
-}
-
-// 9 real SH basis values (Ramamoorthi & Hanrahan 2001), scaled by s.
-void shBasis(double x, double y, double z, double s, float *o)
-{
-    o[0] = (float)(s * 0.282095);
-    o[1] = (float)(s * 0.488603 * y);
-    o[2] = (float)(s * 0.488603 * z);
-    o[3] = (float)(s * 0.488603 * x);
-    o[4] = (float)(s * 1.092548 * x * y);
-    o[5] = (float)(s * 1.092548 * y * z);
-    o[6] = (float)(s * 0.315392 * (3.0 * z * z - 1.0));
-    o[7] = (float)(s * 1.092548 * x * z);
-    o[8] = (float)(s * 0.546274 * (x * x - y * y));
+    const uint32_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const uint32_t nt = std::min(hw, std::max(1u, n / 16));
+    if (nt <= 1) {
+        for (uint32_t i = 0; i < n; ++i) body(i);
+        return;
+    }
+    std::atomic<uint32_t> next(0);
+    std::vector<std::thread> pool;
+    for (uint32_t t = 0; t < nt; ++t)
+        pool.emplace_back([&] {
+            for (uint32_t i; (i = next.fetch_add(1)) < n;) body(i);
+        });
+    for (auto &th : pool) th.join();
 }
 
 }  // namespace
 
-bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, SteerableHost &out, std::string &err)
+
+namespace {
+
+bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
 {
-    if (level > 7) { err = "steerable subdivision level must be <= 7"; return false; }
-    out = SteerableHost();
+    out = SteerGeom();
     out.level = level;
 
     // icosahedron: the 12 cyclic permutations of (0, +-1, +-t), normalised
@@ -125,97 +104,65 @@ bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, St
         cur.swap(next);
     }
     out.levelOffset.push_back((uint32_t)out.tri.size());
+    out.vdir.resize(v.size());
+    for (size_t i = 0; i < v.size(); ++i) out.vdir[i] = make_float4((float)v[i].x, (float)v[i].y, (float)v[i].z, 0.f);
 
-    // vertex weights: SH basis scaled by the map's luminance in the vertex direction
-    const size_t nv = v.size();
-    out.vdir.resize(nv);
-    out.vw.resize(nv * 9);
-    for (size_t i = 0; i < nv; ++i) {
-        out.vdir[i] = make_float4((float)v[i].x, (float)v[i].y, (float)v[i].z, 0.f);
-        const float L = emLuminanceAt(rgb, W, H, (float)v[i].x, (float)v[i].y, (float)v[i].z);
-        shBasis(v[i].x, v[i].y, v[i].z, (double)L, &out.vw[i * 9]);
-    }
-
-    // leaf weights: planar area x mean vertex weight (src/em_steerable_sampler.hxx:1277-1296),
-    // and each leaf's plane (unit normal, distance) for the solid-angle Jacobian
+    // leaves: planar area (the leaf weight is area x mean vertex weight,
+    // src/em_steerable_sampler.hxx:1277-1296) and plane (unit normal, distance) for the
+    // solid-angle Jacobian
     const uint32_t nLeaf = (uint32_t)cur.size();
-    std::vector<float> leafW((size_t)nLeaf * 9);
+    out.leafArea.resize(nLeaf);
     out.leafPlane.resize(nLeaf);
+    auto fdir = [&](int id) { return D3{out.vdir[id].x, out.vdir[id].y, out.vdir[id].z}; };
     for (uint32_t i = 0; i < nLeaf; ++i) {
         const int4 T = cur[i];
-        const D3 a = {out.vdir[T.x].x, out.vdir[T.x].y, out.vdir[T.x].z};
-        const D3 b = {out.vdir[T.y].x, out.vdir[T.y].y, out.vdir[T.y].z};
-        const D3 c = {out.vdir[T.z].x, out.vdir[T.z].y, out.vdir[T.z].z};
+        const D3 a = fdir(T.x), b = fdir(T.y), c = fdir(T.z);
         const D3 cr = crs(sub(b, a), sub(c, a));
-        const double area = 0.5 * std::sqrt(dt(cr, cr));
+        out.leafArea[i] = (float)(0.5 * std::sqrt(dt(cr, cr)));
         const D3 nT = nrm(cr);
         out.leafPlane[i] = make_float4((float)nT.x, (float)nT.y, (float)nT.z, (float)dt(nT, a));
-        for (int k = 0; k < 9; ++k)
-            leafW[(size_t)i * 9 + k] = (float)(area * ((double)out.vw[T.x * 9 + k] + out.vw[T.y * 9 + k] +
-                                                       out.vw[T.z * 9 + k]) / 3.0);
     }
 
-    // 6-ary tree, bottom-up over consecutive nodes (src/em_steerable_sampler.hxx:3755-3793)
-    struct Item { int id; float w[9]; };
-    std::vector<Item> layer(nLeaf);
-    for (uint32_t i = 0; i < nLeaf; ++i) {
-        layer[i].id = ~(int)i;
-        for (int k = 0; k < 9; ++k) layer[i].w[k] = leafW[(size_t)i * 9 + k];
-    }
+    // 6-ary tree topology, bottom-up over consecutive items (src/em_steerable_sampler.hxx:3755-3793)
+    std::vector<int> layer(nLeaf);
+    for (uint32_t i = 0; i < nLeaf; ++i) layer[i] = ~(int)i;
     do {
-        std::vector<Item> up;
+        out.layerStart.push_back((uint32_t)(out.nodeChild.size() / 6));
+        std::vector<int> up;
         for (size_t s = 0; s < layer.size(); s += 6) {
-            const int node = (int)(out.nodeChild.size() / 6);
-            Item parent;
-            parent.id = node;
-            for (int k = 0; k < 9; ++k) parent.w[k] = 0.f;
-            for (size_t c = 0; c < 6; ++c) {
-                if (s + c < layer.size()) {
-                    const Item &ch = layer[s + c];
-                    out.nodeChild.push_back(ch.id);
-                    for (int k = 0; k < 9; ++k) {
-                        out.nodeW.push_back(ch.w[k]);
-                        parent.w[k] += ch.w[k];
-                    }
-                } else {
-                    out.nodeChild.push_back(INT_MIN);
-                    for (int k = 0; k < 9; ++k) out.nodeW.push_back(0.f);
-                }
-            }
-            up.push_back(parent);
+            up.push_back((int)(out.nodeChild.size() / 6));
+            for (size_t c = 0; c < 6; ++c) out.nodeChild.push_back(s + c < layer.size() ? layer[s + c] : INT_MIN);
         }
         layer.swap(up);
     } while (layer.size() > 1);
-    out.root = layer[0].id;
-    out.rootW.assign(9, 0.f);
-    {
-        double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (uint32_t i = 0; i < nLeaf; ++i)
-            for (int k = 0; k < 9; ++k) acc[k] += leafW[(size_t)i * 9 + k];
-        for (int k = 0; k < 9; ++k) out.rootW[k] = (float)acc[k];
-    }
+    out.layerStart.push_back((uint32_t)(out.nodeChild.size() / 6));
+    out.root = layer[0];
 
     // leaf locator: inward edge normals of every leaf, and for every cell of a finer cube map
     // the leaves whose bounding cap meets the cell's bounding cap (a superset of the leaves
-    // that touch the cell); cells with more than 8 keep the face locator
+    // that touch the cell); cells with more than 8 keep the face locator. Caps meet when the
+    // angle between their centres is at most the sum of their radii (plus a margin), i.e. when
+    // the cosine of that angle is at least cos(rLeaf + rCell).
     out.leafEdge.resize((size_t)nLeaf * 3);
     std::vector<D3> capC(nLeaf);
-    std::vector<double> capR(nLeaf);
+    std::vector<double> capCos(nLeaf), capSin(nLeaf);
     for (uint32_t i = 0; i < nLeaf; ++i) {
         const int4 T = cur[i];
-        const D3 a = {out.vdir[T.x].x, out.vdir[T.x].y, out.vdir[T.x].z};
-        const D3 b = {out.vdir[T.y].x, out.vdir[T.y].y, out.vdir[T.y].z};
-        const D3 c = {out.vdir[T.z].x, out.vdir[T.z].y, out.vdir[T.z].z};
+        const D3 a = fdir(T.x), b = fdir(T.y), c = fdir(T.z);
         const D3 e[3] = {nrm(crs(a, b)), nrm(crs(b, c)), nrm(crs(c, a))};
         for (int k = 0; k < 3; ++k)
             out.leafEdge[3 * (size_t)i + k] = make_float4((float)e[k].x, (float)e[k].y, (float)e[k].z, 0.f);
         capC[i] = nrm(add(add(a, b), c));
-        capR[i] = std::acos(std::fmin(1.0, std::fmin(dt(capC[i], a), std::fmin(dt(capC[i], b), dt(capC[i], c)))));
+        const double r = std::acos(std::fmin(1.0, std::fmin(dt(capC[i], a), std::fmin(dt(capC[i], b), dt(capC[i], c)))));
+        capCos[i] = std::cos(r);
+        capSin[i] = std::sin(r);
     }
     const uint32_t LG = 4u << level;
     out.leafGrid = LG;
     out.leafCells.assign((size_t)6 * LG * LG, make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu));
-    for (int f = 0; f < 6; ++f) {
+    parallelFor(6 * LG, [&](uint32_t row) {
+        const int f = (int)(row / LG);
+        const uint32_t iv = row % LG;
         const int ax = f / 2, bx = (ax + 1) % 3, cx = (ax + 2) % 3;
         const double sg = (f & 1) ? -1.0 : 1.0;
         auto dirOf = [&](double u, double vv) {
@@ -223,83 +170,108 @@ bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, St
             p[ax] = sg; p[bx] = u; p[cx] = vv;
             return nrm({p[0], p[1], p[2]});
         };
-        for (uint32_t iv = 0; iv < LG; ++iv)
-            for (uint32_t iu = 0; iu < LG; ++iu) {
-                const double u0 = -1.0 + 2.0 * iu / LG, u1 = -1.0 + 2.0 * (iu + 1) / LG;
-                const double v0 = -1.0 + 2.0 * iv / LG, v1 = -1.0 + 2.0 * (iv + 1) / LG;
-                const D3 cc = dirOf(0.5 * (u0 + u1), 0.5 * (v0 + v1));
-                double rc = 0.0;
-                for (const D3 &q : {dirOf(u0, v0), dirOf(u1, v0), dirOf(u0, v1), dirOf(u1, v1)})
-                    rc = std::fmax(rc, std::acos(std::fmin(1.0, dt(cc, q))));
-                uint32_t ids[8];
-                int n = 0;
-                bool many = false;
-                for (uint32_t i = 0; i < nLeaf && !many; ++i) {
-                    const double ang = std::acos(std::fmax(-1.0, std::fmin(1.0, dt(cc, capC[i]))));
-                    if (ang <= capR[i] + rc + 1e-4) {
-                        if (n == 8 || i >= kSteerLeafMany) many = true;
-                        else ids[n++] = i;
-                    }
+        for (uint32_t iu = 0; iu < LG; ++iu) {
+            const double u0 = -1.0 + 2.0 * iu / LG, u1 = -1.0 + 2.0 * (iu + 1) / LG;
+            const double v0 = -1.0 + 2.0 * iv / LG, v1 = -1.0 + 2.0 * (iv + 1) / LG;
+            const D3 cc = dirOf(0.5 * (u0 + u1), 0.5 * (v0 + v1));
+            double rc = 0.0;
+            for (const D3 &q : {dirOf(u0, v0), dirOf(u1, v0), dirOf(u0, v1), dirOf(u1, v1)})
+                rc = std::fmax(rc, std::acos(std::fmin(1.0, dt(cc, q))));
+            rc += 1e-4;
+            const double cCos = std::cos(rc), cSin = std::sin(rc);
+            uint32_t ids[8];
+            int n = 0;
+            bool many = false;
+            for (uint32_t i = 0; i < nLeaf && !many; ++i) {
+                // cos(rLeaf + rCell); both radii are far below pi/2 at every level
+                const double lim = capCos[i] * cCos - capSin[i] * cSin;
+                if (dt(cc, capC[i]) >= lim) {
+                    // (leaf ids from 0xfffe on do not fit the 16-bit lists: the face locator serves)
+                    if (n == 8 || i >= kSteerLeafMany) many = true;
+                    else ids[n++] = i;
                 }
-                uint4 &cell = out.leafCells[((size_t)f * LG + iv) * LG + iu];
-                if (many) {
-                    cell = make_uint4(0xfffefffeu, 0xfffefffeu, 0xfffefffeu, 0xfffefffeu);
-                    continue;
-                }
-                uint32_t w[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
-                for (int k = 0; k < n; ++k) {
-                    const uint32_t shift = (k & 1) ? 16u : 0u;
-                    w[k >> 1] = (w[k >> 1] & ~(0xffffu << shift)) | (ids[k] << shift);
-                }
-                cell = make_uint4(w[0], w[1], w[2], w[3]);
             }
-    }
+            uint4 &cell = out.leafCells[((size_t)f * LG + iv) * LG + iu];
+            if (many) {
+                cell = make_uint4(0xfffefffeu, 0xfffefffeu, 0xfffefffeu, 0xfffefffeu);
+                continue;
+            }
+            uint32_t w[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
+            for (int k = 0; k < n; ++k) {
+                const uint32_t shift = (k & 1) ? 16u : 0u;
+                w[k >> 1] = (w[k >> 1] & ~(0xffffu << shift)) | (ids[k] << shift);
+            }
+            cell = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    });
 
     // face locator: for every cell of a cube map over the sphere, the level-0 faces that
     // touch the cell (found by dense sampling of the cell enlarged by a margin)
     const int G = kSteerCells;
     out.faceCells.assign(2 * 6 * G * G, make_int4(-1, -1, -1, -1));
-    for (int f = 0; f < 6; ++f) {
+    D3 edgeN[20][3];
+    for (int fi = 0; fi < 20; ++fi) {
+        const int4 tf = level0[fi];
+        const D3 A = fdir(tf.x), B = fdir(tf.y), C = fdir(tf.z);
+        edgeN[fi][0] = crs(A, B);
+        edgeN[fi][1] = crs(B, C);
+        edgeN[fi][2] = crs(C, A);
+    }
+    std::atomic<bool> overflow(false);
+    parallelFor(6 * G * G, [&](uint32_t cell) {
+        const int f = (int)cell / (G * G), iv = ((int)cell / G) % G, iu = (int)cell % G;
         const int ax = f / 2, bx = (ax + 1) % 3, cx = (ax + 2) % 3;
         const double s = (f & 1) ? -1.0 : 1.0;
-        for (int iv = 0; iv < G; ++iv)
-            for (int iu = 0; iu < G; ++iu) {
-                int found[8], nf = 0;
-                const int K = 24;
-                for (int sv = 0; sv <= K; ++sv)
-                    for (int su = 0; su <= K; ++su) {
-                        const double u = -1.0 + 2.0 * (iu + (su / (double)K) * 1.1 - 0.05) / G;
-                        const double vv = -1.0 + 2.0 * (iv + (sv / (double)K) * 1.1 - 0.05) / G;
-                        double p[3];
-                        p[ax] = s; p[bx] = u; p[cx] = vv;
-                        const D3 w = nrm({p[0], p[1], p[2]});
-                        for (int fi = 0; fi < 20; ++fi) {
-                            const int4 t = level0[fi];
-                            const D3 A = {out.vdir[t.x].x, out.vdir[t.x].y, out.vdir[t.x].z};
-                            const D3 B = {out.vdir[t.y].x, out.vdir[t.y].y, out.vdir[t.y].z};
-                            const D3 C = {out.vdir[t.z].x, out.vdir[t.z].y, out.vdir[t.z].z};
-                            const double m = std::fmin(std::fmin(dt(w, crs(A, B)), dt(w, crs(B, C))), dt(w, crs(C, A)));
-                            if (m >= -1e-3) {
-                                bool have = false;
-                                for (int q = 0; q < nf; ++q) have |= (found[q] == fi);
-                                if (!have && nf < 8) found[nf++] = fi;
-                            }
+        int found[8], nf = 0;
+        const int K = 24;
+        for (int sv = 0; sv <= K; ++sv)
+            for (int su = 0; su <= K; ++su) {
+                const double u = -1.0 + 2.0 * (iu + (su / (double)K) * 1.1 - 0.05) / G;
+                const double vv = -1.0 + 2.0 * (iv + (sv / (double)K) * 1.1 - 0.05) / G;
+                double p[3];
+                p[ax] = s; p[bx] = u; p[cx] = vv;
+                const D3 w = nrm({p[0], p[1], p[2]});
+                for (int fi = 0; fi < 20; ++fi) {
+                    const double m = std::fmin(std::fmin(dt(w, edgeN[fi][0]), dt(w, edgeN[fi][1])), dt(w, edgeN[fi][2]));
+                    if (m >= -1e-3) {
+                        bool have = false;
+                        for (int q = 0; q < nf; ++q) have |= (found[q] == fi);
+                        if (!have) {
+                            if (nf < 8) found[nf++] = fi;
+                            else overflow = true;
                         }
                     }
-                if (nf > 8) { err = "steerable face locator: more than 8 faces in a cube-map cell"; return false; }
-                int4 &c0 = out.faceCells[2 * ((f * G + iv) * G + iu)];
-                int4 &c1 = out.faceCells[2 * ((f * G + iv) * G + iu) + 1];
-                c0.x = nf > 0 ? found[0] : -1;
-                c0.y = nf > 1 ? found[1] : -1;
-                c0.z = nf > 2 ? found[2] : -1;
-                c0.w = nf > 3 ? found[3] : -1;
-                c1.x = nf > 4 ? found[4] : -1;
-                c1.y = nf > 5 ? found[5] : -1;
-                c1.z = nf > 6 ? found[6] : -1;
-                c1.w = nf > 7 ? found[7] : -1;
+                }
             }
-    }
+        int4 &c0 = out.faceCells[2 * cell];
+        int4 &c1 = out.faceCells[2 * cell + 1];
+        c0.x = nf > 0 ? found[0] : -1;
+        c0.y = nf > 1 ? found[1] : -1;
+        c0.z = nf > 2 ? found[2] : -1;
+        c0.w = nf > 3 ? found[3] : -1;
+        c1.x = nf > 4 ? found[4] : -1;
+        c1.y = nf > 5 ? found[5] : -1;
+        c1.z = nf > 6 ? found[6] : -1;
+        c1.w = nf > 7 ? found[7] : -1;
+    });
+    if (overflow) { err = "steerable face locator: more than 8 faces in a cube-map cell"; return false; }
     return true;
+}
+
+}  // namespace
+
+const SteerGeom *steerGeometry(uint32_t level, std::string &err)
+{
+    if (level > 7) { err = "steerable subdivision level must be <= 7"; return nullptr; }
+    static std::mutex mu;
+    static std::unique_ptr<SteerGeom> cache[8];
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cache[level]) {
+        std::unique_ptr<SteerGeom> g(new SteerGeom);
+        if (!buildGeometry(level, *g, err)) return nullptr;
+        cache[level] = std::move(g);
+    }
+    return cache[level].get();
 }
 
 }  // namespace pg3

@@ -1,6 +1,5 @@
 // Steerable environment-map sampler (Subr & Arvo 2007, as structured by the
-// reference's EnvironmentMapSteerableSampler, src/em_steerable_sampler.hxx),
-// host-side build in device layout.
+// reference's EnvironmentMapSteerableSampler, src/em_steerable_sampler.hxx).
 //
 // Triangulation: the unit icosahedron (src/geom.hxx:291-346) subdivided 4-way
 // `level` times with edge midpoints pushed to the sphere -- the reference's
@@ -10,6 +9,14 @@
 // each leaf triangle the planar area times its mean vertex weight (:1277-1296).
 // A 6-ary tree is built bottom-up over the leaves in subdivision order
 // (:3755-3793).
+//
+// The build is split by what it depends on:
+// * the geometry (triangulation, tree topology, leaf planes and edge normals, the
+//   cube-map leaf and face locators) depends only on the level: it is built once per
+//   process and level on the host (steerGeometry) and shared by every context;
+// * the weights (vertex, leaf and tree-node weights and the whole-sphere integral)
+//   depend on the map: they are computed on the device from the uploaded texels
+//   (launchSteerWeights), at context creation and again whenever the map changes.
 //
 // Corrections over the reference (whose sampled and evaluated pdfs disagree):
 // * the density is the linear interpolation of the vertex values on the planar
@@ -30,28 +37,31 @@
 
 namespace pg3 {
 
-struct SteerableHost {
+struct SteerGeom {
     uint32_t level = 0;
     std::vector<float4> vdir;          // vertex directions
-    std::vector<float> vw;             // 9 weights per vertex
     std::vector<int4> tri;             // vertex ids of every triangle of every level (level 0 first)
     std::vector<uint32_t> levelOffset; // first triangle of each level in `tri` (level+1 entries + end)
-    std::vector<float> nodeW;          // 6 x 9 child weights per tree node
+    std::vector<float> leafArea;       // planar area of every leaf triangle
     std::vector<int> nodeChild;        // 6 child ids per node: >= 0 node, < 0 ~leaf, INT32_MIN none
+    std::vector<uint32_t> layerStart;  // first node of every tree layer, bottom (parents of leaves)
+                                       // first, then the end of the node list
     std::vector<float4> leafPlane;     // per leaf: unit normal of the planar triangle, distance from origin
     std::vector<int4> faceCells;       // cube-map cells (6 x kSteerCells^2) x 2: up to 8 candidate level-0 faces
-    std::vector<float> rootW;          // 9 weights: the sum over all leaves (whole-sphere integral)
     std::vector<float4> leafEdge;      // per leaf 3 inward great-circle normals (edges ab, bc, ca)
     std::vector<uint4> leafCells;      // cube-map cells (6 x leafGrid^2): up to 8 candidate leaves as
                                        // 16-bit ids (0xffff none); all 0xfffe: more, use the face locator
     uint32_t leafGrid = 0;
     int root = 0;
+    uint32_t numLeaves() const { return (uint32_t)leafArea.size(); }
+    uint32_t numNodes() const { return (uint32_t)(nodeChild.size() / 6); }
 };
 
 constexpr int kSteerCells = 8;         // cube-map resolution of the face locator
 constexpr uint32_t kSteerLeafNone = 0xffffu, kSteerLeafMany = 0xfffeu;
 
-// rgb: env_height rows of env_width RGB float texels (row 0 at theta = 0).
-bool buildSteerable(const float *rgb, uint32_t W, uint32_t H, uint32_t level, SteerableHost &out, std::string &err);
+// The geometry of subdivision level `level` (<= 7), built on first use and kept for the life of
+// the process (thread-safe). Returns null with a message in err on failure.
+const SteerGeom *steerGeometry(uint32_t level, std::string &err);
 
 }  // namespace pg3

@@ -54,17 +54,18 @@ CASES = {
     "cornell_envarea_32_dmis": (lambda: S.cornell_env_area(32, 32, 64, 32), 12, "cdf", "dmis", 64, 128),
     "cornell_areabg_32": (lambda: S.cornell_box_bg(32, 32), 8, "cdf", "pt", 64, 128),
     # Phong, smooth conductor and smooth dielectric materials and a point light
-    # (src/materials.hxx:353-780, src/lights.hxx:232-343)
-    "cornell_mixed_32": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "pt", 64, 128),
-    "cornell_mixed_32_rr": (lambda: S.cornell_mixed(32, 32), 0, "cdf", "pt", 64, 128),
-    "cornell_mixed_32_point": (lambda: S.cornell_mixed(32, 32, area=False), 8, "cdf", "pt", 64, 128),
-    "cornell_mixed_32_naive": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "ptn", 64, 128),
-    "cornell_mixed_32_dmis": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dmis", 64, 128),
-    "cornell_mixed_32_dlsa": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dlsa", 64, 128),
-    "cornell_mixed_32_dlss": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dlss", 64, 128),
-    "cornell_mixed_32_dbs": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dbs", 64, 128),
-    "cornell_mixed_32_sb4_iic16": (lambda: S.cornell_mixed(32, 32), 0, "cdf", "pt", 64, 64, (4, 1.0, 1.0, 16.0)),
-    "cornell_envmixed_32_cdf": (lambda: S.cornell_env_mixed(32, 32, 64, 32), 12, "cdf", "pt", 64, 128),
+    # (src/materials.hxx:353-780, src/lights.hxx:232-343); glossy lobes and caustics are
+    # heavy-tailed: 256 renderers for the per-pixel variance of the mean
+    "cornell_mixed_32": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "pt", 256, 128),
+    "cornell_mixed_32_rr": (lambda: S.cornell_mixed(32, 32), 0, "cdf", "pt", 256, 128),
+    "cornell_mixed_32_point": (lambda: S.cornell_mixed(32, 32, area=False), 8, "cdf", "pt", 256, 128),
+    "cornell_mixed_32_naive": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "ptn", 256, 128),
+    "cornell_mixed_32_dmis": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dmis", 256, 128),
+    "cornell_mixed_32_dlsa": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dlsa", 256, 128),
+    "cornell_mixed_32_dlss": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dlss", 256, 128),
+    "cornell_mixed_32_dbs": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dbs", 256, 128),
+    "cornell_mixed_32_sb4_iic16": (lambda: S.cornell_mixed(32, 32), 0, "cdf", "pt", 256, 64, (4, 1.0, 1.0, 16.0)),
+    "cornell_envmixed_32_cdf": (lambda: S.cornell_env_mixed(32, 32, 64, 32), 12, "cdf", "pt", 256, 128),
 }
 
 EM_TOKEN = "@EM@"
