@@ -222,6 +222,14 @@ int pg3gpu_read_framebuffer(pg3gpu_ctx *ctx, double *mean_rgb, double *var_rgb, 
 /* Clears the framebuffer and the iteration counter. */
 int pg3gpu_clear_framebuffer(pg3gpu_ctx *ctx);
 
+/* Image files (Framebuffer::SaveBMP / SaveHDR, src/frame_buffer.hxx:114-200), the format by
+ * the extension as src/pg3render.cxx:266-273 chooses it: ".hdr" Radiance RGBE, anything else
+ * a 24-bit BMP of pow(value, 1/gamma) (the reference writes gamma 2.2). pg3gpu_write_image
+ * writes a caller's mean image (width*height*3 doubles, row 0 at the top; needs no context
+ * and no GPU); pg3gpu_save_image the context's current mean image. */
+int pg3gpu_write_image(const double *mean_rgb, uint32_t width, uint32_t height, const char *path, float gamma);
+int pg3gpu_save_image(pg3gpu_ctx *ctx, const char *path, float gamma);
+
 /* Number of samples per pixel accumulated so far (WasUsed() == (n > 0)). */
 uint64_t pg3gpu_iterations(const pg3gpu_ctx *ctx);
 
@@ -363,6 +371,8 @@ int pg3gpu_batch_synchronize(pg3gpu_batch *batch);
 int pg3gpu_batch_read_framebuffer(pg3gpu_batch *batch, uint32_t instance, double *mean_rgb, double *var_rgb,
                                   uint64_t *spp);
 int pg3gpu_batch_clear(pg3gpu_batch *batch);
+/* Instance `instance`'s mean image as a file, as pg3gpu_save_image. */
+int pg3gpu_batch_save_image(pg3gpu_batch *batch, uint32_t instance, const char *path, float gamma);
 /* Autotuner: times up to max_trials runs over capacities, refill thresholds and block shapes
  * (coordinate descent, graph launches), keeps the fastest tuning and writes it to *chosen
  * (may be NULL). The trial runs are cleared from the framebuffers afterwards. */

@@ -9,7 +9,9 @@
 // Render() does (src/pg3render.cxx:65-70, 112-128), and writes
 //   * the mean image over all K*N iterations (double RGB), and
 //   * the per-pixel variance of the K per-renderer means (for z-tests).
-// With --time it only renders and reports wall-clock Msamples/s.
+// With --time it only renders and reports wall-clock Msamples/s. --save-image P writes the
+// first renderer's framebuffer through the reference's own SaveBMP (gamma 2.2) or SaveHDR
+// (by P's extension, as src/pg3render.cxx:266-273) and its pixels to P.fb (double RGB).
 //
 // Scene file format (one record per line, '#' comments):
 //   camera px py pz  fx fy fz  ux uy uz  width height hfov_deg
@@ -191,6 +193,7 @@ int main(int argc, char **argv)
     const char *outPath = argv[2];
     int K = 8, N = 1, T = 0, seed = 1234;
     bool timeOnly = false;
+    std::string saveImage;
     AuxDbgParams aux;
     for (int i = 3; i < argc; ++i) {
         std::string a(argv[i]);
@@ -199,6 +202,7 @@ int main(int argc, char **argv)
         else if (a == "--threads") T = std::atoi(argv[++i]);
         else if (a == "--seed") seed = std::atoi(argv[++i]);
         else if (a == "--time") timeOnly = true;
+        else if (a == "--save-image") saveImage = argv[++i];
         else if (a == "--em-params") {
             aux.float1 = (float)std::atof(argv[++i]);
             aux.float2 = (float)std::atof(argv[++i]);
@@ -255,6 +259,24 @@ int main(int argc, char **argv)
     const double samples = (double)npx * K * N;
     std::printf("{\"seconds\": %.6f, \"samples\": %.0f, \"msamples_per_s\": %.6f, \"threads\": %d}\n",
                 secs, samples, samples / secs / 1e6, T);
+
+    if (!saveImage.empty()) {
+        Framebuffer fb;
+        renderers[0]->GetFramebuffer(fb);
+        const std::string ext = saveImage.substr(saveImage.size() - 3, 3);
+        if (ext == "bmp") fb.SaveBMP(saveImage.c_str(), 2.2f);
+        else if (ext == "hdr") fb.SaveHDR(saveImage.c_str());
+        else Fail("--save-image wants a .bmp or .hdr path");
+        const std::vector<FramebufferSpectrum> *rad = reinterpret_cast<const std::vector<FramebufferSpectrum> *>(&fb);
+        FILE *f = std::fopen((saveImage + ".fb").c_str(), "wb");
+        if (!f) Fail("cannot write the framebuffer dump");
+        for (size_t p = 0; p < npx; ++p)
+            for (int c = 0; c < 3; ++c) {
+                const double v = (*rad)[p].Get(c);
+                std::fwrite(&v, 8, 1, f);
+            }
+        std::fclose(f);
+    }
 
     if (!timeOnly) {
         std::vector<double> mean(npx * 3, 0.0), m2(npx * 3, 0.0);

@@ -102,6 +102,9 @@ SIGNATURES = {
     "pg3gpu_read_framebuffer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.POINTER(ctypes.c_uint64)]),
     "pg3gpu_clear_framebuffer": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg3gpu_write_image": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_char_p,
+                                          ctypes.c_float]),
+    "pg3gpu_save_image": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_float]),
     "pg3gpu_iterations": (ctypes.c_uint64, [ctypes.c_void_p]),
     "pg3gpu_render_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
                                              ctypes.c_void_p]),
@@ -133,6 +136,7 @@ SIGNATURES = {
     "pg3gpu_batch_read_framebuffer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
                                                      ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     "pg3gpu_batch_clear": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg3gpu_batch_save_image": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_float]),
     "pg3gpu_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(BatchTuning)]),
     "pg3gpu_batch_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "pg3gpu_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),

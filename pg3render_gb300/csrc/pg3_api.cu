@@ -479,6 +479,23 @@ int pg3gpu_read_framebuffer(pg3gpu_ctx *ctx, double *mean, double *var, uint64_t
     return PG3GPU_OK;
 }
 
+int pg3gpu_write_image(const double *rgb, uint32_t width, uint32_t height, const char *path, float gamma)
+{
+    std::string err;
+    const int st = writeImage(rgb, width, height, path, gamma, err);
+    return st ? fail(nullptr, st, "%s", err.c_str()) : PG3GPU_OK;
+}
+
+int pg3gpu_save_image(pg3gpu_ctx *ctx, const char *path, float gamma)
+{
+    if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
+    std::vector<double> mean((size_t)ctx->W * ctx->H * 3);
+    if (int st = pg3gpu_read_framebuffer(ctx, mean.data(), nullptr, nullptr)) return st;
+    std::string err;
+    const int st = writeImage(mean.data(), ctx->W, ctx->H, path, gamma, err);
+    return st ? fail(ctx, st, "%s", err.c_str()) : PG3GPU_OK;
+}
+
 int pg3gpu_clear_framebuffer(pg3gpu_ctx *ctx)
 {
     if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;

@@ -765,6 +765,16 @@ int pg3gpu_batch_read_framebuffer(pg3gpu_batch *b, uint32_t i, double *mean, dou
     return PG3GPU_OK;
 }
 
+int pg3gpu_batch_save_image(pg3gpu_batch *b, uint32_t i, const char *path, float gamma)
+{
+    if (!b) return PG3GPU_ERR_INVALID_ARGUMENT;
+    if (i >= b->inst.size()) return bfail(b, PG3GPU_ERR_INVALID_ARGUMENT, "instance out of range");
+    if (int st = pg3gpu_batch_synchronize(b)) return st;
+    const int st = pg3gpu_save_image(b->inst[i], path, gamma);
+    if (st) return bfail(b, st, pg3gpu_last_error(b->inst[i]));
+    return PG3GPU_OK;
+}
+
 int pg3gpu_batch_clear(pg3gpu_batch *b)
 {
     if (!b) return PG3GPU_ERR_INVALID_ARGUMENT;

@@ -32,6 +32,9 @@ struct HostScene {
     uint32_t numPointLights = 0;
 };
 
+// pg3_image.cpp: writes a mean image as BMP or Radiance HDR by the path's extension.
+int writeImage(const double *rgb, uint32_t width, uint32_t height, const char *path, float gamma, std::string &err);
+
 // Returns PG3GPU_OK or an error status with a message in err.
 int prepareScene(const pg3gpu_scene &scene, const pg3gpu_options &opts, HostScene &out, std::string &err);
 

@@ -10,6 +10,7 @@ reference reports with PG3_FATAL_ERROR raise :class:`Pg3Error` here.
 """
 import ctypes
 import dataclasses
+import os
 
 import numpy as np
 
@@ -17,6 +18,16 @@ from . import _lib
 from ._lib import (ALG_PATH_TRACING, ALG_PATH_TRACING_NAIVE, EM_CDF, EM_COSINE, EM_STEERABLE,  # noqa: F401
                    PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT, TRAVERSAL_AUTO, TRAVERSAL_BVH,
                    TRAVERSAL_LIST, Pg3Error)
+
+def write_image(mean_rgb, path, gamma=2.2):
+    """Writes an (H, W, 3) mean image as ``.hdr`` or a gamma-encoded 24-bit BMP (no GPU needed)."""
+    a = np.ascontiguousarray(mean_rgb, np.float64)
+    if a.ndim != 3 or a.shape[2] != 3:
+        raise ValueError("mean_rgb must be (height, width, 3)")
+    L = _lib.load()
+    _lib.check(L.pg3gpu_write_image(a.ctypes.data_as(ctypes.c_void_p), a.shape[1], a.shape[0], os.fsencode(path),
+                                    gamma), None)
+
 
 # Algorithm enum of src/config.hxx:23-34
 kEyeLight, kNormalVisualiser, kDirectIllumBsdfSampling, kDirectIllumLightSamplingAll, \
@@ -118,6 +129,11 @@ class GpuPathTracer:
 
     def clear(self):
         _lib.check(self._L.pg3gpu_clear_framebuffer(self._ctx), self._ctx)
+
+    def save_image(self, path, gamma=2.2):
+        """The mean image as ``.hdr`` (Radiance RGBE) or, for any other extension, a 24-bit BMP
+        with 1/gamma applied (the reference's main program writes gamma 2.2)."""
+        _lib.check(self._L.pg3gpu_save_image(self._ctx, os.fsencode(path), gamma), self._ctx)
 
     def render_samples(self, algorithm, iteration, spp):
         out = np.zeros((spp, self.height, self.width, 3), np.float32)
@@ -246,6 +262,9 @@ class GpuBatch:
 
     def clear(self):
         self._check(self._L.pg3gpu_batch_clear(self._b))
+
+    def save_image(self, i, path, gamma=2.2):
+        self._check(self._L.pg3gpu_batch_save_image(self._b, i, os.fsencode(path), gamma))
 
     def framebuffer(self, i, with_variance=False):
         h, w = self.sizes[i]

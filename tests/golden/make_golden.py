@@ -91,6 +91,30 @@ def make(name):
     print(name, "done", r["timing"])
 
 
+def make_image_writer():
+    """image_writer.npz: one reference renderer's framebuffer (16x12 Cornell box, 4 iterations)
+    and the files the reference's own Framebuffer::SaveBMP (gamma 2.2) and SaveHDR wrote from it."""
+    scene = S.cornell_box(16, 12)
+    text = scene.to_text(max_path_length=8)
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        for ext in ("bmp", "hdr"):
+            p = os.path.join(td, "img." + ext)
+            O.reference_render(text, renderers=1, iters=4, seed=777, extra=("--save-image", p))
+            with open(p, "rb") as f:
+                out[ext] = np.frombuffer(f.read(), np.uint8).copy()
+            out["fb_" + ext] = np.fromfile(p + ".fb", np.float64).reshape(12, 16, 3)
+    assert np.array_equal(out["fb_bmp"], out["fb_hdr"])
+    np.savez_compressed(os.path.join(HERE, "image_writer.npz"), framebuffer=out["fb_bmp"], bmp=out["bmp"],
+                        hdr=out["hdr"])
+    print("image_writer done")
+
+
 if __name__ == "__main__":
+    if "image_writer" in sys.argv[1:]:
+        make_image_writer()
+        sys.argv.remove("image_writer")
+        if len(sys.argv) == 1:
+            sys.exit(0)
     for n in (sys.argv[1:] or CASES):
         make(n)
