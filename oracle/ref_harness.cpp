@@ -9,7 +9,10 @@
 // Render() does (src/pg3render.cxx:65-70, 112-128), and writes
 //   * the mean image over all K*N iterations (double RGB), and
 //   * the per-pixel variance of the K per-renderer means (for z-tests).
-// With --time it only renders and reports wall-clock Msamples/s. --save-image P writes the
+// With --time it only renders and reports wall-clock Msamples/s. --preset ID W H EM replaces
+// the file's scene by the reference's own built-in scene number ID (Scene::LoadCornellBox with
+// g_SceneConfigs[ID], src/scene.hxx:176-1000, src/config.hxx:45-115) at W x H with environment
+// map type EM; the file then only supplies the options record. --save-image P writes the
 // first renderer's framebuffer through the reference's own SaveBMP (gamma 2.2) or SaveHDR
 // (by P's extension, as src/pg3render.cxx:266-273) and its pixels to P.fb (double RGB).
 //
@@ -194,6 +197,7 @@ int main(int argc, char **argv)
     int K = 8, N = 1, T = 0, seed = 1234;
     bool timeOnly = false;
     std::string saveImage;
+    int presetId = -1, presetW = 0, presetH = 0, presetEm = 0;
     AuxDbgParams aux;
     for (int i = 3; i < argc; ++i) {
         std::string a(argv[i]);
@@ -203,6 +207,12 @@ int main(int argc, char **argv)
         else if (a == "--seed") seed = std::atoi(argv[++i]);
         else if (a == "--time") timeOnly = true;
         else if (a == "--save-image") saveImage = argv[++i];
+        else if (a == "--preset") {
+            presetId = std::atoi(argv[++i]);
+            presetW = std::atoi(argv[++i]);
+            presetH = std::atoi(argv[++i]);
+            presetEm = std::atoi(argv[++i]);
+        }
         else if (a == "--em-params") {
             aux.float1 = (float)std::atof(argv[++i]);
             aux.float2 = (float)std::atof(argv[++i]);
@@ -212,6 +222,13 @@ int main(int argc, char **argv)
     if (T <= 0) T = omp_get_num_procs();
 
     SceneFile sf = LoadScene(scenePath, aux);
+    if (presetId >= 0) {
+        if (presetId >= (int)(sizeof(g_SceneConfigs) / sizeof(g_SceneConfigs[0]))) Fail("preset id out of range");
+        delete sf.scene;
+        sf.scene = new Scene;
+        sf.scene->LoadCornellBox(Vec2i(presetW, presetH), aux, g_SceneConfigs[presetId],
+                                 Scene::EnvironmentMapType(presetEm));
+    }
 
     // Options as the reference's Config carries them (src/config.hxx:1100-1137); -sb 1 -iic 0
     // unless the scene file's options record gives them.

@@ -41,7 +41,10 @@ def scene_from_golden(d):
     from pg3render_gb300 import scene as S
     text = str(d["scene_text"])
     name = text.splitlines()[0][2:].strip()
-    if name.startswith("cornell_mixed_area_point_"):
+    if name.startswith("reference_scene_"):
+        from pg3render_gb300 import presets as PR
+        s = PR.reference_scene(int(name.split("_")[2]), 32, 32)
+    elif name.startswith("cornell_mixed_area_point_"):
         s = S.cornell_mixed(32, 32)
     elif name.startswith("cornell_mixed_point_"):
         s = S.cornell_mixed(32, 32, area=False)

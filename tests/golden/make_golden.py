@@ -68,6 +68,24 @@ CASES = {
     "cornell_envmixed_32_cdf": (lambda: S.cornell_env_mixed(32, 32, 64, 32), 12, "cdf", "pt", 256, 128),
 }
 
+# The reference's own built-in scenes (Scene::LoadCornellBox, -s ids of src/config.hxx:45-115):
+# the reference renders the scene it builds itself, the tests render pg3render_gb300.presets' build
+# name: (scene id, max_path_length, algorithm, renderers, iterations)
+PRESET_CASES = {
+    "preset_00": (0, 8, "pt", 64, 128),      # point light, Phong diffuse box
+    "preset_01": (1, 8, "pt", 256, 128),     # point light, Phong glossy box
+    "preset_03": (3, 8, "pt", 64, 128),      # ceiling light, glossy
+    "preset_05": (5, 8, "pt", 256, 128),      # light box, glossy
+    "preset_07": (7, 8, "pt", 64, 128),      # constant environment, glossy
+    "preset_12": (12, 8, "pt", 64, 128),     # point + light box + environment
+    "preset_16": (16, 8, "pt", 256, 128),    # point light, smooth conductor spheres
+    "preset_19": (19, 8, "pt", 256, 128),     # light box, smooth conductors, glossy walls
+    "preset_29": (29, 8, "pt", 64, 128),     # environment, rectangles, GGX dielectric
+    "preset_31": (31, 8, "pt", 256, 128),    # light box, smooth dielectric sphere in the box
+    "preset_38": (38, 8, "pt", 64, 128),     # layered sphere (GGX dielectric around a GGX conductor)
+    "preset_12_dmis": (12, 8, "dmis", 64, 128),
+}
+
 EM_TOKEN = "@EM@"
 
 
@@ -88,6 +106,22 @@ def make(name):
         mean=r["mean"], var_mean=r["var_of_renderer_mean"] / K, spp=np.array(K * N),
         max_path_length=np.array(maxpl), em_sampler=np.array(sampler), algorithm=np.array(alg),
         splitting=np.array(splitting if splitting is not None else (1, 1.0, 1.0, 0.0), np.float64))
+    print(name, "done", r["timing"])
+
+
+def make_preset(name):
+    from pg3render_gb300 import presets as PR
+    sid, maxpl, alg, K, N = PRESET_CASES[name]
+    scene = PR.reference_scene(sid, 32, 32)
+    text = scene.to_text(algorithm=alg, max_path_length=maxpl)
+    opts = "options %s 1 %d\n" % (alg, maxpl)
+    r = O.reference_render(opts, renderers=K, iters=N, seed=4321, extra=("--preset", str(sid), "32", "32", "0"))
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        scene_text=np.array(text), env_map=np.zeros((0, 0, 3), np.float32),
+        mean=r["mean"], var_mean=r["var_of_renderer_mean"] / K, spp=np.array(K * N),
+        max_path_length=np.array(maxpl), em_sampler=np.array("cdf"), algorithm=np.array(alg),
+        splitting=np.array((1, 1.0, 1.0, 0.0), np.float64))
     print(name, "done", r["timing"])
 
 
@@ -116,5 +150,8 @@ if __name__ == "__main__":
         sys.argv.remove("image_writer")
         if len(sys.argv) == 1:
             sys.exit(0)
-    for n in (sys.argv[1:] or CASES):
+    names = sys.argv[1:] or (list(CASES) + list(PRESET_CASES))
+    for n in [x for x in names if x in PRESET_CASES]:
+        make_preset(n)
+    for n in [x for x in names if x not in PRESET_CASES]:
         make(n)

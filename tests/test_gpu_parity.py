@@ -24,7 +24,10 @@ GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr"
                 "cornell_envarea_32_cdf", "cornell_envarea_32_dmis", "cornell_areabg_32",
                 "cornell_mixed_32", "cornell_mixed_32_rr", "cornell_mixed_32_point", "cornell_mixed_32_naive",
                 "cornell_mixed_32_dmis", "cornell_mixed_32_dlsa", "cornell_mixed_32_dlss", "cornell_mixed_32_dbs",
-                "cornell_mixed_32_sb4_iic16", "cornell_envmixed_32_cdf"]
+                "cornell_mixed_32_sb4_iic16", "cornell_envmixed_32_cdf",
+                # the reference's own built-in scenes (-s ids), built here by pg3render_gb300.presets
+                "preset_00", "preset_01", "preset_03", "preset_05", "preset_07", "preset_12", "preset_16",
+                "preset_19", "preset_29", "preset_31", "preset_38", "preset_12_dmis"]
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
 # the reference's acronyms of its algorithm ids (src/config.hxx:147-170)
 ALG_IDS = {"el": 0, "nv": 1, "dbs": 2, "dlsa": 3, "dlss": 4, "dmis": 5, "ptn": 6, "pt": 7}
@@ -175,6 +178,22 @@ def test_mixed_materials_and_point_light_path_by_path(case, tmp_path):
         se = np.sqrt(g.var(axis=0) / len(g) + o.var(axis=0) / len(o))
         assert np.all(np.abs(g.mean(axis=0) - o.mean(axis=0)) <= 5 * se), (g.mean(axis=0), o.mean(axis=0), se)
         return
+    o = _oracle_samples(scene, text, 8, seed, 0)
+    frac = _match_fraction(g, o)
+    assert frac >= MIN_MATCH, "only %.4f of samples match the oracle" % frac
+    assert np.isfinite(g).all() and g.max() > 0
+
+
+@pytest.mark.parametrize("sid", [1, 5, 12, 16, 29, 31, 36, 38])
+def test_reference_scenes_path_by_path(sid, tmp_path):
+    """The reference's built-in scenes (presets) through the wavefront pipeline, against the
+    oracle sample by sample."""
+    from pg3render_gb300 import presets as PR
+    scene = PR.reference_scene(sid, 24, 24)
+    text = scene.to_text(max_path_length=8)
+    seed = 61
+    with P.GpuPathTracer(_cfg(scene, 8), seed=seed) as r:
+        g = r.render_samples(P.renderer.kPathTracing, 0, 8)
     o = _oracle_samples(scene, text, 8, seed, 0)
     frac = _match_fraction(g, o)
     assert frac >= MIN_MATCH, "only %.4f of samples match the oracle" % frac

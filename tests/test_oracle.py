@@ -24,7 +24,10 @@ GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr"
                 "cornell_envarea_32_cdf", "cornell_envarea_32_dmis", "cornell_areabg_32",
                 "cornell_mixed_32", "cornell_mixed_32_rr", "cornell_mixed_32_point", "cornell_mixed_32_naive",
                 "cornell_mixed_32_dmis", "cornell_mixed_32_dlsa", "cornell_mixed_32_dlss", "cornell_mixed_32_dbs",
-                "cornell_mixed_32_sb4_iic16", "cornell_envmixed_32_cdf"]
+                "cornell_mixed_32_sb4_iic16", "cornell_envmixed_32_cdf",
+                # the reference's own built-in scenes (-s ids), built here by pg3render_gb300.presets
+                "preset_00", "preset_01", "preset_03", "preset_05", "preset_07", "preset_12", "preset_16",
+                "preset_19", "preset_29", "preset_31", "preset_38", "preset_12_dmis"]
 # the visualisers are deterministic inside a surface (zero variance): only the fraction of
 # |z| <= 4 is a meaningful statistic for them
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
@@ -50,7 +53,9 @@ def test_oracle_matches_reference_golden(name):
            "cornell_env_32_dbs": 8192, "cornell_mixed_32_naive": 8192, "cornell_mixed_32_dbs": 8192,
            # glossy Phong lobes lit by a point light, caustics through smooth glass: heavy tails
            "cornell_mixed_32": 8192, "cornell_mixed_32_rr": 8192, "cornell_mixed_32_point": 8192,
-           "cornell_envmixed_32_cdf": 8192}.get(name, 1024)
+           "cornell_envmixed_32_cdf": 8192,
+           "preset_00": 8192, "preset_03": 8192, "preset_07": 8192, "preset_29": 8192, "preset_01": 32768,
+           "preset_05": 32768, "preset_16": 32768, "preset_19": 32768, "preset_31": 32768}.get(name, 1024)
     o = O.render(text, 32, 32, seed=99, spp=spp, em_sampler=sampler)
     m = o["sum"] / spp
     v = np.maximum(o["sumsq"] / spp - m * m, 0.0) / spp
