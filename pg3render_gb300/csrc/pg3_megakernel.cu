@@ -51,26 +51,24 @@ __global__ void __launch_bounds__(kMegaBlock) megakernel(const __grid_constant__
 }
 
 // Adds `passes` samples per pixel from the per-sample buffer into the fp64
-// framebuffer accumulators (sum and sum of squares). Samples are summed in fp32
-// in groups of 32 and the group sums in fp64, which keeps the fp64 work at 1/32.
+// framebuffer accumulators (sum and sum of squares).
 __global__ void __launch_bounds__(256) accumulateKernel(uint32_t npix, uint32_t passes, const float *__restrict__ inR,
                                                          const float *__restrict__ inG, const float *__restrict__ inB,
                                                          double *__restrict__ sum, double *__restrict__ sumsq)
 {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npix) return;
+    // every sample is added in fp64, as the reference's framebuffer adds each iteration's
+    // radiance (src/frame_buffer.hxx:30-77): the sum of identical samples stays exact
     double s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
-    for (uint32_t k0 = 0; k0 < passes; k0 += 32) {
-        float fs[3] = {0, 0, 0}, fq[3] = {0, 0, 0};
-        const uint32_t k1 = min(passes, k0 + 32);
-        for (uint32_t k = k0; k < k1; ++k) {
-            const size_t idx = (size_t)k * npix + p;
-            const float v[3] = {inR[idx], inG[idx], inB[idx]};
+    for (uint32_t k = 0; k < passes; ++k) {
+        const size_t idx = (size_t)k * npix + p;
+        const double v[3] = {inR[idx], inG[idx], inB[idx]};
 #pragma unroll
-            for (int c = 0; c < 3; ++c) { fs[c] += v[c]; fq[c] += v[c] * v[c]; }
+        for (int c = 0; c < 3; ++c) {
+            s[c] += v[c];
+            q[c] = fma(v[c], v[c], q[c]);
         }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) { s[c] += fs[c]; q[c] += fq[c]; }
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {

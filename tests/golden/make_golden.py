@@ -82,7 +82,7 @@ PRESET_CASES = {
     "preset_19": (19, 8, "pt", 256, 128),     # light box, smooth conductors, glossy walls
     "preset_29": (29, 8, "pt", 64, 128),     # environment, rectangles, GGX dielectric
     "preset_31": (31, 8, "pt", 256, 128),    # light box, smooth dielectric sphere in the box
-    "preset_38": (38, 8, "pt", 64, 128),     # layered sphere (GGX dielectric around a GGX conductor)
+    "preset_38": (38, 8, "pt", 256, 128),     # layered sphere (GGX dielectric around a GGX conductor)
     "preset_12_dmis": (12, 8, "dmis", 64, 128),
 }
 

@@ -55,7 +55,8 @@ def test_oracle_matches_reference_golden(name):
            "cornell_mixed_32": 8192, "cornell_mixed_32_rr": 8192, "cornell_mixed_32_point": 8192,
            "cornell_envmixed_32_cdf": 8192,
            "preset_00": 8192, "preset_03": 8192, "preset_07": 8192, "preset_29": 8192, "preset_01": 32768,
-           "preset_05": 32768, "preset_16": 32768, "preset_19": 32768, "preset_31": 32768}.get(name, 1024)
+           "preset_05": 32768, "preset_16": 32768, "preset_19": 32768, "preset_31": 32768,
+           "preset_38": 32768}.get(name, 1024)
     o = O.render(text, 32, 32, seed=99, spp=spp, em_sampler=sampler)
     m = o["sum"] / spp
     v = np.maximum(o["sumsq"] / spp - m * m, 0.0) / spp
