@@ -318,9 +318,9 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
         a.nodeChild = sv.nodeChild;
         a.numLayers = (uint32_t)g.layerStart.size() - 1;
         for (uint32_t l = 0; l <= a.numLayers; ++l) a.layerStart[l] = g.layerStart[l];
-        if ((st = devAlloc(ctx, &a.vw, 9 * (size_t)a.numVertices))) return bail(st);
+        if ((st = devAlloc(ctx, &a.vw, 12 * (size_t)a.numVertices))) return bail(st);
         if ((st = devAlloc(ctx, &a.leafW, 9 * (size_t)a.numLeaves))) return bail(st);
-        if ((st = devAlloc(ctx, &a.nodeW, 54 * (size_t)g.numNodes()))) return bail(st);
+        if ((st = devAlloc(ctx, &a.nodeW, 72 * (size_t)g.numNodes()))) return bail(st);
         a.rootW = reinterpret_cast<float *>(const_cast<float4 *>(sv.leafPlane) + rootAt);
         sv.vw = a.vw;
         sv.nodeW = a.nodeW;

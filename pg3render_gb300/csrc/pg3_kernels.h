@@ -55,7 +55,7 @@ struct SteerWeightArgs {
     const int *nodeChild;
     uint32_t layerStart[kSteerMaxLayers + 1];    // tree layers bottom-up, node ranges
     uint32_t numLayers;
-    float *vw, *leafW, *nodeW, *rootW;           // outputs (9 / 9 / 54 floats per item, 9)
+    float *vw, *leafW, *nodeW, *rootW;           // outputs (12 / 9 / 72 floats per item, 9)
 };
 cudaError_t launchSteerWeights(const SteerWeightArgs &args, cudaStream_t stream);
 

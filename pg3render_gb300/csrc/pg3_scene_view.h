@@ -57,10 +57,10 @@ struct BvhNode {
 // Steerable sampler tables (host build in pg3_steerable.cpp, sampling in pg3_steer.cuh).
 struct SteerView {
     const float4 *vdir;       // per vertex: unit direction xyz
-    const float *vw;          // per vertex: 9 SH basis values scaled by the map's luminance
+    const float *vw;          // per vertex: 9 SH basis values scaled by the map's luminance (padded to 12)
     const int4 *tri;          // vertex ids of the triangles of every subdivision level
-    const float *nodeW;       // per 6-ary tree node: 6 children x 9 summed weights
-    const int *nodeChild;     // per node: 6 child ids (>= 0 node, < 0 ~leaf, INT_MIN none)
+    const float *nodeW;       // per 6-ary tree node: 9 coefficients x 8 child slots of summed weights
+    const int *nodeChild;     // per node: 8 child slots (>= 0 node, < 0 ~leaf, INT_MIN none)
     const float4 *leafPlane;  // per leaf: unit plane normal, distance from the origin; followed in the
                               // same allocation by the leaf-locator tables (pg3_steer.cuh)
     const int4 *faceCells;    // cube-map cells: up to 4 candidate level-0 faces (-1 none)

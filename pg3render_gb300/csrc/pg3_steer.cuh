@@ -66,7 +66,17 @@ PG3_DI const float *steerRootW(const SteerView &T)
 PG3_DI float steerTotal(const SteerView &T, const float c[9]) { return fmaxf(dot9(steerRootW(T), c), 0.f); }
 
 PG3_DI float3 vdir(const SteerView &T, int v) { return xyz(__ldg(&T.vdir[v])); }
-PG3_DI float vval(const SteerView &T, int v, const float c[9]) { return fmaxf(dot9(&T.vw[v * 9], c), 0.f); }
+// a vertex's value: its 9 weights (padded to 12 floats, three vector loads) dotted with c
+PG3_DI float vval(const SteerView &T, int v, const float c[9])
+{
+    const float4 *w = reinterpret_cast<const float4 *>(T.vw) + 3 * v;
+    const float4 a = __ldg(&w[0]), b = __ldg(&w[1]), d = __ldg(&w[2]);
+    float s = 0.f;
+    s += a.x * c[0]; s += a.y * c[1]; s += a.z * c[2]; s += a.w * c[3];
+    s += b.x * c[4]; s += b.y * c[5]; s += b.z * c[6]; s += b.w * c[7];
+    s += d.x * c[8];
+    return fmaxf(s, 0.f);
+}
 
 // base density of the point p = b0 A + b1 B + b2 C of leaf `leaf` (vertex values v).
 PG3_DI float steerLeafPdf(const SteerView &T, int leaf, float3 p, float g, float Z)
@@ -211,12 +221,23 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     float u = u0;
     int leaf = -1;
     for (int depth = 0; depth < 32; ++depth) {
+        // a node: 8 child slots (two int4) and its weights coefficient-major (9 x two float4)
+        const int4 *ch4 = reinterpret_cast<const int4 *>(T.nodeChild) + 2 * node;
+        const int4 ia = __ldg(&ch4[0]), ib = __ldg(&ch4[1]);
+        const int ids[6] = {ia.x, ia.y, ia.z, ia.w, ib.x, ib.y};
+        const float4 *w4 = reinterpret_cast<const float4 *>(T.nodeW) + 18 * node;
+        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const float4 a = __ldg(&w4[2 * k]);
+            const float2 b = __ldg(reinterpret_cast<const float2 *>(&w4[2 * k + 1]));
+            acc[0] += a.x * c[k]; acc[1] += a.y * c[k]; acc[2] += a.z * c[k]; acc[3] += a.w * c[k];
+            acc[4] += b.x * c[k]; acc[5] += b.y * c[k];
+        }
         float val[6], cum = 0.f;
-        int ids[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
-            ids[i] = __ldg(&T.nodeChild[node * 6 + i]);
-            val[i] = (ids[i] != INT_MIN) ? fmaxf(dot9(&T.nodeW[(node * 6 + i) * 9], c), 0.f) : 0.f;
+            val[i] = (ids[i] != INT_MIN) ? fmaxf(acc[i], 0.f) : 0.f;
             cum += val[i];
         }
         // children occupy the first slots; the first one whose running sum exceeds t wins,

@@ -5,10 +5,12 @@
 //
 // vertex weight   vw[v][k]  = Y_k(d_v) * L(d_v)         (src/em_steerable_sampler.hxx:181-202, 3084-3095)
 // leaf weight     lw[t][k]  = area_t * mean of its three vertex weights           (:1277-1296)
-// node weight     nodeW[n][c][k] = the summed weight of child c                    (:3755-3793)
+// node weight     nodeW[n][k][c] = the summed weight of child c                    (:3755-3793)
 // whole sphere    rootW[k]  = sum over all leaves of lw[t][k]
 // with Y the 9 real SH basis functions (Ramamoorthi & Hanrahan 2001) and L the luminance of
 // the map's bilinear (tent) lookup in the vertex direction (src/em_image.hxx:95-143).
+// Layouts for vector loads: a vertex's 9 weights padded to 12 floats (three float4), a node's
+// weights coefficient-major over 8 child slots (9 x 8 floats, two float4 per coefficient).
 #include <climits>
 
 #include "pg3_kernels.h"
@@ -48,7 +50,7 @@ __global__ void vertexWeightsKernel(const float4 *em, uint32_t W, uint32_t H, co
     const float bot = (1.f - xl) * texelLum(em, W, H, x0, cy) + xl * texelLum(em, W, H, cx, cy);
     const float L = (1.f - yl) * top + yl * bot;
     const float x = d.x, y = d.y, z = d.z;
-    float *o = vw + 9 * (size_t)i;
+    float *o = vw + 12 * (size_t)i;
     o[0] = L * 0.282095f;
     o[1] = L * 0.488603f * y;
     o[2] = L * 0.488603f * z;
@@ -58,6 +60,7 @@ __global__ void vertexWeightsKernel(const float4 *em, uint32_t W, uint32_t H, co
     o[6] = L * 0.315392f * (3.f * z * z - 1.f);
     o[7] = L * 1.092548f * x * z;
     o[8] = L * 0.546274f * (x * x - y * y);
+    o[9] = o[10] = o[11] = 0.f;
 }
 
 __global__ void leafWeightsKernel(const int4 *leafTri, const float *leafArea, uint32_t nLeaf, const float *vw,
@@ -69,17 +72,17 @@ __global__ void leafWeightsKernel(const int4 *leafTri, const float *leafArea, ui
     const float a = leafArea[i] * (1.f / 3.f);
 #pragma unroll
     for (int k = 0; k < 9; ++k)
-        lw[9 * (size_t)i + k] = a * (vw[9 * (size_t)t.x + k] + vw[9 * (size_t)t.y + k] + vw[9 * (size_t)t.z + k]);
+        lw[9 * (size_t)i + k] = a * (vw[12 * (size_t)t.x + k] + vw[12 * (size_t)t.y + k] + vw[12 * (size_t)t.z + k]);
 }
 
 // One tree layer: every child slot of nodes [n0, n1) gets its child's summed weight (a leaf's
-// weight, or the sum of a lower node's six child slots, written by the previous launch).
+// weight, or the sum of a lower node's child slots, written by the previous launch).
 __global__ void treeLayerKernel(const int *nodeChild, uint32_t n0, uint32_t n1, const float *lw, float *nodeW)
 {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= 6 * (n1 - n0)) return;
-    const uint32_t n = n0 + j / 6, c = j % 6;
-    const int ch = nodeChild[6 * (size_t)n + c];
+    if (j >= 8 * (n1 - n0)) return;
+    const uint32_t n = n0 + j / 8, c = j % 8;
+    const int ch = nodeChild[8 * (size_t)n + c];
     float w[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) w[k] = 0.f;
@@ -88,13 +91,13 @@ __global__ void treeLayerKernel(const int *nodeChild, uint32_t n0, uint32_t n1, 
 #pragma unroll
             for (int k = 0; k < 9; ++k) w[k] = lw[9 * (size_t)(~ch) + k];
         } else {
-            for (int cc = 0; cc < 6; ++cc)
+            for (int cc = 0; cc < 8; ++cc)
 #pragma unroll
-                for (int k = 0; k < 9; ++k) w[k] += nodeW[54 * (size_t)ch + 9 * cc + k];
+                for (int k = 0; k < 9; ++k) w[k] += nodeW[72 * (size_t)ch + 8 * k + cc];
         }
     }
 #pragma unroll
-    for (int k = 0; k < 9; ++k) nodeW[54 * (size_t)n + 9 * c + k] = w[k];
+    for (int k = 0; k < 9; ++k) nodeW[72 * (size_t)n + 8 * k + c] = w[k];
 }
 
 // Whole-sphere weights: one block, fp64 partial sums over all leaves.
@@ -131,7 +134,7 @@ cudaError_t launchSteerWeights(const SteerWeightArgs &a, cudaStream_t st)
     for (uint32_t l = 0; l < a.numLayers; ++l) {
         const uint32_t n0 = a.layerStart[l], n1 = a.layerStart[l + 1];
         if (n1 <= n0) return cudaErrorInvalidValue;
-        treeLayerKernel<<<(6 * (n1 - n0) + 127) / 128, 128, 0, st>>>(a.nodeChild, n0, n1, a.leafW, a.nodeW);
+        treeLayerKernel<<<(8 * (n1 - n0) + 127) / 128, 128, 0, st>>>(a.nodeChild, n0, n1, a.leafW, a.nodeW);
     }
     rootWeightsKernel<<<1, 256, 0, st>>>(a.leafW, a.numLeaves, a.rootW);
     return cudaGetLastError();

@@ -127,15 +127,16 @@ bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
     std::vector<int> layer(nLeaf);
     for (uint32_t i = 0; i < nLeaf; ++i) layer[i] = ~(int)i;
     do {
-        out.layerStart.push_back((uint32_t)(out.nodeChild.size() / 6));
+        out.layerStart.push_back((uint32_t)(out.nodeChild.size() / 8));
         std::vector<int> up;
         for (size_t s = 0; s < layer.size(); s += 6) {
-            up.push_back((int)(out.nodeChild.size() / 6));
-            for (size_t c = 0; c < 6; ++c) out.nodeChild.push_back(s + c < layer.size() ? layer[s + c] : INT_MIN);
+            up.push_back((int)(out.nodeChild.size() / 8));
+            for (size_t c = 0; c < 8; ++c)
+                out.nodeChild.push_back(c < 6 && s + c < layer.size() ? layer[s + c] : INT_MIN);
         }
         layer.swap(up);
     } while (layer.size() > 1);
-    out.layerStart.push_back((uint32_t)(out.nodeChild.size() / 6));
+    out.layerStart.push_back((uint32_t)(out.nodeChild.size() / 8));
     out.root = layer[0];
 
     // leaf locator: inward edge normals of every leaf, and for every cell of a finer cube map

@@ -43,7 +43,8 @@ struct SteerGeom {
     std::vector<int4> tri;             // vertex ids of every triangle of every level (level 0 first)
     std::vector<uint32_t> levelOffset; // first triangle of each level in `tri` (level+1 entries + end)
     std::vector<float> leafArea;       // planar area of every leaf triangle
-    std::vector<int> nodeChild;        // 6 child ids per node: >= 0 node, < 0 ~leaf, INT32_MIN none
+    std::vector<int> nodeChild;        // 8 child slots per node (6 used, two int4 loads): >= 0 node,
+                                       // < 0 ~leaf, INT32_MIN none
     std::vector<uint32_t> layerStart;  // first node of every tree layer, bottom (parents of leaves)
                                        // first, then the end of the node list
     std::vector<float4> leafPlane;     // per leaf: unit normal of the planar triangle, distance from origin
@@ -54,7 +55,7 @@ struct SteerGeom {
     uint32_t leafGrid = 0;
     int root = 0;
     uint32_t numLeaves() const { return (uint32_t)leafArea.size(); }
-    uint32_t numNodes() const { return (uint32_t)(nodeChild.size() / 6); }
+    uint32_t numNodes() const { return (uint32_t)(nodeChild.size() / 8); }
 };
 
 constexpr int kSteerCells = 8;         // cube-map resolution of the face locator
