@@ -11,7 +11,9 @@
 // then p with density proportional to g_T on the planar triangle, then w = p/|p|;
 // its pdf is exactly base(w). Directions below the horizon are mirrored through
 // the origin as in the reference (:2196-2208), so the returned pdf is
-// base(w) + base(-w) for both sampled and evaluated directions.
+// base(w) + base(-w) for both sampled and evaluated directions. The triangulation is
+// centrally symmetric: -w lies in the leaf of the antipodal vertices at the same barycentric
+// coordinates and the same r / d_T, so base(-w) needs only those vertices' values.
 #pragma once
 
 #include <climits>
@@ -176,8 +178,11 @@ PG3_DI int steerLocate(const SteerView &T, float3 w)
     return steerLocateFaces(T, w);
 }
 
-// base(w) for any direction.
-PG3_DI float steerBasePdf(const SteerView &T, float3 w, const float c[9], float Z)
+PG3_DI int antipode(float4 v) { return __float_as_int(v.w); }
+
+// base(w) + base(-w): w's leaf, w's barycentric coordinates there, and the values of the
+// leaf's vertices and of their antipodes.
+PG3_DI float steerPairPdf(const SteerView &T, float3 w, const float c[9], float Z)
 {
     const int leaf = steerLocate(T, w);
     const int4 tri = __ldg(&T.tri[T.levelOff[T.level] + leaf]);
@@ -185,7 +190,8 @@ PG3_DI float steerBasePdf(const SteerView &T, float3 w, const float c[9], float 
     const float3 nT = xyz(pl);
     const float dw = dot(nT, w);
     if (!(dw > 0.f)) return 0.f;
-    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
+    const float4 A4 = __ldg(&T.vdir[tri.x]), B4 = __ldg(&T.vdir[tri.y]), C4 = __ldg(&T.vdir[tri.z]);
+    const float3 A = xyz(A4), B = xyz(B4), C = xyz(C4);
     const float3 p = w * (pl.w / dw);            // w meets the leaf's plane
     const float3 n = cross(B - A, C - A);
     const float nn = dot(n, n);
@@ -193,7 +199,8 @@ PG3_DI float steerBasePdf(const SteerView &T, float3 w, const float c[9], float 
     const float b1 = dot(cross(C - p, A - p), n) / nn;
     const float b2 = 1.f - b0 - b1;
     const float g = b0 * vval(T, tri.x, c) + b1 * vval(T, tri.y, c) + b2 * vval(T, tri.z, c);
-    return steerLeafPdf(T, leaf, p, g, Z);
+    const float ga = b0 * vval(T, antipode(A4), c) + b1 * vval(T, antipode(B4), c) + b2 * vval(T, antipode(C4), c);
+    return steerLeafPdf(T, leaf, p, g, Z) + steerLeafPdf(T, leaf, p, ga, Z);
 }
 
 // Pdf of the mirrored-hemisphere sampler for a direction above the surface (front side).
@@ -204,7 +211,7 @@ PG3_DI float steerPdf(const SteerView &T, float3 w, float3 n)
     steerCoeffs(n, c);
     const float Z = steerTotal(T, c);
     if (!(Z > 0.f)) return 0.f;
-    return steerBasePdf(T, w, c, Z) + steerBasePdf(T, -w, c, Z);
+    return steerPairPdf(T, w, c, Z);
 }
 
 // Samples a direction in the upper hemisphere of n. Returns false when the map is black.
@@ -263,6 +270,7 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     // probability v_i / sum, then barycentric b_i from its marginal 6b(1-b) (inverse of
     // 3b^2 - 2b^3), the other two uniformly along the remaining segment
     const int4 tri = __ldg(&T.tri[T.levelOff[T.level] + leaf]);
+    const float4 A4 = __ldg(&T.vdir[tri.x]), B4 = __ldg(&T.vdir[tri.y]), C4 = __ldg(&T.vdir[tri.z]);
     const float v0 = vval(T, tri.x, c), v1 = vval(T, tri.y, c), v2 = vval(T, tri.z, c);
     const float vs = v0 + v1 + v2;
     const float ts = u * vs;
@@ -274,9 +282,11 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     if (corner == 0) { b0 = bi; b1 = bj; b2 = bk; }
     else if (corner == 1) { b1 = bi; b2 = bj; b0 = bk; }
     else { b2 = bi; b0 = bj; b1 = bk; }
-    const float3 p = vdir(T, tri.x) * b0 + vdir(T, tri.y) * b1 + vdir(T, tri.z) * b2;
+    const float3 p = xyz(A4) * b0 + xyz(B4) * b1 + xyz(C4) * b2;
     const float3 w0 = normalize(p);
-    pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) + steerBasePdf(T, -w0, c, Z);
+    // -w0 lies in the antipodal leaf at the same barycentric coordinates
+    const float ga = b0 * vval(T, antipode(A4), c) + b1 * vval(T, antipode(B4), c) + b2 * vval(T, antipode(C4), c);
+    pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) + steerLeafPdf(T, leaf, p, ga, Z);
     float cosIn = dot(w0, n);
     wig = w0;
     if (cosIn < 0.f) { wig = -w0; cosIn = -cosIn; }

@@ -8,7 +8,9 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <cstring>
 #include <thread>
+#include <tuple>
 #include <utility>
 
 namespace pg3 {
@@ -106,6 +108,20 @@ bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
     out.levelOffset.push_back((uint32_t)out.tri.size());
     out.vdir.resize(v.size());
     for (size_t i = 0; i < v.size(); ++i) out.vdir[i] = make_float4((float)v[i].x, (float)v[i].y, (float)v[i].z, 0.f);
+    // antipodal vertices: negation commutes with the midpoint normalisation, so -v is a vertex
+    // with exactly the negated coordinates
+    {
+        std::map<std::tuple<float, float, float>, int> byDir;
+        for (size_t i = 0; i < v.size(); ++i) byDir[std::make_tuple(out.vdir[i].x, out.vdir[i].y, out.vdir[i].z)] = (int)i;
+        for (size_t i = 0; i < v.size(); ++i) {
+            const auto it = byDir.find(std::make_tuple(-out.vdir[i].x, -out.vdir[i].y, -out.vdir[i].z));
+            if (it == byDir.end()) { err = "steerable triangulation is not centrally symmetric"; return false; }
+            int bits = it->second;
+            float w;
+            std::memcpy(&w, &bits, sizeof w);
+            out.vdir[i].w = w;
+        }
+    }
 
     // leaves: planar area (the leaf weight is area x mean vertex weight,
     // src/em_steerable_sampler.hxx:1277-1296) and plane (unit normal, distance) for the

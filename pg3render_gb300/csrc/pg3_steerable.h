@@ -39,7 +39,8 @@ namespace pg3 {
 
 struct SteerGeom {
     uint32_t level = 0;
-    std::vector<float4> vdir;          // vertex directions
+    std::vector<float4> vdir;          // vertex directions; w: the id of the antipodal vertex (int bits;
+                                       // the subdivided icosahedron is centrally symmetric)
     std::vector<int4> tri;             // vertex ids of every triangle of every level (level 0 first)
     std::vector<uint32_t> levelOffset; // first triangle of each level in `tri` (level+1 entries + end)
     std::vector<float> leafArea;       // planar area of every leaf triangle
