@@ -167,6 +167,30 @@ PG3_DI void flushBlockGrad(const float *sGrad, uint32_t nmat, float *gMat)
 // ------------------------------------------------------------------------------------------
 // one vertex
 // ------------------------------------------------------------------------------------------
+PG3_DI void prefetchL1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// Software pipelining of a shade kernel's grid-stride loop: while a thread shades one entry of
+// its bucket it pulls the next entry's ray, then that ray's path state, towards L1, so the
+// next iteration's chain of dependent loads (bucket -> ray -> state) finds them on chip.
+struct NextEntry {
+    const float4 *ray = nullptr;   // the next entry's ray record (null: none)
+};
+PG3_DI void prefetchNextRay(const NextEntry &nx)
+{
+    if (nx.ray) {
+        prefetchL1(nx.ray);
+        prefetchL1(nx.ray + 1);
+    }
+}
+PG3_DI void prefetchNextState(const Queues &Q, const NextEntry &nx)
+{
+    if (nx.ray) {
+        const uint32_t slot = __float_as_uint(__ldg(&nx.ray[1].w)) & kSlotMask;
+        prefetchL1(&Q.beta[slot]);
+        prefetchL1(&Q.ew[slot]);
+        prefetchL1(&Q.pn[slot]);
+    }
+}
 struct ShadeOut {
     bool shadow = false, next = false;
     float4 s0, s1, s2;        // shadow record: origin + distance, direction + tag, contribution
@@ -178,7 +202,7 @@ struct ShadeOut {
 template <int K, int EMK, bool GRAD>
 PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float4 r0, float4 r1, uint32_t slot,
                         uint32_t tag, uint32_t pixel, uint32_t sample, PathCounters &pc, ShadeOut &o, float3 &L,
-                        const GradArgs &G, float *sGrad, float3 acc)
+                        const GradArgs &G, float *sGrad, float3 acc, const NextEntry &nx = NextEntry())
 {
     const float3 org = xyz(r0), dir = xyz(r1);
     const float4 sb = Q.beta[slot], se = Q.ew[slot], sn = Q.pn[slot];
@@ -225,6 +249,7 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
     float3 pt, nrm;
     int matId;
     hitAttributes(S, h, org, dir, pt, nrm, matId);
+    prefetchNextRay(nx);
     const Frame frame = frameFromZ(nrm);
     const float3 wol = toLocal(frame, -dir);
     const int lightId = __ldg(&S.mat2light[matId]);
@@ -287,6 +312,7 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
             }
         }
     }
+    prefetchNextState(Q, nx);
     // Russian roulette (src/path_tracer.hxx:267-303)
     float rrProb = 1.0f;
     bool cut = false;

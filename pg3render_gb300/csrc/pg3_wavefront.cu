@@ -102,12 +102,20 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
     constexpr int kBucket = bucketOfShade(K);
     const uint32_t n = Q.cnt->bucket[kBucket];
     const float4 *rq = Q.ray[cur];
+    const uint32_t stride = gridDim.x * blockDim.x;
     PathCounters pc;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    // the bucket entry of the next iteration is loaded one iteration ahead
+    uint32_t nextIdx = (blockIdx.x * blockDim.x + threadIdx.x < n) ? Q.bucket[kBucket][blockIdx.x * blockDim.x + threadIdx.x] : 0u;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t j = base + threadIdx.x;
         ShadeOut o;
         if (j < n) {
-            const uint32_t idx = Q.bucket[kBucket][j];
+            const uint32_t idx = nextIdx;
+            NextEntry nx;
+            if (j + stride < n) {
+                nextIdx = Q.bucket[kBucket][j + stride];
+                nx.ray = rq + 2 * (size_t)nextIdx;
+            }
             const float4 r0 = rq[2 * idx], r1 = rq[2 * idx + 1];
             const uint32_t slot = __float_as_uint(r1.w) & kSlotMask;
             const uint32_t g = base0 + slot;
@@ -115,7 +123,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
             float3 acc = f3(0.f);
             if (GRAD && G.adjoint) acc = make_float3(outR[slot], outG[slot], outB[slot]);
             float3 L;
-            shadeVertex<K, EMK, GRAD>(S, Q, idx, r0, r1, slot, slot, pixel, sample, pc, o, L, G, sGrad, acc);
+            shadeVertex<K, EMK, GRAD>(S, Q, idx, r0, r1, slot, slot, pixel, sample, pc, o, L, G, sGrad, acc, nx);
             if (!isZero(L)) {
                 outR[slot] += L.x;
                 outG[slot] += L.y;
