@@ -174,12 +174,14 @@ PG3_DI void prefetchL1(const void *p) { asm volatile("prefetch.global.L1 [%0];" 
 // next iteration's chain of dependent loads (bucket -> ray -> state) finds them on chip.
 struct NextEntry {
     const float4 *ray = nullptr;   // the next entry's ray record (null: none)
+    const float2 *hit = nullptr;   // and its hit record
 };
 PG3_DI void prefetchNextRay(const NextEntry &nx)
 {
     if (nx.ray) {
         prefetchL1(nx.ray);
         prefetchL1(nx.ray + 1);
+        prefetchL1(nx.hit);
     }
 }
 PG3_DI void prefetchNextState(const Queues &Q, const NextEntry &nx)

@@ -74,10 +74,15 @@ __global__ void __launch_bounds__(kWaveBlock) extendKernel(const __grid_constant
     const uint32_t n = Q.cnt->ray[cur];
     const float4 *rq = Q.ray[cur];
     uint32_t rays = 0;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
         int bucket = -1;
         if (i < n) {
+            if (i + stride < n) {   // the next iteration's ray, while this one is traced
+                prefetchL1(rq + 2 * (size_t)(i + stride));
+                prefetchL1(rq + 2 * (size_t)(i + stride) + 1);
+            }
             bucket = extendOne(S, Q, rq, i);
             ++rays;
         }
@@ -115,6 +120,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
             if (j + stride < n) {
                 nextIdx = Q.bucket[kBucket][j + stride];
                 nx.ray = rq + 2 * (size_t)nextIdx;
+                nx.hit = Q.hit + nextIdx;
             }
             const float4 r0 = rq[2 * idx], r1 = rq[2 * idx + 1];
             const uint32_t slot = __float_as_uint(r1.w) & kSlotMask;
@@ -150,10 +156,17 @@ __global__ void __launch_bounds__(kWaveBlock) shadowKernel(const __grid_constant
     initBlockGrad<GRAD>(sGrad, S.nmat);
     const uint32_t n = Q.cnt->shadow;
     uint32_t cnt = 0;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t j = base + threadIdx.x;
         if (j < n) {
             const float4 *rec = Q.shadow + (size_t)SW * j;
+            if (j + stride < n) {   // the next iteration's record, while this ray is tested
+                const float4 *nr = Q.shadow + (size_t)SW * (j + stride);
+                prefetchL1(nr);
+                prefetchL1(nr + 1);
+                prefetchL1(nr + 2);
+            }
             const float4 s0 = rec[0], s1 = rec[1];
             ++cnt;
             if (!occludedAny(S, xyz(s0), xyz(s1), s0.w)) {
