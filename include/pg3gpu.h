@@ -61,14 +61,18 @@ enum {
 };
 
 /* Material kinds: LambertMaterial, MicrofacetGGXConductorMaterial, MicrofacetGGXDielectricMaterial,
-   PhongMaterial, SmoothConductorMaterial, SmoothDielectricMaterial (src/materials.hxx:250-1266). */
+   PhongMaterial, SmoothConductorMaterial, SmoothDielectricMaterial, SraLayeredMaterial
+   (src/materials.hxx:250-1566). The SRA layered material is rendered by the one-hit algorithms
+   only: the reference's path tracers stop with a fatal error on it (its IsReflectanceZero and
+   GetRRContinuationProb are not implemented, :1544-1557), and so they are refused here. */
 enum {
     PG3GPU_MAT_LAMBERT = 0,
     PG3GPU_MAT_GGX_CONDUCTOR = 1,
     PG3GPU_MAT_GGX_DIELECTRIC = 2,
     PG3GPU_MAT_PHONG = 3,
     PG3GPU_MAT_SMOOTH_CONDUCTOR = 4,
-    PG3GPU_MAT_SMOOTH_DIELECTRIC = 5
+    PG3GPU_MAT_SMOOTH_DIELECTRIC = 5,
+    PG3GPU_MAT_SRA_LAYERED = 6
 };
 enum { PG3GPU_BG_NONE = 0, PG3GPU_BG_CONSTANT = 1, PG3GPU_BG_ENVMAP = 2 };
 /* Environment-map light samplers (compile-time choice in src/hard_config.hxx:17-18, run-time here). */
@@ -96,6 +100,14 @@ typedef struct pg3gpu_material {
     float absorb;                    /* conductor absorbance k */
     float glossy[3];                 /* Phong glossy reflectance (mPhongReflectance) */
     float phong_exponent;            /* Phong lobe exponent (mPhongExponent), >= 0 */
+    /* PG3GPU_MAT_SRA_LAYERED: the outer layer is a GGX dielectric (alpha, ior, ior_outer), the
+       inner layer a Lambert (albedo) or a GGX conductor (inner_alpha, inner_ior, inner_ior_outer,
+       absorb), with a medium of attenuation coefficients medium_attenuation and thickness
+       medium_thickness between them (SraLayeredMaterial, src/materials.hxx:1304-1324) */
+    int32_t inner_kind;              /* PG3GPU_MAT_LAMBERT or PG3GPU_MAT_GGX_CONDUCTOR */
+    float inner_alpha, inner_ior, inner_ior_outer;
+    float medium_attenuation[3];
+    float medium_thickness;
 } pg3gpu_material;
 
 typedef struct pg3gpu_triangle {     /* Triangle(p0, p1, p2, matId), src/scene_graph.hxx:88-101 */

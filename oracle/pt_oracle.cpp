@@ -418,7 +418,8 @@ static inline float GgxPdfVisibleNormals(V3 wo, V3 h, float D, float a)
 // --------------------------------------------------------------------------------------------
 // Materials (src/materials.hxx)
 // --------------------------------------------------------------------------------------------
-enum { kLambert = 0, kGgxConductor = 1, kGgxDielectric = 2, kPhong = 3, kSmoothConductor = 4, kSmoothDielectric = 5 };
+enum { kLambert = 0, kGgxConductor = 1, kGgxDielectric = 2, kPhong = 3, kSmoothConductor = 4, kSmoothDielectric = 5,
+       kSra = 6 };
 
 struct MatRecord {   // src/materials.hxx:48-207 (the fields the path tracer reads)
     V3 wol, wil, attenuation;
@@ -433,6 +434,12 @@ struct Material {
     V3 reflectance;            // Lambert reflectance; Phong diffuse reflectance (mDiffuseReflectance)
     V3 glossy;                 // Phong mPhongReflectance
     float exponent = 1.f;      // Phong mPhongExponent
+    // SRA layered (:1304-1324): this record is the outer GGX dielectric (alpha, eta, etaInv); the
+    // inner Lambert (reflectance) or GGX conductor (innerAlpha, innerEta, absorb); the medium
+    int innerKind = kLambert;
+    float innerAlpha = 0.1f, innerEta = 1.f;
+    V3 mediumAtt;
+    float mediumThickness = 0.f;
     float alpha = 0.1f, eta = 1.f, etaInv = 1.f, absorb = 0.f;
     // Sampling overrides (not in the reference): the GGX roughness that sampling and pdfs use and
     // the roulette continuation probability, for finite differences that hold sampling fixed
@@ -471,6 +478,19 @@ struct Material {
         m.absorb = k;
         return m;
     }
+    static Material Sra(const Material &outer, const Material &inner, V3 att, float thickness)
+    {
+        Material m = outer;
+        m.kind = kSra;
+        m.innerKind = inner.kind;
+        m.reflectance = inner.reflectance;
+        m.innerAlpha = inner.alpha;
+        m.innerEta = inner.eta;
+        m.absorb = inner.absorb;
+        m.mediumAtt = att;
+        m.mediumThickness = thickness;
+        return m;
+    }
     static Material SmoothDielectric(float n, float no)   // :713-727
     {
         Material m; m.kind = kSmoothDielectric;
@@ -481,7 +501,7 @@ struct Material {
 
     // Light-sampling sides (:36-45): front side for all but the smooth materials, whose Dirac
     // lobes take no light samples (kBsdfNone, :604-609) -- their light samples are all zero.
-    bool SamplesLights() const { return kind < kSmoothConductor; }
+    bool SamplesLights() const { return kind != kSmoothConductor && kind != kSmoothDielectric; }
 
     bool IsReflectanceZero() const   // :321-324, 572-575, 702-705, 777-780, 873-876, 1110-1113
     {
@@ -505,6 +525,88 @@ struct Material {
         }
         if (kind == kSmoothConductor) return FresnelConductor(wol.z, eta, absorb);
         return 1.0f;
+    }
+
+    // ---- SRA layered material (:1304-1566)
+    V3 BeerLambert(float len) const   // Physics::BeerLambert
+    {
+        return V3(std::exp(-(mediumAtt.x * len)), std::exp(-(mediumAtt.y * len)), std::exp(-(mediumAtt.z * len)));
+    }
+    // the inner layer: EvalBsdf with kOptSamplingProbs and kOptReflectance
+    void SraInner(V3 wi, V3 wo, V3 &att, float &pdf, float &refl) const
+    {
+        if (innerKind == kLambert) {
+            att = (wi.z <= 0.f || wo.z <= 0.f) ? V3(0.f) : reflectance / kPiF;
+            pdf = CosHemispherePdfW(wi.z);
+            refl = Luminance(reflectance);
+            return;
+        }
+        const V3 h = HalfwayReflection(wi, wo);
+        const float D = DistributionGgx(h, innerAlpha);
+        const float F = FresnelConductor(Dot(h, wo), innerEta, absorb);
+        if (wi.z <= 0.f || wo.z <= 0.f || IsTiny(4.0f * wi.z * wo.z)) att = V3(0.f);
+        else att = V3((F * SmithG1(wi, h, innerAlpha) * SmithG1(wo, h, innerAlpha) * D) / (4.0f * wi.z * wo.z));
+        pdf = (wo.z < 0.f) ? 0.0f : GgxPdfVisibleNormals(wo, h, D, innerAlpha) * ReflectionJacobian(wo, h);
+        refl = F;   // GetReflectanceEst: the microfacet Fresnel reflectance (:978-982)
+    }
+    void SraEval(MatRecord &r) const   // :1328-1451
+    {
+        const V3 wil = r.wil, wol = r.wol;
+        r.compProb = 1.f;
+        if (wil.z <= 0.f || wol.z <= 0.f) { r.attenuation = V3(0.f); r.pdfW = 0.f; return; }
+        // outer layer, reflection only
+        DielCtx c = DielInit(wil, wol);
+        const V3 outerAtt = DielEval(c);
+        const float outerPdf = (c.wo.z < 0.f) ? 0.f
+                               : GgxPdfVisibleNormals(c.wo, c.m, c.Dp, AlphaS()) * ReflectionJacobian(c.wi, c.m);
+        V3 wilRefract, wolRefract;
+        bool dummy;
+        wilRefract = Refract(dummy, wil, V3(0.f, 0.f, 1.f), eta);
+        wolRefract = Refract(dummy, wol, V3(0.f, 0.f, 1.f), eta);
+        const float wilFresnelTrans = 1.f - FresnelDielectric(wil.z, eta);
+        const float wolFresnelRefl = FresnelDielectric(wol.z, eta);
+        const float wolFresnelTrans = 1.f - wolFresnelRefl;
+        const float cO = std::max(wol.z, 0.0001f), cI = std::max(wil.z, 0.0001f);
+        const V3 mediumTrans = BeerLambert(mediumThickness * (1.f / cO + 1.f / cI));
+        V3 innerAtt;
+        float innerPdf, innerRefl;
+        SraInner(-wilRefract, -wolRefract, innerAtt, innerPdf, innerRefl);
+        const float innerSolAngCompr = Sqr(1.f / eta);
+        r.attenuation = outerAtt + innerAtt * (wilFresnelTrans * wolFresnelTrans) * innerSolAngCompr * mediumTrans;
+        const V3 mediumTransEst = BeerLambert(mediumThickness * (1.f / cO * 2.f));
+        const float outerC = wolFresnelRefl, innerC = innerRefl * wolFresnelTrans * Luminance(mediumTransEst);
+        const float tot = outerC + innerC;
+        const float innerPdfSolAngCompr = Sqr(1.f / eta) * (wil.z / -wilRefract.z);
+        r.pdfW = outerPdf * (outerC / tot) + (innerPdf * innerPdfSolAngCompr) * (innerC / tot);
+    }
+    void SraSample(const float u[3], MatRecord &r) const   // :1457-1537; u[2] picks the layer
+    {
+        const V3 wol = r.wol;
+        const float wolFresnelRefl = FresnelDielectric(wol.z, eta);
+        const float wolFresnelTrans = 1.f - wolFresnelRefl;
+        float innerRefl;
+        if (innerKind == kLambert) innerRefl = Luminance(reflectance);
+        else innerRefl = FresnelConductor(Dot(HalfwayReflection(V3(0.f), wol), wol), innerEta, absorb);
+        const float cO = std::max(wol.z, 0.0001f);
+        const V3 mediumTransEst = BeerLambert(mediumThickness * (1.f / cO * 2.f));
+        const float outerC = wolFresnelRefl, innerC = innerRefl * wolFresnelTrans * Luminance(mediumTransEst);
+        const float tot = outerC + innerC;
+        bool dummy;
+        if (u[2] * tot < outerC) {
+            const bool below = wol.z < 0.f;
+            const float s = below ? -1.0f : 1.0f;
+            const V3 wo = wol * s;
+            const V3 m = SampleVndf(wo, AlphaS(), u[0], u[1]);
+            r.wil = Reflect(dummy, wo, m) * s;
+        } else {
+            const V3 wolRefract = Refract(dummy, wol, V3(0.f, 0.f, 1.f), eta);
+            const V3 wo = -wolRefract;
+            V3 wi;
+            if (innerKind == kLambert) wi = SampleCosHemisphereW(u[0], u[1], nullptr);
+            else wi = Reflect(dummy, wo, SampleVndf(wo, innerAlpha, u[0], u[1]));
+            r.wil = Refract(dummy, -wi, V3(0.f, 0.f, 1.f), eta);
+        }
+        SraEval(r);
     }
 
     // ---- Phong helpers (:383-531)
@@ -609,6 +711,8 @@ struct Material {
             r.attenuation = DielEval(c);
             r.compProb = 1.0f;
             r.pdfW = DielPdf(c);
+        } else if (kind == kSra) {
+            SraEval(r);
         } else if (kind == kPhong) {   // :416-431, 577-593
             r.attenuation = PhongEval(r.wil, r.wol);
             r.pdfW = PhongPdf(r.wol, r.wil, PhongDiffuseEst(), PhongGlossyEst(r.wol));
@@ -668,6 +772,8 @@ struct Material {
             r.pdfW = DielPdf(c);
             if (!above || cosAbs < 0.0f) r.attenuation = V3(0.f);
             else r.attenuation = DielEval(c);
+        } else if (kind == kSra) {
+            SraSample(u, r);
         } else if (kind == kPhong) {   // :437-495; u[2] picks the component
             const float dEst = PhongDiffuseEst(), gEst = PhongGlossyEst(r.wol);
             const float tot = dEst + gEst;
@@ -1560,6 +1666,22 @@ static bool ParseScene(const char *text, Scene &s, std::string &err)
         } else if (k == "smooth_dielectric") {
             float n, no; ls >> n >> no;
             s.mats.push_back(Material::SmoothDielectric(n, no));
+        } else if (k == "sra") {
+            // sra outer_alpha outer_n outer_no (lambert r g b | ggx_conductor a n no k) att_r att_g att_b thickness
+            float a, n, no;
+            std::string ik;
+            ls >> a >> n >> no >> ik;
+            Material inner;
+            if (ik == "lambert") {
+                float r, g, b; ls >> r >> g >> b;
+                inner = Material::Lambert(V3(r, g, b));
+            } else if (ik == "ggx_conductor") {
+                float ia, in, ino, kk; ls >> ia >> in >> ino >> kk;
+                inner = Material::Conductor(ia, in, ino, kk);
+            } else { err = "sra: unknown inner layer " + ik; return false; }
+            float att[3], th;
+            ls >> att[0] >> att[1] >> att[2] >> th;
+            s.mats.push_back(Material::Sra(Material::Dielectric(a, n, no), inner, V3(att[0], att[1], att[2]), th));
         } else if (k == "point_light") {
             float p[3], w[3];
             ls >> p[0] >> p[1] >> p[2] >> w[0] >> w[1] >> w[2];
@@ -1667,6 +1789,15 @@ int pg3o_render(const char *scene_text, uint64_t seed, uint32_t sample0, uint32_
     }
     s.em.sampler = em_sampler;
     s.rrMinPL = rr_min_path_length;
+    if (s.algorithm >= 6)
+        for (const Material &m : s.mats)
+            if (m.kind == kSra) {
+                // the reference's path tracers stop with a fatal error on this material
+                // (IsReflectanceZero / GetRRContinuationProb not implemented, src/materials.hxx:1544-1557)
+                const char *msg = "the path tracers cannot render the SRA layered material";
+                if (err && errlen > 0) { std::strncpy(err, msg, errlen - 1); err[errlen - 1] = 0; }
+                return 1;
+            }
     const Tracer tr(s);
     const uint32_t npix = s.W * s.H;
 #ifdef _OPENMP

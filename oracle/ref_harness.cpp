@@ -24,6 +24,7 @@
 //   phong dr dg db gr gg gb exponent         (diffuse part as the material holds it)
 //   smooth_conductor n_inner n_outer k
 //   smooth_dielectric n_inner n_outer
+//   sra outer_alpha outer_n outer_no (lambert r g b | ggx_conductor alpha n no k) att_r att_g att_b thickness
 //   triangle x0 y0 z0 x1 y1 z1 x2 y2 z2 material
 //   sphere cx cy cz radius material
 //   area_light x0 y0 z0 x1 y1 z1 x2 y2 z2 material Lr Lg Lb
@@ -115,6 +116,30 @@ SceneFile LoadScene(const char *path, const AuxDbgParams &aux)
             float n, no;
             ls >> n >> no;
             s->mMaterials.push_back(new SmoothDielectricMaterial(n, no));
+        } else if (kind == "sra") {
+            float a, n, no;
+            std::string ik;
+            ls >> a >> n >> no >> ik;
+            AbstractMaterial *inner = nullptr;
+            if (ik == "lambert") {
+                float r, g, b;
+                ls >> r >> g >> b;
+                SpectrumF refl;
+                refl.SetSRGBAttenuation(r, g, b);
+                inner = new LambertMaterial(refl);
+            } else if (ik == "ggx_conductor") {
+                float ia, in, ino, k;
+                ls >> ia >> in >> ino >> k;
+                inner = new MicrofacetGGXConductorMaterial(ia, in, ino, k);
+            } else {
+                Fail("sra: unknown inner layer " + ik);
+            }
+            float att[3], th;
+            ls >> att[0] >> att[1] >> att[2] >> th;
+            SpectrumF medium;
+            medium.SetSRGBAttenuation(att[0], att[1], att[2]);
+            s->mMaterials.push_back(
+                new SraLayeredMaterial(new MicrofacetGGXDielectricMaterial(a, n, no), inner, medium, th, aux));
         } else if (kind == "point_light") {
             float p[3], w[3];
             ls >> p[0] >> p[1] >> p[2] >> w[0] >> w[1] >> w[2];

@@ -32,7 +32,10 @@ class Camera(ctypes.Structure):
 class Material(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("albedo", c_float3), ("alpha", ctypes.c_float),
                 ("ior", ctypes.c_float), ("ior_outer", ctypes.c_float), ("absorb", ctypes.c_float),
-                ("glossy", c_float3), ("phong_exponent", ctypes.c_float)]
+                ("glossy", c_float3), ("phong_exponent", ctypes.c_float),
+                ("inner_kind", ctypes.c_int32), ("inner_alpha", ctypes.c_float), ("inner_ior", ctypes.c_float),
+                ("inner_ior_outer", ctypes.c_float), ("medium_attenuation", c_float3),
+                ("medium_thickness", ctypes.c_float)]
 
 
 class Triangle(ctypes.Structure):
@@ -186,7 +189,8 @@ def scene_desc(scene):
     mats = (Material * max(1, len(scene.materials)))()
     for i, m in enumerate(scene.materials):
         mats[i] = Material(m.kind, c_float3(*m.albedo), m.alpha, m.ior, m.ior_outer, m.absorb,
-                           c_float3(*m.glossy), m.phong_exponent)
+                           c_float3(*m.glossy), m.phong_exponent, m.inner_kind, m.inner_alpha, m.inner_ior,
+                           m.inner_ior_outer, c_float3(*m.medium_attenuation), m.medium_thickness)
     tris = (Triangle * max(1, len(scene.triangles)))()
     for i, (p0, p1, p2, mat) in enumerate(scene.triangles):
         tris[i] = Triangle((ctypes.c_float * 9)(*p0, *p1, *p2), mat)

@@ -145,6 +145,11 @@ void foldTimers(pg3gpu_ctx *ctx)
 // on the megakernel
 int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passes)
 {
+    if ((ctx->kindMask & (1u << kMatSra)) &&
+        (algorithm == PG3GPU_ALG_PATH_TRACING || algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE))
+        return fail(ctx, PG3GPU_ERR_UNSUPPORTED,
+                    "the SRA layered material has no roulette probability or zero-reflectance test, so the path "
+                    "tracers cannot render it (the reference stops with a fatal error, src/materials.hxx:1544-1557)");
     const uint32_t npix = ctx->W * ctx->H;
     const uint64_t paths = (uint64_t)passes * npix;
     int st = ensureOutput(ctx, paths);

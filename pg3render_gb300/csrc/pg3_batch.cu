@@ -658,6 +658,8 @@ int pg3gpu_batch_create(const pg3gpu_scene *scenes, const pg3gpu_options *opts, 
         b->inst.push_back(c);
         b->spp.push_back(spp[i]);
         b->kindMask |= c->kindMask;
+        if (c->kindMask & (1u << kMatSra))
+            return bail(bfail(b, PG3GPU_ERR_UNSUPPORTED, who + "the path tracers cannot render the SRA layered material"));
         if (c->view.bgKind == kBgEnvMap) {
             if (emk >= 0 && emk != c->view.emSampler)
                 return bail(bfail(b, PG3GPU_ERR_UNSUPPORTED, who + "all environment-map instances must use one sampler"));

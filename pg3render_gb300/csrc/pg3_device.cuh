@@ -422,6 +422,120 @@ PG3_DI float phongPdf(const DevMaterial &m, float3 wol, float3 wil, float dEst, 
 }
 PG3_DI float smoothDielectricFresnel(const DevMaterial &m, float3 wol) { return fresnelDielectric(wol.z, m.eta); }
 
+// SRA layered material (SraLayeredMaterial, src/materials.hxx:1304-1566): a GGX dielectric outer
+// layer taken for reflection only, an inner Lambert or GGX conductor seen through the refracted
+// directions, and a Beer-Lambert medium between them. The inner layer's record fields: r,g,b
+// (Lambert), innerAlpha / innerEta / absorb (conductor); the medium: gr,gg,gb and exponent.
+PG3_DI float3 sraMediumTrans(const DevMaterial &m, float len)   // Physics::BeerLambert
+{
+    return make_float3(expf(-(m.gr * len)), expf(-(m.gg * len)), expf(-(m.gb * len)));
+}
+// the inner layer's value, pdf and reflectance estimate (LambertMaterial :262-345; GGX conductor
+// :878-989, its estimate the microfacet Fresnel reflectance :978-982)
+PG3_DI void sraInnerEval(const DevMaterial &m, float3 wi, float3 wo, float3 &att, float &pdf, float &refl)
+{
+    if (m.innerKind == kMatLambert) {
+        const float3 R = make_float3(m.r, m.g, m.b);
+        att = (wi.z <= 0.f || wo.z <= 0.f) ? f3(0.f) : R * kPiInvF;
+        pdf = cosHemispherePdf(wi.z);
+        refl = luminance(R);
+        return;
+    }
+    const float a = m.innerAlpha;
+    const float3 h = halfwayReflection(wi, wo);
+    const float D = ggxD(h, a);
+    const float F = fresnelConductor(dot(h, wo), m.innerEta, m.absorb);
+    if (wi.z <= 0.f || wo.z <= 0.f || isTiny(4.0f * wi.z * wo.z)) att = f3(0.f);
+    else att = f3((F * smithG1(wi, h, a) * smithG1(wo, h, a) * D) / (4.0f * wi.z * wo.z));
+    pdf = (wo.z < 0.f) ? 0.f : ggxPdfVisibleNormals(wo, h, D, a) * reflectionJacobian(wo, h);
+    refl = F;
+}
+// EvalBsdf with kOptSamplingProbs (:1328-1451)
+PG3_DI void sraEval(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
+{
+    r.wil = wil;
+    r.compProb = 1.f;
+    if (wil.z <= 0.f || wol.z <= 0.f) {   // no transmission below the horizon
+        r.att = f3(0.f);
+        r.pdfW = 0.f;
+        return;
+    }
+    // outer layer, reflection only: the dielectric's reflection lobe, component probability 1
+    DielCtx c;
+    c.refl = true;
+    c.wo = wol;
+    c.wi = wil;
+    c.etaS = m.eta;
+    c.etaInvS = m.etaInv;
+    c.m = halfwayReflection(wil, wol);
+    c.D = ggxD(c.m, m.alpha);
+    c.Dp = c.D;
+    c.F = fresnelDielectric(dot(c.m, c.wo), c.etaS);
+    const float3 attO = dielEval(m, c);
+    const float pdfO = ggxPdfVisibleNormals(wol, c.m, c.D, m.alpha) * reflectionJacobian(wil, c.m);
+    // inner layer through the refracted directions
+    bool ab;
+    const float3 n = make_float3(0.f, 0.f, 1.f);
+    const float3 wiR = refract(ab, wil, n, m.eta), woR = refract(ab, wol, n, m.eta);
+    const float Ti = 1.f - fresnelDielectric(wil.z, m.eta), Fo = fresnelDielectric(wol.z, m.eta);
+    const float To = 1.f - Fo;
+    const float cO = fmaxf(wol.z, 0.0001f), cI = fmaxf(wil.z, 0.0001f);
+    const float3 mt = sraMediumTrans(m, m.exponent * (1.f / cO + 1.f / cI));
+    float3 attI;
+    float pdfI, reflI;
+    sraInnerEval(m, -wiR, -woR, attI, pdfI, reflI);
+    const float invEta2 = sqr(1.f / m.eta);
+    r.att = attO + attI * (Ti * To) * invEta2 * mt;
+    // mixture pdf with the component weights of the sampling routine
+    const float3 mtEst = sraMediumTrans(m, m.exponent * (1.f / cO * 2.f));
+    const float outerC = Fo, innerC = reflI * To * luminance(mtEst);
+    const float tot = outerC + innerC;
+    const float compr = invEta2 * (wil.z / -wiR.z);
+    r.pdfW = pdfO * (outerC / tot) + (pdfI * compr) * (innerC / tot);
+}
+// SampleBsdf (:1457-1537): u2 picks the layer, (u0, u1) the direction
+PG3_DI void sraSample(const DevMaterial &m, float3 wol, float u0, float u1, float u2, BsdfRec &r)
+{
+    const float Fo = fresnelDielectric(wol.z, m.eta), To = 1.f - Fo;
+    float reflI;
+    if (m.innerKind == kMatLambert) {
+        reflI = luminance(make_float3(m.r, m.g, m.b));
+    } else {
+        // the inner record is queried before a direction exists (incoming direction zero): the
+        // estimate is the Fresnel reflectance at the outgoing direction's own half vector
+        const float3 h = halfwayReflection(f3(0.f), wol);
+        reflI = fresnelConductor(dot(h, wol), m.innerEta, m.absorb);
+    }
+    const float cO = fmaxf(wol.z, 0.0001f);
+    const float3 mtEst = sraMediumTrans(m, m.exponent * (1.f / cO * 2.f));
+    const float outerC = Fo, innerC = reflI * To * luminance(mtEst);
+    const float tot = outerC + innerC;
+    float3 wil;
+    bool ab;
+    const float3 n = make_float3(0.f, 0.f, 1.f);
+    if (u2 * tot < outerC) {
+        // the outer dielectric sampled for reflection only (:1045-1079 with kReflectionOnly)
+        const bool below = wol.z < 0.f;
+        const float s = below ? -1.0f : 1.0f;
+        const float3 wo = wol * s;
+        const float3 mf = sampleGgxVndf(wo, m.alpha, u0, u1, m.vndfExact != 0);
+        wil = reflect(ab, wo, mf) * s;
+    } else {
+        const float3 woR = refract(ab, wol, n, m.eta);
+        const float3 wo = -woR;
+        float3 wi;
+        if (m.innerKind == kMatLambert) {
+            float pdf;
+            wi = sampleCosHemisphere(u0, u1, pdf);
+        } else {
+            const float3 h = sampleGgxVndf(wo, m.innerAlpha, u0, u1, m.vndfExact != 0);
+            wi = reflect(ab, wo, h);
+        }
+        wil = refract(ab, -wi, n, m.eta);   // total internal reflection can send it below
+    }
+    sraEval(m, wil, wol, r);
+}
+
 // EvalBsdf + GetOptData(kOptSamplingProbs) per material kind: :277-283 (Lambert),
 // :809-817 (conductor), :1023-1031 with InitEvalContext :1123-1160 (dielectric)
 // DA: also compute BsdfRec::dAtt
@@ -462,6 +576,9 @@ PG3_DI void evalBsdfK(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
         r.att = phongEval(m, wil, wol);
         r.pdfW = phongPdf(m, wol, wil, phongDiffuseEst(m), phongGlossyEst(m, wol));
         if (DA) r.dAtt = 0.f;
+    } else if (K == kMatSra) {
+        sraEval(m, wil, wol, r);
+        if (DA) r.dAtt = 0.f;
     } else {
         // smooth conductor / dielectric (:611-655): Dirac lobes only, no finite component
         r.att = f3(0.f);
@@ -477,6 +594,7 @@ PG3_DI void evalBsdf(const DevMaterial &m, float3 wil, float3 wol, BsdfRec &r)
     case kMatGgxConductor: evalBsdfK<kMatGgxConductor>(m, wil, wol, r); break;
     case kMatGgxDielectric: evalBsdfK<kMatGgxDielectric>(m, wil, wol, r); break;
     case kMatPhong: evalBsdfK<kMatPhong>(m, wil, wol, r); break;
+    case kMatSra: evalBsdfK<kMatSra>(m, wil, wol, r); break;
     default: evalBsdfK<kMatSmoothConductor>(m, wil, wol, r); break;
     }
 }
@@ -541,6 +659,9 @@ PG3_DI void sampleBsdfK(const DevMaterial &m, float3 wol, float u0, float u1, fl
         }
         r.pdfW = phongPdf(m, wol, r.wil, dEst, gEst);
         r.att = (r.wil.z > 0.f) ? phongEval(m, r.wil, wol) : f3(0.f);
+    } else if (K == kMatSra) {
+        if (DA) r.dAtt = 0.f;
+        sraSample(m, wol, u0, u1, u2, r);
     } else if (K == kMatSmoothConductor) {
         // :670-689: mirror direction, grey conductor Fresnel
         if (DA) r.dAtt = 0.f;
@@ -575,6 +696,7 @@ PG3_DI void sampleBsdf(const DevMaterial &m, float3 wol, float u0, float u1, flo
     case kMatGgxDielectric: sampleBsdfK<kMatGgxDielectric>(m, wol, u0, u1, u2, r); break;
     case kMatPhong: sampleBsdfK<kMatPhong>(m, wol, u0, u1, u2, r); break;
     case kMatSmoothConductor: sampleBsdfK<kMatSmoothConductor>(m, wol, u0, u1, u2, r); break;
+    case kMatSra: sampleBsdfK<kMatSra>(m, wol, u0, u1, u2, r); break;
     default: sampleBsdfK<kMatSmoothDielectric>(m, wol, u0, u1, u2, r); break;
     }
 }
@@ -589,7 +711,10 @@ PG3_DI void sampleBsdfSmooth(const DevMaterial &m, float3 wol, float u2, BsdfRec
 // Does the material take light samples? Every kind but the Dirac ones samples lights from its
 // front side (kBsdfFrontSideLightSampling); smooth materials have no finite component
 // (kBsdfNone, src/materials.hxx:604-609), so their light samples are always zero.
-PG3_DI bool takesLightSamples(const DevMaterial &m) { return m.kind < kMatSmoothConductor; }
+PG3_DI bool takesLightSamples(const DevMaterial &m)
+{
+    return m.kind != kMatSmoothConductor && m.kind != kMatSmoothDielectric;
+}
 
 // GetRRContinuationProb (src/materials.hxx:301-322, 542-570, 691-700, 770-775, 853-869, 1093-1098)
 // clamped to [0, 0.997] (src/path_tracer.hxx:281-283). Phong and the smooth conductor depend on

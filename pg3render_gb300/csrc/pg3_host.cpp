@@ -207,12 +207,38 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
             d.eta = (std::fabs(m.ior_outer) < kTiny) ? 1.0f : m.ior / m.ior_outer;
             d.etaInv = (std::fabs(m.ior) < kTiny) ? 1.0f : m.ior_outer / m.ior;
             d.rrProb = 0.997f;
+        } else if (m.kind == PG3GPU_MAT_SRA_LAYERED) {
+            // outer GGX dielectric as MicrofacetGGXDielectricMaterial (:996-1021); inner Lambert
+            // or GGX conductor (:262-266, 791-806); the medium between them (:1307-1324)
+            if (std::fabs(m.ior_outer) >= kTiny) { d.eta = m.ior / m.ior_outer; d.etaInv = m.ior_outer / m.ior; }
+            if (!(d.eta > 0.f) || !std::isfinite(d.eta))
+                return bad(PG3GPU_ERR_INVALID_ARGUMENT, "SRA outer layer needs positive indices of refraction");
+            d.innerKind = m.inner_kind;
+            if (m.inner_kind == PG3GPU_MAT_LAMBERT) {
+                if (!finite3(m.albedo) || m.albedo[0] < 0.f || m.albedo[1] < 0.f || m.albedo[2] < 0.f)
+                    return bad(PG3GPU_ERR_INVALID_ARGUMENT, "SRA inner Lambert reflectance must be finite and >= 0");
+            } else if (m.inner_kind == PG3GPU_MAT_GGX_CONDUCTOR) {
+                if (!(m.inner_alpha >= 0.f) || !std::isfinite(m.inner_ior) || !std::isfinite(m.inner_ior_outer))
+                    return bad(PG3GPU_ERR_INVALID_ARGUMENT, "SRA inner conductor needs alpha >= 0 and finite IORs");
+                d.innerAlpha = std::min(std::max(m.inner_alpha, 0.001f), 1.0f);
+                d.innerEta = (std::fabs(m.inner_ior_outer) < kTiny) ? 1.0f : m.inner_ior / m.inner_ior_outer;
+                d.absorb = m.absorb;
+            } else {
+                return bad(PG3GPU_ERR_INVALID_ARGUMENT, "SRA inner layer must be Lambert or GGX conductor");
+            }
+            if (!finite3(m.medium_attenuation) || m.medium_attenuation[0] < 0.f || m.medium_attenuation[1] < 0.f ||
+                m.medium_attenuation[2] < 0.f || !(m.medium_thickness >= 0.f) || !std::isfinite(m.medium_thickness))
+                return bad(PG3GPU_ERR_INVALID_ARGUMENT, "SRA medium attenuation and thickness must be finite and >= 0");
+            d.gr = m.medium_attenuation[0]; d.gg = m.medium_attenuation[1]; d.gb = m.medium_attenuation[2];
+            d.exponent = m.medium_thickness;
+            d.rrProb = 1.f;   // (not used: the path tracers refuse the material)
         } else {
             std::snprintf(buf, sizeof buf, "material %u: unknown kind %d", i, m.kind);
             err = buf;
             return PG3GPU_ERR_INVALID_ARGUMENT;
         }
-        if (!(m.alpha >= 0.f) && (m.kind == PG3GPU_MAT_GGX_CONDUCTOR || m.kind == PG3GPU_MAT_GGX_DIELECTRIC))
+        if (!(m.alpha >= 0.f) && (m.kind == PG3GPU_MAT_GGX_CONDUCTOR || m.kind == PG3GPU_MAT_GGX_DIELECTRIC ||
+                                  m.kind == PG3GPU_MAT_SRA_LAYERED))
             return bad(PG3GPU_ERR_INVALID_ARGUMENT, "GGX roughness must be >= 0");
         if ((m.kind == PG3GPU_MAT_GGX_CONDUCTOR || m.kind == PG3GPU_MAT_GGX_DIELECTRIC ||
              m.kind == PG3GPU_MAT_SMOOTH_CONDUCTOR || m.kind == PG3GPU_MAT_SMOOTH_DIELECTRIC) &&

@@ -14,26 +14,29 @@ namespace pg3 {
 
 enum : int {
     kMatLambert = 0, kMatGgxConductor = 1, kMatGgxDielectric = 2,
-    kMatPhong = 3, kMatSmoothConductor = 4, kMatSmoothDielectric = 5, kNumMatKinds = 6
+    kMatPhong = 3, kMatSmoothConductor = 4, kMatSmoothDielectric = 5, kMatSra = 6, kNumMatKinds = 7
 };
 enum : int { kBgNone = 0, kBgConstant = 1, kBgEnvMap = 2 };
 enum : int { kEmCdf = 0, kEmCosine = 1, kEmSteerable = 2 };
 
-struct DevMaterial {          // 64 bytes
+struct DevMaterial {          // 80 bytes
     int kind;
-    float r, g, b;            // Lambert reflectance; Phong diffuse reflectance
-    float alpha;              // GGX roughness (already clamped)
-    float eta, etaInv;        // inner/outer, outer/inner
-    float absorb;             // conductor k
+    float r, g, b;            // Lambert reflectance; Phong diffuse reflectance; SRA inner Lambert reflectance
+    float alpha;              // GGX roughness (already clamped); SRA outer roughness
+    float eta, etaInv;        // inner/outer, outer/inner (SRA: of the outer layer)
+    float absorb;             // conductor k (SRA: of the inner conductor)
     float rrProb;             // Russian-roulette continuation probability (clamped to 0.997); Phong: the
                               // diffuse part of its view-dependent estimate
     int zeroRefl;             // zero reflectance (IsReflectanceZero): paths end here (lights)
     int vndfExact;            // GGX: exact visible-normal sampling (1) or the reference's fitted routine (0)
     float alphaS;             // GGX roughness the sampling routines and pdfs use (normally == alpha)
-    float gr, gg, gb;         // Phong glossy reflectance
-    float exponent;           // Phong lobe exponent
+    float gr, gg, gb;         // Phong glossy reflectance; SRA medium attenuation coefficients
+    float exponent;           // Phong lobe exponent; SRA medium thickness
+    int innerKind;            // SRA: kMatLambert or kMatGgxConductor
+    float innerAlpha, innerEta;   // SRA inner conductor: roughness (clamped), n / n_outer
+    float pad;
 };
-static_assert(sizeof(DevMaterial) == 64, "DevMaterial is one 64-byte record");
+static_assert(sizeof(DevMaterial) == 80, "DevMaterial is one 80-byte record");
 
 // One entry of the light table: area lights first, then point lights (the background light is
 // the id after the table).

@@ -7,7 +7,8 @@ the same material table (ids 0-12), lights of the same power. Environment-map ty
 reference reads from OpenEXR light probes need the caller's texels (``env_map``, float32
 [H, W, 3], row 0 at theta = 0): there is no EXR decoder here. Two cases differ:
 
-* the SRA layered sphere material (``SPHERES_SRA_LAYERS``, configuration 27) is not built;
+* the SRA layered sphere material (``SPHERES_SRA_LAYERS``, configuration 27) renders with the
+  one-hit algorithms only, as in the reference, whose path tracers stop on it;
 * the vertical GGX-dielectric rectangle (configuration 29) samples lights from its front side
   only (the reference also from its back side); the estimate keeps its expectation, only its
   noise differs.
@@ -158,7 +159,11 @@ def _materials(mask: int):
     elif mask & SPHERES_GGX_DIELECTRIC:
         m.append(M(S.MAT_GGX_DIELECTRIC, alpha=0.01, ior=S.GLASS_IOR, ior_outer=S.AIR_IOR))
     elif mask & SPHERES_SRA_LAYERS:
-        raise NotImplementedError("the SRA layered material (src/materials.hxx:1304-1566) is not built")
+        # outer GGX dielectric 0.010 glass in air, inner GGX conductor 0.200 silver under glass,
+        # a yellow-to-dark-red medium 0.001 thick (the defaults of src/scene.hxx:325-371)
+        m.append(M(S.MAT_SRA_LAYERED, alpha=0.01, ior=S.GLASS_IOR, ior_outer=S.AIR_IOR, absorb=S.SILVER_ABSORB,
+                   inner_kind=S.MAT_GGX_CONDUCTOR, inner_alpha=0.2, inner_ior=S.SILVER_IOR,
+                   inner_ior_outer=S.GLASS_IOR, medium_attenuation=(0.05, 0.8, 4.0), medium_thickness=0.001))
     else:
         m.append(P((0.803922, 0.803922, 0.803922), (0.5, 0.5, 0.5), 90, *sph))
     if mask & VERT_RECT_FRESNEL_DIELECTRIC:                                   # 9 vertical rectangle

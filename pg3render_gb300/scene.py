@@ -33,6 +33,7 @@ MAT_GGX_DIELECTRIC = 2
 MAT_PHONG = 3
 MAT_SMOOTH_CONDUCTOR = 4
 MAT_SMOOTH_DIELECTRIC = 5
+MAT_SRA_LAYERED = 6
 
 # Copper IOR and absorbance at ~590 nm, and the IOR of air, as the reference
 # defines them (src/materials.hxx:22-27).
@@ -56,6 +57,14 @@ class Material:
     absorb: float = 0.0                # conductor k
     glossy: Vec3 = (0.0, 0.0, 0.0)     # Phong glossy reflectance
     phong_exponent: float = 1.0        # Phong lobe exponent
+    # SRA layered: outer GGX dielectric (alpha, ior, ior_outer), inner Lambert (albedo) or GGX
+    # conductor (inner_alpha, inner_ior, inner_ior_outer, absorb), medium between them
+    inner_kind: int = 0
+    inner_alpha: float = 0.1
+    inner_ior: float = 1.0
+    inner_ior_outer: float = 1.0
+    medium_attenuation: Vec3 = (0.0, 0.0, 0.0)
+    medium_thickness: float = 0.0
 
 
 def phong(diffuse: Vec3, glossy: Vec3, exponent: float, use_diffuse: bool = True, use_glossy: bool = True) -> Material:
@@ -142,6 +151,11 @@ class Scene:
                 out.append("smooth_conductor %r %r %r" % (m.ior, m.ior_outer, m.absorb))
             elif m.kind == MAT_SMOOTH_DIELECTRIC:
                 out.append("smooth_dielectric %r %r" % (m.ior, m.ior_outer))
+            elif m.kind == MAT_SRA_LAYERED:
+                inner = ("lambert %r %r %r" % tuple(m.albedo) if m.inner_kind == MAT_LAMBERT else
+                         "ggx_conductor %r %r %r %r" % (m.inner_alpha, m.inner_ior, m.inner_ior_outer, m.absorb))
+                out.append("sra %r %r %r %s %r %r %r %r" % (m.alpha, m.ior, m.ior_outer, inner, *m.medium_attenuation,
+                                                          m.medium_thickness))
             else:
                 raise ValueError("unknown material kind %d" % m.kind)
         light_of = {ti: rad for ti, rad in self.area_lights}
@@ -355,14 +369,22 @@ def _mixed_materials_box(s: Scene, ceiling: bool) -> None:
     s.spheres.append(((-0.35, -0.5, -0.75), 0.25, m_glass))
 
 
-def cornell_mixed(width: int = 256, height: int = 256, area: bool = True, point: bool = True) -> Scene:
+def cornell_mixed(width: int = 256, height: int = 256, area: bool = True, point: bool = True,
+                  sra: bool = False) -> Scene:
     """The closed box with the reference's other materials and a point light: Phong walls
     (diffuse + grey glossy 0.5, exponent 90), a Phong sphere (yellow diffuse, glossy 0.7, exponent
     200), a smooth copper sphere and a smooth glass sphere (IOR 1.51 in air), lit by the ceiling
-    quad light and/or a 20 W point light under the ceiling."""
+    quad light and/or a 20 W point light under the ceiling. With ``sra`` the Phong sphere is an
+    SRA layered one (GGX glass coat alpha 0.05 over an orange Lambert base, a 0.01 thick blue
+    medium); the reference renders that material with the one-hit algorithms only."""
     s = Scene(_camera_for_box(width, height),
-              name="cornell_mixed%s%s_%dx%d" % ("_area" if area else "", "_point" if point else "", width, height))
+              name="cornell_mixed%s%s%s_%dx%d" % ("_area" if area else "", "_point" if point else "",
+                                                 "_sra" if sra else "", width, height))
     _mixed_materials_box(s, ceiling=True)
+    if sra:
+        s.materials[s.spheres[0][2]] = Material(MAT_SRA_LAYERED, alpha=0.05, ior=GLASS_IOR, ior_outer=AIR_IOR,
+                                                albedo=(0.81, 0.18, 0.06), inner_kind=MAT_LAMBERT,
+                                                medium_attenuation=(5.0, 2.5, 0.5), medium_thickness=0.01)
     if area:
         _ceiling_light(s)
     if point:

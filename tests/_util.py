@@ -27,13 +27,18 @@ def zscores(mean_a, var_a, mean_b, var_b):
     return (mean_a - mean_b) / np.sqrt(var_a + var_b + 1e-300)
 
 
-def z_ok(z, frac_limit=0.999, zmax=4.0):
-    """Fraction of |z| <= zmax at least frac_limit (the spec gate), plus a
-    sanity bound on the mean z (systematic bias would shift it)."""
+def z_ok(z, frac_limit=0.999, zmax=4.0, stochastic=None):
+    """Fraction of |z| <= zmax at least frac_limit (the spec gate), plus the mean and
+    standard deviation of z (systematic bias would shift the mean). stochastic (optional mask):
+    the entries with sampling variance; deterministic pixels (a constant background seen
+    directly, an emitter) have z = 0 and are left out of the two moments."""
     z = np.asarray(z).ravel()
-    z = z[np.isfinite(z)]
-    frac = float(np.mean(np.abs(z) <= zmax))
-    return frac, float(np.mean(z)), float(np.std(z))
+    keep = np.isfinite(z)
+    frac = float(np.mean(np.abs(z[keep]) <= zmax))
+    if stochastic is not None:
+        keep &= np.asarray(stochastic).ravel()
+    zz = z[keep]
+    return frac, float(np.mean(zz)), float(np.std(zz))
 
 
 def scene_from_golden(d):
@@ -41,7 +46,9 @@ def scene_from_golden(d):
     from pg3render_gb300 import scene as S
     text = str(d["scene_text"])
     name = text.splitlines()[0][2:].strip()
-    if name.startswith("reference_scene_"):
+    if name.startswith("cornell_mixed_area_point_sra_"):
+        s = S.cornell_mixed(32, 32, sra=True)
+    elif name.startswith("reference_scene_"):
         from pg3render_gb300 import presets as PR
         s = PR.reference_scene(int(name.split("_")[2]), 32, 32)
     elif name.startswith("cornell_mixed_area_point_"):

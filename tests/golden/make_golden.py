@@ -66,6 +66,8 @@ CASES = {
     "cornell_mixed_32_dbs": (lambda: S.cornell_mixed(32, 32), 8, "cdf", "dbs", 256, 128),
     "cornell_mixed_32_sb4_iic16": (lambda: S.cornell_mixed(32, 32), 0, "cdf", "pt", 256, 64, (4, 1.0, 1.0, 16.0)),
     "cornell_envmixed_32_cdf": (lambda: S.cornell_env_mixed(32, 32, 64, 32), 12, "cdf", "pt", 256, 128),
+    "cornell_mixedsra_32_dmis": (lambda: S.cornell_mixed(32, 32, sra=True), 8, "cdf", "dmis", 256, 128),
+    "cornell_mixedsra_32_dbs": (lambda: S.cornell_mixed(32, 32, sra=True), 8, "cdf", "dbs", 256, 128),
 }
 
 # The reference's own built-in scenes (Scene::LoadCornellBox, -s ids of src/config.hxx:45-115):
@@ -84,6 +86,9 @@ PRESET_CASES = {
     "preset_31": (31, 8, "pt", 256, 128),    # light box, smooth dielectric sphere in the box
     "preset_38": (38, 8, "pt", 256, 128),     # layered sphere (GGX dielectric around a GGX conductor)
     "preset_12_dmis": (12, 8, "dmis", 64, 128),
+    # the SRA layered sphere: the reference renders it with the one-hit algorithms only
+    "preset_27_dmis": (27, 8, "dmis", 64, 128),
+    "preset_27_dlss": (27, 8, "dlss", 64, 128),
 }
 
 EM_TOKEN = "@EM@"

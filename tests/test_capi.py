@@ -113,9 +113,23 @@ def test_phong_smooth_and_point_light_validation():
     st, err = _create(s)
     assert st == _lib.ERR_INVALID_ARGUMENT and "point light" in err
     s = S.cornell_mixed(8, 8)
-    s.materials[0].kind = 6
+    s.materials[0].kind = 7
     st, err = _create(s)
     assert st == _lib.ERR_INVALID_ARGUMENT and "unknown kind" in err
+
+
+def test_sra_layered_validation():
+    s = S.cornell_mixed(8, 8, sra=True)
+    st, err = _create(s, algorithm=5)
+    assert st == _lib.ERR_CUDA and "device" in err           # valid (no GPU here)
+    i = next(k for k, m in enumerate(s.materials) if m.kind == S.MAT_SRA_LAYERED)
+    for field, value, msg in [("inner_kind", S.MAT_PHONG, "inner layer"), ("medium_thickness", -1.0, "medium"),
+                              ("medium_attenuation", (0.0, np.nan, 1.0), "medium")]:
+        s = S.cornell_mixed(8, 8, sra=True)
+        setattr(s.materials[i], field, value)
+        st, err = _create(s, algorithm=5)
+        assert st == _lib.ERR_INVALID_ARGUMENT and msg in err, (field, st, err)
+    assert "sra 0.05 1.51 1.000277 lambert" in S.cornell_mixed(8, 8, sra=True).to_text()
 
 
 def test_phong_constructor_halves_diffuse_with_glossy_lobe():

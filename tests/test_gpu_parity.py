@@ -27,7 +27,9 @@ GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr"
                 "cornell_mixed_32_sb4_iic16", "cornell_envmixed_32_cdf",
                 # the reference's own built-in scenes (-s ids), built here by pg3render_gb300.presets
                 "preset_00", "preset_01", "preset_03", "preset_05", "preset_07", "preset_12", "preset_16",
-                "preset_19", "preset_29", "preset_31", "preset_38", "preset_12_dmis"]
+                "preset_19", "preset_29", "preset_31", "preset_38", "preset_12_dmis",
+                # the SRA layered material (one-hit algorithms, as in the reference)
+                "preset_27_dmis", "preset_27_dlss", "cornell_mixedsra_32_dmis", "cornell_mixedsra_32_dbs"]
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
 # the reference's acronyms of its algorithm ids (src/config.hxx:147-170)
 ALG_IDS = {"el": 0, "nv": 1, "dbs": 2, "dlsa": 3, "dlss": 4, "dmis": 5, "ptn": 6, "pt": 7}
@@ -184,6 +186,34 @@ def test_mixed_materials_and_point_light_path_by_path(case, tmp_path):
     assert np.isfinite(g).all() and g.max() > 0
 
 
+@pytest.mark.parametrize("alg", [2, 3, 4, 5])
+def test_sra_layered_material_path_by_path(alg, tmp_path):
+    """The SRA layered material (GGX coat over a Lambert base, and the reference's scene 27 with a
+    conductor base) through the one-hit algorithms, against the oracle sample by sample."""
+    from pg3render_gb300 import presets as PR
+    names = ["el", "nv", "dbs", "dlsa", "dlss", "dmis"]
+    for scene in (S.cornell_mixed(24, 24, sra=True), PR.reference_scene(27, 24, 24)):
+        text = scene.to_text(algorithm=names[alg], max_path_length=8)
+        seed = 71
+        with P.GpuPathTracer(_cfg(scene, 8, alg), seed=seed) as r:
+            g = r.render_samples(alg, 0, 8)
+        o = _oracle_samples(scene, text, 8, seed, 0)
+        frac = _match_fraction(g, o)
+        assert frac >= MIN_MATCH, "%s: only %.4f of samples match the oracle" % (scene.name, frac)
+        assert np.isfinite(g).all() and g.max() > 0
+
+
+def test_sra_layered_material_is_refused_by_the_path_tracers():
+    scene = S.cornell_mixed(16, 16, sra=True)
+    with P.GpuPathTracer(_cfg(scene, 8, P.renderer.kDirectIllumMis)) as r:
+        for alg in (P.renderer.kPathTracing, P.renderer.kPathTracingNaive):
+            with pytest.raises(P.Pg3Error) as e:
+                r.RunIteration(alg, 0, 1)
+            assert "SRA" in str(e.value)
+        r.RunIteration(P.renderer.kDirectIllumMis, 0, 2)
+        assert r.iterations == 2
+
+
 @pytest.mark.parametrize("sid", [1, 5, 12, 16, 29, 31, 36, 38])
 def test_reference_scenes_path_by_path(sid, tmp_path):
     """The reference's built-in scenes (presets) through the wavefront pipeline, against the
@@ -214,7 +244,8 @@ def test_against_reference_golden(name):
         mean, var, n = r.framebuffer(with_variance=True)
         assert n == spp and r.WasUsed()
     z = zscores(mean, var / spp, d["mean"], d["var_mean"])
-    frac, zm, zs = z_ok(z)
+    # (deterministic pixels carry fp64 rounding in their variance: relative threshold)
+    frac, zm, zs = z_ok(z, stochastic=(var / spp + d["var_mean"]) > 1e-10 * d["mean"] ** 2)
     assert frac >= 0.999, "%s: only %.4f of |z| <= 4 (mean z %.3f, std %.3f)" % (name, frac, zm, zs)
     if name not in VISUALISERS:   # (deterministic inside a surface: no z distribution there)
         assert abs(zm) < 0.25 and 0.7 < zs < 1.3, "%s: z distribution off (mean %.3f, std %.3f)" % (name, zm, zs)

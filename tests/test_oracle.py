@@ -27,7 +27,9 @@ GOLDEN_CASES = ["cornell_area_32", "cornell_area_32_naive", "cornell_area_32_rr"
                 "cornell_mixed_32_sb4_iic16", "cornell_envmixed_32_cdf",
                 # the reference's own built-in scenes (-s ids), built here by pg3render_gb300.presets
                 "preset_00", "preset_01", "preset_03", "preset_05", "preset_07", "preset_12", "preset_16",
-                "preset_19", "preset_29", "preset_31", "preset_38", "preset_12_dmis"]
+                "preset_19", "preset_29", "preset_31", "preset_38", "preset_12_dmis",
+                # the SRA layered material (one-hit algorithms, as in the reference)
+                "preset_27_dmis", "preset_27_dlss", "cornell_mixedsra_32_dmis", "cornell_mixedsra_32_dbs"]
 # the visualisers are deterministic inside a surface (zero variance): only the fraction of
 # |z| <= 4 is a meaningful statistic for them
 VISUALISERS = ("cornell_area_32_el", "cornell_area_32_nv")
@@ -56,11 +58,12 @@ def test_oracle_matches_reference_golden(name):
            "cornell_envmixed_32_cdf": 8192,
            "preset_00": 8192, "preset_03": 8192, "preset_07": 8192, "preset_29": 8192, "preset_01": 32768,
            "preset_05": 32768, "preset_16": 32768, "preset_19": 32768, "preset_31": 32768,
-           "preset_38": 32768}.get(name, 1024)
+           "preset_38": 32768, "preset_27_dmis": 8192, "preset_27_dlss": 8192, "cornell_mixedsra_32_dmis": 8192,
+           "cornell_mixedsra_32_dbs": 8192}.get(name, 1024)
     o = O.render(text, 32, 32, seed=99, spp=spp, em_sampler=sampler)
     m = o["sum"] / spp
     v = np.maximum(o["sumsq"] / spp - m * m, 0.0) / spp
-    frac, zm, zs = z_ok(zscores(m, v, d["mean"], d["var_mean"]))
+    frac, zm, zs = z_ok(zscores(m, v, d["mean"], d["var_mean"]), stochastic=(v + d["var_mean"]) > 1e-10 * m * m)
     assert frac >= 0.999, "%s: %.4f of |z| <= 4" % (name, frac)
     if name not in VISUALISERS:
         assert abs(zm) < 0.25 and 0.7 < zs < 1.3, "%s: z mean %.3f std %.3f" % (name, zm, zs)

@@ -1,5 +1,5 @@
-"""The reference's built-in scenes (pg3render_gb300.presets): every -s id builds (the SRA
-layered sphere, id 27, is reported as not built), and the scenes carry the reference's lights.
+"""The reference's built-in scenes (pg3render_gb300.presets): every -s id builds, and the scenes
+carry the reference's lights.
 Their renders are checked against the reference's own scene construction by the preset_*
 golden fixtures (tests/test_oracle.py, tests/test_gpu_parity.py)."""
 import math
@@ -13,10 +13,6 @@ from pg3render_gb300 import scene as S
 
 def test_every_scene_id_builds():
     for sid in range(len(PR.SCENE_CONFIGS)):
-        if sid == 27:
-            with pytest.raises(NotImplementedError):
-                PR.reference_scene(sid, 8, 8)
-            continue
         sc = PR.reference_scene(sid, 8, 8)
         assert len(sc.materials) == 13 and sc.num_lights >= 1
         mask = PR.SCENE_CONFIGS[sid]
@@ -24,6 +20,7 @@ def test_every_scene_id_builds():
         assert sc.has_background == bool(mask & PR.LIGHT_ENV)
         text = sc.to_text(max_path_length=8)
         assert text.startswith("# reference_scene_%d" % sid)
+        assert ("\nsra " in text) == (sid == 27)   # the SRA layered sphere
 
 
 def test_area_lights_emit_25_watts():
