@@ -471,10 +471,41 @@ def inverse_metric():
     return r
 
 
+def mesh_metric(reps=3):
+    """The environment-map box with its spheres as triangle meshes (two icospheres of 20480
+    triangles each, 40968 triangles in all), 512x512 x 64 spp, steerable sampler: every closest-hit
+    and any-hit query runs through the device LBVH (the list loop would test every triangle)."""
+    import torch
+    import pg3render_gb300 as P
+    from pg3render_gb300 import scene as S
+    R = P.renderer
+    sc = S.cornell_env_mesh(512, 512, 1024, 512, level=5)
+    spp = 64
+    cfg = P.Config(scene=sc, max_path_length=12, rr_min_path_length=4, em_sampler=R.EM_STEERABLE,
+                   traversal=R.TRAVERSAL_BVH)
+    with P.GpuPathTracer(cfg) as r:
+        r.RunIteration(R.kPathTracing, 0, spp)
+        r.synchronize()
+        ts = []
+        for rep in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r.RunIteration(R.kPathTracing, (rep + 1) * spp, spp)
+            r.synchronize()
+            ts.append(time.perf_counter() - t0)
+        st = r.stats()
+    t = statistics.median(ts)
+    paths = 512 * 512 * spp
+    return {"metric": "Msamples/s (LBVH traversal)", "triangles": len(sc.triangles), "spp": spp,
+            "msamples_per_s": round(paths / t / 1e6, 1), "ms_per_run": round(t * 1e3, 2),
+            "segments_per_path": round(st["extension_rays"] / max(1, st["paths"]), 3),
+            "timing": "host wall clock of whole runs incl. synchronisation, median of %d" % reps}
+
+
 def secondary_metrics():
     out = {}
     for name, fn in (("batched", batched_metric), ("differentiable", differentiable_metric),
-                     ("inverse_rendering", inverse_metric)):
+                     ("inverse_rendering", inverse_metric), ("mesh_bvh", mesh_metric)):
         try:
             out[name] = fn()
         except Exception as e:   # reported, never hidden

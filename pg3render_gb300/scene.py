@@ -402,6 +402,53 @@ def cornell_env_mixed(width: int = 256, height: int = 256, em_width: int = 512, 
     return s
 
 
+def icosphere(level: int) -> Tuple[np.ndarray, np.ndarray]:
+    """Unit icosahedron subdivided 4-way ``level`` times with midpoints pushed to the sphere:
+    (vertices [V, 3] float64, faces [20 * 4^level, 3] int, counter-clockwise seen from outside)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.asarray(p, np.float64) / np.linalg.norm(p) for p in v]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(level):
+        mid = {}
+
+        def m(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                p = verts[a] + verts[b]
+                verts.append(p / np.linalg.norm(p))
+                mid[key] = len(verts) - 1
+            return mid[key]
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = m(a, b), m(b, c), m(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts), np.array(faces)
+
+
+def cornell_env_mesh(width: int = 512, height: int = 512, em_width: int = 1024, em_height: int = 512,
+                     level: int = 5, em_seed: int = 7) -> Scene:
+    """cornell_env with its two spheres as triangle meshes (icospheres of ``level`` subdivisions,
+    20 * 4^level flat triangles each; 40968 triangles in all at level 5): the closest-hit and
+    any-hit queries run through the device LBVH instead of the primitive list."""
+    s = Scene(_camera_for_box(width, height), name="cornell_envmesh_%dx%d_l%d" % (width, height, level))
+    _box(s, ceiling=False)
+    m_diel = s.add_material(Material(MAT_GGX_DIELECTRIC, alpha=0.3, ior=1.5, ior_outer=1.0))
+    m_cond = s.add_material(Material(MAT_GGX_CONDUCTOR, alpha=0.05, ior=COPPER_IOR, ior_outer=AIR_IOR,
+                                     absorb=COPPER_ABSORB))
+    verts, faces = icosphere(level)
+    for centre, mat in (((-0.45, 0.25, -0.65), m_diel), ((0.45, -0.25, -0.65), m_cond)):
+        p = verts * 0.35 + np.asarray(centre)
+        for a, b, c in faces:
+            s.add_triangle(p[a], p[b], p[c], mat)
+    s.env_map = synthetic_sky(em_width, em_height, seed=em_seed)
+    return s
+
+
 def cornell_env_diff(width: int = 256, height: int = 256, em_width: int = 512, em_height: int = 256,
                      em_seed: int = 7) -> Scene:
     """The environment-lit box for gradients: four Lambert materials (floor, back wall, red

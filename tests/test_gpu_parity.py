@@ -186,6 +186,22 @@ def test_mixed_materials_and_point_light_path_by_path(case, tmp_path):
     assert np.isfinite(g).all() and g.max() > 0
 
 
+def test_triangle_mesh_scene_through_the_lbvh_path_by_path(tmp_path):
+    """The environment box with icosphere meshes (1288 triangles): the LBVH wavefront against the
+    oracle's list loop, sample by sample."""
+    scene = S.cornell_env_mesh(24, 24, 64, 32, level=3)
+    em = str(tmp_path / "em.bin")
+    scene.write_env_map(em)
+    text = scene.to_text(em_path=em, max_path_length=12)
+    seed = 83
+    cfg = _cfg(scene, 12, P.renderer.kPathTracing, P.renderer.EM_CDF, traversal=P.renderer.TRAVERSAL_BVH)
+    with P.GpuPathTracer(cfg, seed=seed) as r:
+        g = r.render_samples(P.renderer.kPathTracing, 0, 4)
+    o = _oracle_samples(scene, text, 4, seed, 0)
+    frac = _match_fraction(g, o)
+    assert frac >= MIN_MATCH, "only %.4f of samples match the oracle" % frac
+
+
 @pytest.mark.parametrize("alg", [2, 3, 4, 5])
 def test_sra_layered_material_path_by_path(alg, tmp_path):
     """The SRA layered material (GGX coat over a Lambert base, and the reference's scene 27 with a
