@@ -5,7 +5,7 @@
 * the sampled directions pass a chi-square goodness-of-fit test against that
   pdf, integrated per equal-area bin (low-expectation bins pooled).
 
-Samplers: Lambert, GGX conductor and GGX dielectric BSDFs; the area light; the
+Samplers: Lambert, GGX conductor, GGX dielectric and Phong BSDFs; the area light; the
 environment map's cosine, CDF and (corrected) steerable samplers.
 """
 import numpy as np
@@ -28,7 +28,11 @@ def _bsdf_scene():
             S.Material(S.MAT_GGX_CONDUCTOR, alpha=0.3, ior=S.COPPER_IOR, ior_outer=S.AIR_IOR, absorb=S.COPPER_ABSORB),
             S.Material(S.MAT_GGX_CONDUCTOR, alpha=0.1, ior=S.COPPER_IOR, ior_outer=S.AIR_IOR, absorb=S.COPPER_ABSORB),
             S.Material(S.MAT_GGX_DIELECTRIC, alpha=0.3, ior=1.5, ior_outer=1.0),
-            S.Material(S.MAT_GGX_DIELECTRIC, alpha=0.5, ior=1.5, ior_outer=1.0)]
+            S.Material(S.MAT_GGX_DIELECTRIC, alpha=0.5, ior=1.5, ior_outer=1.0),
+            # Phong: a diffuse + glossy mixture and a glossy-dominant lobe (component choice by
+            # the luminance estimates, power-cosine lobe around the mirror direction)
+            S.phong((0.6, 0.5, 0.4), (0.5, 0.5, 0.5), 20),
+            S.phong((0.05, 0.05, 0.05), (0.8, 0.8, 0.8), 60)]
     for m in mats:
         s.add_material(m)
     s.add_triangle((-1, 0, -1), (1, 0, -1), (0, 0, 1), 0)
@@ -51,7 +55,8 @@ def _wol(theta_deg, below=False):
     return -w if below else w
 
 
-BSDF_CASES = [(0, 40, False), (1, 45, False), (2, 30, False), (3, 50, False), (3, 35, True), (4, 60, False)]
+BSDF_CASES = [(0, 40, False), (1, 45, False), (2, 30, False), (3, 50, False), (3, 35, True), (4, 60, False),
+              (5, 30, False), (6, 55, False)]
 
 
 @pytest.mark.parametrize("mat,theta,below", BSDF_CASES)
