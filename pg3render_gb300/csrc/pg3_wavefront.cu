@@ -68,7 +68,13 @@ __global__ void __launch_bounds__(kWaveBlock) raygenKernel(const __grid_constant
     }
 }
 
-__global__ void __launch_bounds__(kWaveBlock) extendKernel(const __grid_constant__ SceneView S, Queues Q, int cur,
+// Resident blocks per SM the ray-query kernels (extend, shadow) are compiled and launched for:
+// their few registers allow more warps than the shade kernels' grid provides.
+#ifndef PG3_QUERY_MIN_BLOCKS
+#define PG3_QUERY_MIN_BLOCKS 6
+#endif
+
+__global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) extendKernel(const __grid_constant__ SceneView S, Queues Q, int cur,
                                                            DevStats *stats)
 {
     const uint32_t n = Q.cnt->ray[cur];
@@ -147,7 +153,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
 }
 
 template <bool GRAD>
-__global__ void __launch_bounds__(kWaveBlock) shadowKernel(const __grid_constant__ SceneView S, Queues Q,
+__global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) shadowKernel(const __grid_constant__ SceneView S, Queues Q,
                                                            float *outR, float *outG, float *outB, DevStats *stats,
                                                            GradArgs G)
 {
@@ -252,6 +258,8 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
     Queues Q = carve(scratch, capacity, GRAD);
     Q.err = S.errorFlag;
     const uint32_t maxBounces = S.maxPL > 0 ? S.maxPL : kMaxPathLengthHard;
+    // (gridBlocks is SMs x the shade kernels' 1024 threads per SM)
+    const int queryGrid = std::max(1, gridBlocks / (1024 / kWaveBlock)) * PG3_QUERY_MIN_BLOCKS;
     const size_t smem = GRAD ? 16 * (size_t)S.nmat : 0;
     cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(stream, &capturing);
@@ -270,7 +278,7 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
         *launches += 1;
         for (uint32_t bounce = 0; bounce < maxBounces; ++bounce) {
             const int cur = bounce & 1;
-            extendKernel<<<gridBlocks, kWaveBlock, 0, stream>>>(S, Q, cur, stats);
+            extendKernel<<<queryGrid, kWaveBlock, 0, stream>>>(S, Q, cur, stats);
             const int emk = (S.bgKind == kBgEnvMap) ? S.emSampler : kEmCosine;   // no map: constant/area paths
             const uint32_t b32 = (uint32_t)base;
             int shades;
@@ -280,7 +288,7 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
                 shades = launchShade<kEmSteerable, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
             else
                 shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
-            shadowKernel<GRAD><<<gridBlocks, kWaveBlock, smem, stream>>>(S, Q, r, g, b, stats, G);
+            shadowKernel<GRAD><<<queryGrid, kWaveBlock, smem, stream>>>(S, Q, r, g, b, stats, G);
             advanceKernel<<<1, 1, 0, stream>>>(Q.cnt, cur);
             *launches += 3 + shades;
             if (S.maxPL == 0 && (bounce & 7) == 7 && capturing == cudaStreamCaptureStatusNone) {
