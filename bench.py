@@ -43,6 +43,7 @@ METRIC = "Msamples/s at matched rel-MSE vs CPU"
 UNIT = "Msamples/s"
 WIDTH = HEIGHT = 512
 SPP = 256
+MESH_SIDE, MESH_SPP = 512, 64
 MAX_PATH = 12
 RR_FROM = 4            # Russian roulette from path length 4, i.e. after 3 bounces
 EM_W, EM_H = 1024, 512
@@ -72,10 +73,16 @@ def parse():
     ap.add_argument("--paths-in-flight", type=int, default=0, help="wavefront chunk size (0: automatic)")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the batched (64 scenes), forward+adjoint and inverse-rendering measurements")
+    ap.add_argument("--only-secondary", default=None,
+                    choices=["batched", "differentiable", "inverse_rendering", "mesh_bvh"],
+                    help="run one secondary measurement alone and print its JSON (profiling captures)")
+    ap.add_argument("--mesh-side", type=int, default=512, help="image side of the LBVH mesh measurement")
+    ap.add_argument("--mesh-spp", type=int, default=64, help="samples per pixel of the LBVH mesh measurement")
     a = ap.parse_args()
-    global WIDTH, HEIGHT, SPP
+    global WIDTH, HEIGHT, SPP, MESH_SIDE, MESH_SPP
     WIDTH = HEIGHT = a.width
     SPP = a.spp
+    MESH_SIDE, MESH_SPP = a.mesh_side, a.mesh_spp
     return a
 
 
@@ -473,14 +480,16 @@ def inverse_metric():
 
 def mesh_metric(reps=3):
     """The environment-map box with its spheres as triangle meshes (two icospheres of 20480
-    triangles each, 40968 triangles in all), 512x512 x 64 spp, steerable sampler: every closest-hit
-    and any-hit query runs through the device LBVH (the list loop would test every triangle)."""
+    triangles each, 40968 triangles in all), 512x512 x 64 spp by default, steerable sampler: every
+    closest-hit and any-hit query runs through the device LBVH (the list loop would test every
+    triangle)."""
     import torch
     import pg3render_gb300 as P
     from pg3render_gb300 import scene as S
     R = P.renderer
-    sc = S.cornell_env_mesh(512, 512, 1024, 512, level=5)
-    spp = 64
+    side = MESH_SIDE
+    sc = S.cornell_env_mesh(side, side, 1024, 512, level=5)
+    spp = MESH_SPP
     cfg = P.Config(scene=sc, max_path_length=12, rr_min_path_length=4, em_sampler=R.EM_STEERABLE,
                    traversal=R.TRAVERSAL_BVH)
     with P.GpuPathTracer(cfg) as r:
@@ -495,17 +504,19 @@ def mesh_metric(reps=3):
             ts.append(time.perf_counter() - t0)
         st = r.stats()
     t = statistics.median(ts)
-    paths = 512 * 512 * spp
-    return {"metric": "Msamples/s (LBVH traversal)", "triangles": len(sc.triangles), "spp": spp,
+    paths = side * side * spp
+    return {"metric": "Msamples/s (LBVH traversal)", "triangles": len(sc.triangles), "side": side, "spp": spp,
             "msamples_per_s": round(paths / t / 1e6, 1), "ms_per_run": round(t * 1e3, 2),
             "segments_per_path": round(st["extension_rays"] / max(1, st["paths"]), 3),
             "timing": "host wall clock of whole runs incl. synchronisation, median of %d" % reps}
 
 
-def secondary_metrics():
+def secondary_metrics(only=None):
     out = {}
     for name, fn in (("batched", batched_metric), ("differentiable", differentiable_metric),
                      ("inverse_rendering", inverse_metric), ("mesh_bvh", mesh_metric)):
+        if only and name != only:
+            continue
         try:
             out[name] = fn()
         except Exception as e:   # reported, never hidden
@@ -549,6 +560,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.only_secondary:
+        line = secondary_metrics(args.only_secondary) if rank == 0 else None
     else:
         if world > 1:
             import torch

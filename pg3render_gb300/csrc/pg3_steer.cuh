@@ -248,19 +248,27 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
             cum += val[i];
         }
         // children occupy the first slots; the first one whose running sum exceeds t wins,
-        // rounding past the end falls back to the last child
+        // rounding past the end falls back to the last child. The scan is unrolled over the
+        // six slots with the chosen child's value and id carried in registers (an indexed
+        // pick would place ids[] and val[] in local memory).
         const float t = u * 0.999999f * cum;
-        float lo = 0.f;
-        int pick = -1, last = -1;
-        for (int i = 0; i < 6 && ids[i] != INT_MIN; ++i) {
-            last = i;
-            if (t < lo + val[i]) { pick = i; break; }
-            lo += val[i];
+        float lo = 0.f, vPick = 0.f;
+        int idPick = INT_MIN;
+        bool alive = true, found = false;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            alive = alive && ids[i] != INT_MIN;
+            if (alive && !found) {
+                vPick = val[i];
+                idPick = ids[i];
+                if (t < lo + val[i]) found = true;
+                else lo += val[i];
+            }
         }
-        if (last < 0) { atomicOr(S.errorFlag, kErrSteerDescent); return false; }
-        if (pick < 0) { pick = last; lo -= val[last]; }
-        u = fminf((t - lo) / fmaxf(val[pick], 1e-30f), 1.f);
-        const int id = ids[pick];
+        if (idPick == INT_MIN) { atomicOr(S.errorFlag, kErrSteerDescent); return false; }
+        if (!found) lo -= vPick;
+        u = fminf((t - lo) / fmaxf(vPick, 1e-30f), 1.f);
+        const int id = idPick;
         if (id < 0) { leaf = ~id; break; }
         node = id;
     }

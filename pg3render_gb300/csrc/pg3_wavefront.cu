@@ -97,13 +97,34 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) extendKernel
     countWarp(&stats->extRays, rays);
 }
 
-// Resident blocks per SM the shade kernels are compiled for (register budget 65536 / (256 x N)).
+// Resident blocks per SM each shade kernel is compiled and launched for (register budget
+// 65536 / (256 x N)): the miss (background) kernel holds no material code and fits 4.
 #ifndef PG3_SHADE_MIN_BLOCKS
 #define PG3_SHADE_MIN_BLOCKS 2
 #endif
+#ifndef PG3_MISS_MIN_BLOCKS
+#define PG3_MISS_MIN_BLOCKS 4
+#endif
+#ifndef PG3_LAMBERT_MIN_BLOCKS
+#define PG3_LAMBERT_MIN_BLOCKS PG3_SHADE_MIN_BLOCKS
+#endif
+#ifndef PG3_CONDUCTOR_MIN_BLOCKS
+#define PG3_CONDUCTOR_MIN_BLOCKS PG3_SHADE_MIN_BLOCKS
+#endif
+#ifndef PG3_DIELECTRIC_MIN_BLOCKS
+#define PG3_DIELECTRIC_MIN_BLOCKS PG3_SHADE_MIN_BLOCKS
+#endif
+constexpr int shadeMinBlocks(int K)
+{
+    return K < 0                      ? PG3_MISS_MIN_BLOCKS
+           : K == kMatLambert         ? PG3_LAMBERT_MIN_BLOCKS
+           : K == kMatGgxConductor    ? PG3_CONDUCTOR_MIN_BLOCKS
+           : K == kMatGgxDielectric   ? PG3_DIELECTRIC_MIN_BLOCKS
+                                      : PG3_SHADE_MIN_BLOCKS;
+}
 
 template <int K, int EMK, bool GRAD>
-__global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
     shadeKernel(const __grid_constant__ SceneView S, Queues Q, int cur, uint32_t base0, uint32_t npix,
                 uint32_t sample0, float *outR, float *outG, float *outB, DevStats *stats, GradArgs G)
 {
@@ -218,6 +239,18 @@ Queues carve(void *scratch, uint64_t cap, bool grad)
     return q;
 }
 
+// One shade kernel: grid = SMs x 1024 / kWaveBlock on entry; the kernel gets two waves of the
+// blocks it is compiled to keep resident per SM.
+template <int K, int EMK, bool GRAD>
+void launchShadeKind(const SceneView &S, const Queues &Q, int cur, uint32_t base, uint32_t npix, uint32_t sample0,
+                     float *r, float *g, float *b, DevStats *stats, int grid, size_t smem, const GradArgs &G,
+                     cudaStream_t st, int &launched)
+{
+    const int blocks = std::max(1, grid / (1024 / kWaveBlock)) * 2 * shadeMinBlocks(K);
+    shadeKernel<K, EMK, GRAD><<<blocks, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+    ++launched;
+}
+
 // The shade kernels of one bounce (the miss bucket and the material kinds of the scene),
 // specialised on the environment-map sampler. Returns the number of launches.
 template <int EMK, bool GRAD>
@@ -225,28 +258,18 @@ int launchShade(const SceneView &S, uint32_t kindMask, const Queues &Q, int cur,
                 uint32_t sample0, float *r, float *g, float *b, DevStats *stats, int grid, size_t smem,
                 const GradArgs &G, cudaStream_t st)
 {
-    int n = 1;
-    shadeKernel<-1, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-    if (kindMask & (1u << kMatLambert)) {
-        shadeKernel<kMatLambert, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-        ++n;
-    }
-    if (kindMask & (1u << kMatGgxConductor)) {
-        shadeKernel<kMatGgxConductor, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-        ++n;
-    }
-    if (kindMask & (1u << kMatGgxDielectric)) {
-        shadeKernel<kMatGgxDielectric, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-        ++n;
-    }
-    if (kindMask & (1u << kMatPhong)) {
-        shadeKernel<kMatPhong, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-        ++n;
-    }
-    if (kindMask & ((1u << kMatSmoothConductor) | (1u << kMatSmoothDielectric))) {
-        shadeKernel<kShadeSmooth, EMK, GRAD><<<grid, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
-        ++n;
-    }
+    int n = 0;
+    launchShadeKind<-1, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+    if (kindMask & (1u << kMatLambert))
+        launchShadeKind<kMatLambert, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+    if (kindMask & (1u << kMatGgxConductor))
+        launchShadeKind<kMatGgxConductor, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+    if (kindMask & (1u << kMatGgxDielectric))
+        launchShadeKind<kMatGgxDielectric, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+    if (kindMask & (1u << kMatPhong))
+        launchShadeKind<kMatPhong, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+    if (kindMask & ((1u << kMatSmoothConductor) | (1u << kMatSmoothDielectric)))
+        launchShadeKind<kShadeSmooth, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
     return n;
 }
 
