@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kWaveBlock) batchRegen(const SceneView *views,
     const unsigned long long g0 = ctl->regenBase;
     const uint32_t top = ctl->regenFreeTop;
     const int cur = (int)ctl->cur;
-    float4 *rq = B.q.ray[cur];
+    float4 *rq = rayQ(B.q, cur);
     for (uint32_t base = blockIdx.x * blockDim.x; base < k; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const bool want = i < k;
@@ -150,15 +150,15 @@ __global__ void __launch_bounds__(kWaveBlock) batchRegen(const SceneView *views,
             r0 = make_float4(S.camPos.x, S.camPos.y, S.camPos.z, 0.f);
             r1 = make_float4(dir.x, dir.y, dir.z, __uint_as_float(slot | (id << kSlotBits)));
             B.local[slot] = local;
-            initPathState(B.q, slot);
             B.outR[slot] = 0.f;
             B.outG[slot] = 0.f;
             B.outB[slot] = 0.f;
         }
         const uint32_t pos = warpAppend(&B.q.cnt->ray[cur], want);
         if (want && pos < B.q.cap) {
-            rq[2 * pos] = r0;
-            rq[2 * pos + 1] = r1;
+            rq[2 * (size_t)pos] = r0;
+            rq[2 * (size_t)pos + 1] = r1;
+            initPathState(B.q, cur, pos);
         } else if (want) {
             atomicOr(B.q.err, kErrQueueOverflow);
         }
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kWaveBlock) batchExtend(const SceneView *views
     const SceneView *sv = stageViews(views, ninst, smem);
     const int cur = (int)ctl->cur;
     const uint32_t n = B.q.cnt->ray[cur];
-    const float4 *rq = B.q.ray[cur];
+    const float4 *rq = rayQ(B.q, cur);
     uint32_t rays = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
     constexpr int kBucket = bucketOfShade(K);
     const int cur = (int)ctl->cur;
     const uint32_t n = B.q.cnt->bucket[kBucket];
-    const float4 *rq = B.q.ray[cur];
+    const float4 *rq = rayQ(B.q, cur);
     const GradArgs G{};
     PathCounters pc;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
             const uint32_t npix = __ldg(&inst[id].npix);
             const uint32_t pixel = local % npix, sample = __ldg(&inst[id].sample0) + local / npix;
             float3 L;
-            shadeVertex<K, EMK, false>(sv[id], B.q, idx, r0, r1, slot, tag, pixel, sample, pc, o, L, G, nullptr,
-                                       f3(0.f));
+            shadeVertex<K, EMK, false>(sv[id], B.q, idx, r0, r1, stQ(B.q, cur) + 3 * (size_t)idx, slot, tag, pixel, sample,
+                                       pc, o, L, G, nullptr, f3(0.f));
             if (!isZero(L)) {
                 B.outR[slot] += L.x;
                 B.outG[slot] += L.y;
@@ -316,7 +316,7 @@ size_t a256(size_t b) { return (b + 255) & ~size_t(255); }
 size_t batchBytes(uint64_t cap)
 {
     return a256(sizeof(Counters)) + a256(sizeof(BatchCtl)) + 2 * a256(32 * cap) + a256(8 * cap) +
-           kNumBuckets * a256(4 * cap) + 3 * a256(16 * cap) + a256(48 * cap) + 3 * a256(4 * cap) + 2 * a256(4 * cap);
+           kNumBuckets * a256(4 * cap) + 2 * a256(48 * cap) + a256(48 * cap) + 3 * a256(4 * cap) + 2 * a256(4 * cap);
 }
 
 void carveBatch(void *scratch, uint64_t cap, BatchQ &B, BatchCtl *&ctl)
@@ -329,9 +329,9 @@ void carveBatch(void *scratch, uint64_t cap, BatchQ &B, BatchCtl *&ctl)
     B.q.ray[1] = (float4 *)take(32 * cap);
     B.q.hit = (float2 *)take(8 * cap);
     for (int b = 0; b < kNumBuckets; ++b) B.q.bucket[b] = (uint32_t *)take(4 * cap);
-    B.q.beta = (float4 *)take(16 * cap);
-    B.q.ew = (float4 *)take(16 * cap);
-    B.q.pn = (float4 *)take(16 * cap);
+    B.q.bucketStride = a256(4 * cap) / 4;
+    B.q.st[0] = (float4 *)take(48 * cap);
+    B.q.st[1] = (float4 *)take(48 * cap);
     B.q.shadow = (float4 *)take(48 * cap);
     B.q.pend = nullptr;
     B.q.cap = (uint32_t)cap;

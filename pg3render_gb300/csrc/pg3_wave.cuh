@@ -1,9 +1,12 @@
 // Stage code shared by the wavefront pipelines: the single-scene pipeline and its path-replay
 // adjoint (pg3_wavefront.cu) and the many-scene pipeline (pg3_batch.cu).
 //
-// A path lives in a slot: its state (beta, ew, pn; 48 bytes) and its radiance accumulator are
-// slot-indexed arrays. Rays and shadow records name their path by a tag: the slot in the low
-// 24 bits and, in the batch pipeline, the scene instance in the high 8 bits.
+// A path lives in a slot, which indexes its radiance accumulator. Its state (beta, ew, pn; 48
+// bytes) travels with its ray: the state record at position i of a state queue belongs to the ray
+// at position i of the ray queue of the same parity, so a shade kernel reads ray, hit and state
+// of a bucket entry at one index, and writes the next state where it appends the next ray. Rays
+// and shadow records name their path by a tag: the slot in the low 24 bits and, in the batch
+// pipeline, the scene instance in the high 8 bits.
 //
 // shadeVertex is one vertex of the estimator of pg3_estimator.cuh (src/path_tracer.hxx:167-430)
 // for one material kind K: emitter / background MIS, the light sample (folded into a shadow
@@ -55,10 +58,11 @@ struct Counters {
 struct Queues {
     float4 *ray[2];           // 2 float4 per entry: origin + tmin, direction + tag
     float2 *hit;              // (t, primitive as int bits)
-    uint32_t *bucket[kNumBuckets];
-    float4 *beta;             // per slot: beta.xyz, parent bsdf pdf
-    float4 *ew;               // per slot: emission weight.xyz, parent light-estimate sum
-    float4 *pn;               // per slot: parent normal.xyz, flags (path length | finite | compute-reflected)
+    uint32_t *bucket[kNumBuckets];   // consecutive: bucket[b] = bucket[0] + b * bucketStride
+    size_t bucketStride;
+    float4 *st[2];            // per ray-queue entry, 3 float4: beta.xyz + parent bsdf pdf, emission
+                              // weight.xyz + parent light-estimate sum, parent normal.xyz + flags
+                              // (path length | finite | compute-reflected)
     float4 *shadow;           // kShadowWords<GRAD> float4 per record
     float2 *pend;             // GRAD, per slot: material of the previous vertex (int bits), its d att
     Counters *cnt;
@@ -67,6 +71,12 @@ struct Queues {
 };
 
 template <bool GRAD> constexpr int kShadowWords = GRAD ? 5 : 3;
+
+// Queue q of a pair, chosen by a select: indexing the pointer pair of a kernel parameter with a
+// run-time value would copy the whole parameter to local memory.
+PG3_DI float4 *rayQ(const Queues &Q, int q) { return q ? Q.ray[1] : Q.ray[0]; }
+PG3_DI float4 *stQ(const Queues &Q, int q) { return q ? Q.st[1] : Q.st[0]; }
+PG3_DI uint32_t *bucketQ(const Queues &Q, int b) { return Q.bucket[0] + (size_t)b * Q.bucketStride; }
 
 // Warp-aggregated append: lanes with `want` get consecutive slots of *counter.
 PG3_DI uint32_t warpAppend(uint32_t *counter, bool want)
@@ -170,11 +180,12 @@ PG3_DI void flushBlockGrad(const float *sGrad, uint32_t nmat, float *gMat)
 PG3_DI void prefetchL1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 
 // Software pipelining of a shade kernel's grid-stride loop: while a thread shades one entry of
-// its bucket it pulls the next entry's ray, then that ray's path state, towards L1, so the
-// next iteration's chain of dependent loads (bucket -> ray -> state) finds them on chip.
+// its bucket it pulls the next entry's ray and hit, then its path state, towards L1, so the
+// next iteration's loads (bucket -> ray, hit, state) find them on chip.
 struct NextEntry {
     const float4 *ray = nullptr;   // the next entry's ray record (null: none)
-    const float2 *hit = nullptr;   // and its hit record
+    const float2 *hit = nullptr;   // its hit record
+    const float4 *st = nullptr;    // and its state record
 };
 PG3_DI void prefetchNextRay(const NextEntry &nx)
 {
@@ -184,13 +195,11 @@ PG3_DI void prefetchNextRay(const NextEntry &nx)
         prefetchL1(nx.hit);
     }
 }
-PG3_DI void prefetchNextState(const Queues &Q, const NextEntry &nx)
+PG3_DI void prefetchNextState(const NextEntry &nx)
 {
-    if (nx.ray) {
-        const uint32_t slot = __float_as_uint(__ldg(&nx.ray[1].w)) & kSlotMask;
-        prefetchL1(&Q.beta[slot]);
-        prefetchL1(&Q.ew[slot]);
-        prefetchL1(&Q.pn[slot]);
+    if (nx.st) {
+        prefetchL1(nx.st);
+        prefetchL1(nx.st + 2);
     }
 }
 struct ShadeOut {
@@ -198,16 +207,18 @@ struct ShadeOut {
     float4 s0, s1, s2;        // shadow record: origin + distance, direction + tag, contribution
     float4 s3, s4;            // GRAD: material gradient (albedo rgb, roughness), environment weight + material
     float4 r0, r1;            // next ray
+    float4 t0, t1, t2;        // its path state record
 };
 
 // acc: the path's radiance accumulated before this vertex (GRAD adjoint only).
+// st: the entry's path state record (3 float4).
 template <int K, int EMK, bool GRAD>
-PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float4 r0, float4 r1, uint32_t slot,
-                        uint32_t tag, uint32_t pixel, uint32_t sample, PathCounters &pc, ShadeOut &o, float3 &L,
-                        const GradArgs &G, float *sGrad, float3 acc, const NextEntry &nx = NextEntry())
+PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float4 r0, float4 r1, const float4 *st,
+                        uint32_t slot, uint32_t tag, uint32_t pixel, uint32_t sample, PathCounters &pc, ShadeOut &o,
+                        float3 &L, const GradArgs &G, float *sGrad, float3 acc, const NextEntry &nx = NextEntry())
 {
     const float3 org = xyz(r0), dir = xyz(r1);
-    const float4 sb = Q.beta[slot], se = Q.ew[slot], sn = Q.pn[slot];
+    const float4 sb = st[0], se = st[1], sn = st[2];
     const uint32_t flags = __float_as_uint(sn.w);
     const uint32_t pl = flags & 0xffffu;
     const bool prevFinite = (flags & kFlagFinite) != 0, computeRefl = (flags & kFlagRefl) != 0;
@@ -314,7 +325,7 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
             }
         }
     }
-    prefetchNextState(Q, nx);
+    prefetchNextState(nx);
     // Russian roulette (src/path_tracer.hxx:267-303)
     float rrProb = 1.0f;
     bool cut = false;
@@ -336,10 +347,10 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
     const float3 ew2 = beta * f;
     const float3 beta2 = ew2 / rrProb;
     if (cut) ++pc.rr;
-    Q.beta[slot] = make_float4(beta2.x, beta2.y, beta2.z, br.pdfW * br.compProb);
-    Q.ew[slot] = make_float4(ew2.x, ew2.y, ew2.z, sum);
+    o.t0 = make_float4(beta2.x, beta2.y, beta2.z, br.pdfW * br.compProb);
+    o.t1 = make_float4(ew2.x, ew2.y, ew2.z, sum);
     const uint32_t nf = (pl + 1) | (finite ? kFlagFinite : 0u) | (cut ? 0u : kFlagRefl);
-    Q.pn[slot] = make_float4(nrm.x, nrm.y, nrm.z, __uint_as_float(nf));
+    o.t2 = make_float4(nrm.x, nrm.y, nrm.z, __uint_as_float(nf));
     if (GRAD) Q.pend[slot] = make_float2(__int_as_float(matId), br.dAtt);
     const float3 nd = toWorld(frame, br.wil);
     o.next = true;
@@ -347,7 +358,7 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
     o.r1 = make_float4(nd.x, nd.y, nd.z, __uint_as_float(tag));
 }
 
-// Appends a vertex's shadow record and next ray (all lanes of the warp call this).
+// Appends a vertex's shadow record and next ray with its state (all lanes of the warp call this).
 template <bool GRAD>
 PG3_DI void emitRecords(const Queues &Q, int nextQueue, const ShadeOut &o)
 {
@@ -364,12 +375,16 @@ PG3_DI void emitRecords(const Queues &Q, int nextQueue, const ShadeOut &o)
             d[4] = o.s4;
         }
     }
-    float4 *nq = Q.ray[nextQueue];
+    float4 *nq = rayQ(Q, nextQueue);
     const uint32_t rp = warpAppend(&Q.cnt->ray[nextQueue], o.next);
     if (o.next && rp >= Q.cap) atomicOr(Q.err, kErrQueueOverflow);
     else if (o.next) {
-        nq[2 * rp] = o.r0;
-        nq[2 * rp + 1] = o.r1;
+        nq[2 * (size_t)rp] = o.r0;
+        nq[2 * (size_t)rp + 1] = o.r1;
+        float4 *ns = stQ(Q, nextQueue) + 3 * (size_t)rp;
+        ns[0] = o.t0;
+        ns[1] = o.t1;
+        ns[2] = o.t2;
     }
 }
 
@@ -395,11 +410,13 @@ PG3_DI void cameraRay(const SceneView &S, uint32_t pixel, uint32_t sample, float
     dir = normalize(S.camFwd + S.camRight * (nx * S.tanX) - S.camUp * (ny * S.tanY));
 }
 
-PG3_DI void initPathState(const Queues &Q, uint32_t slot)
+// State of a camera ray at position pos of ray queue q.
+PG3_DI void initPathState(const Queues &Q, int q, uint32_t pos)
 {
-    Q.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
-    Q.ew[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-    Q.pn[slot] = make_float4(0.f, 0.f, 1.f, __uint_as_float(1u | kFlagFinite | kFlagRefl));
+    float4 *st = stQ(Q, q) + 3 * (size_t)pos;
+    st[0] = make_float4(1.f, 1.f, 1.f, 0.f);
+    st[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    st[2] = make_float4(0.f, 0.f, 1.f, __uint_as_float(1u | kFlagFinite | kFlagRefl));
 }
 
 // Closest hit of one ray and its material bucket (-1 none).
@@ -426,7 +443,7 @@ PG3_DI void bucketAppend(const Queues &Q, int bucket, uint32_t i)
     base = __shfl_sync(0xffffffffu, base, leader);
     if (bucket >= 0) {
         const uint32_t pos = base + __popc(peers & ((1u << lane) - 1u));
-        if (pos < Q.cap) Q.bucket[bucket][pos] = i;
+        if (pos < Q.cap) bucketQ(Q, bucket)[pos] = i;
         else atomicOr(Q.err, kErrQueueOverflow);
     }
 }

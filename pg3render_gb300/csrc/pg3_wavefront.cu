@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kWaveBlock) raygenKernel(const __grid_constant
         cameraRay(S, pixel, sample, dir);
         Q.ray[0][2 * i] = make_float4(S.camPos.x, S.camPos.y, S.camPos.z, 0.f);
         Q.ray[0][2 * i + 1] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(i));
-        initPathState(Q, i);
+        initPathState(Q, 0, i);
         if (GRAD) Q.pend[i] = make_float2(__int_as_float(-1), 0.f);
         outR[i] = 0.f;
         outG[i] = 0.f;
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) extendKernel
                                                            DevStats *stats)
 {
     const uint32_t n = Q.cnt->ray[cur];
-    const float4 *rq = Q.ray[cur];
+    const float4 *rq = rayQ(Q, cur);
     uint32_t rays = 0;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
     sample0 = sampleBase<GRAD>(sample0, G);
     constexpr int kBucket = bucketOfShade(K);
     const uint32_t n = Q.cnt->bucket[kBucket];
-    const float4 *rq = Q.ray[cur];
+    const float4 *rq = rayQ(Q, cur);
     const uint32_t stride = gridDim.x * blockDim.x;
     PathCounters pc;
     // the bucket entry of the next iteration is loaded one iteration ahead
@@ -148,6 +148,7 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
                 nextIdx = Q.bucket[kBucket][j + stride];
                 nx.ray = rq + 2 * (size_t)nextIdx;
                 nx.hit = Q.hit + nextIdx;
+                nx.st = stQ(Q, cur) + 3 * (size_t)nextIdx;
             }
             const float4 r0 = rq[2 * idx], r1 = rq[2 * idx + 1];
             const uint32_t slot = __float_as_uint(r1.w) & kSlotMask;
@@ -156,7 +157,8 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
             float3 acc = f3(0.f);
             if (GRAD && G.adjoint) acc = make_float3(outR[slot], outG[slot], outB[slot]);
             float3 L;
-            shadeVertex<K, EMK, GRAD>(S, Q, idx, r0, r1, slot, slot, pixel, sample, pc, o, L, G, sGrad, acc, nx);
+            shadeVertex<K, EMK, GRAD>(S, Q, idx, r0, r1, stQ(Q, cur) + 3 * (size_t)idx, slot, slot, pixel, sample, pc, o,
+                                      L, G, sGrad, acc, nx);
             if (!isZero(L)) {
                 outR[slot] += L.x;
                 outG[slot] += L.y;
@@ -229,9 +231,9 @@ Queues carve(void *scratch, uint64_t cap, bool grad)
     q.ray[1] = (float4 *)take(32 * cap);
     q.hit = (float2 *)take(8 * cap);
     for (int b = 0; b < kNumBuckets; ++b) q.bucket[b] = (uint32_t *)take(4 * cap);
-    q.beta = (float4 *)take(16 * cap);
-    q.ew = (float4 *)take(16 * cap);
-    q.pn = (float4 *)take(16 * cap);
+    q.bucketStride = align256(4 * cap) / 4;
+    q.st[0] = (float4 *)take(48 * cap);
+    q.st[1] = (float4 *)take(48 * cap);
     q.shadow = (float4 *)take((grad ? 80 : 48) * cap);
     q.pend = grad ? (float2 *)take(8 * cap) : nullptr;
     q.cap = (uint32_t)cap;
@@ -331,7 +333,7 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
 size_t wavefrontBytes(uint64_t cap, bool grad)
 {
     return align256(sizeof(Counters)) + 2 * align256(32 * cap) + align256(8 * cap) + kNumBuckets * align256(4 * cap) +
-           3 * align256(16 * cap) + align256((grad ? 80 : 48) * cap) + (grad ? align256(8 * cap) : 0);
+           2 * align256(48 * cap) + align256((grad ? 80 : 48) * cap) + (grad ? align256(8 * cap) : 0);
 }
 
 cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix,
