@@ -242,6 +242,22 @@ int pg3gpu_clear_framebuffer(pg3gpu_ctx *ctx);
 int pg3gpu_write_image(const double *mean_rgb, uint32_t width, uint32_t height, const char *path, float gamma);
 int pg3gpu_save_image(pg3gpu_ctx *ctx, const char *path, float gamma);
 
+/* Steerable-sampler data files in the reference's ".emssd" format 2.1
+ * (EnvironmentMapSteerableSampler::SaveToDisk / LoadFromDisk, src/em_steerable_sampler.hxx:1648-2058),
+ * for a context created with em_sampler PG3GPU_EM_STEERABLE.
+ * pg3gpu_save_steerable writes the context's triangulation (its uniform subdivision level as
+ * both the minimum and the maximum level, the reference's default debugging parameters, 6
+ * children per tree node), its vertex weights and its 6-ary tree; max_approx_error is the value
+ * written into the parameter block (the reference's default is 5.0; it checks the parameters of
+ * a file against its own before loading it). pg3gpu_load_steerable reads a file of that format
+ * whose leaf triangles are exactly those of the context's level (any vertex numbering, tree order
+ * or duplicated vertices), replaces the context's vertex weights with the file's and rebuilds the
+ * tree weights on the device; a file of an adaptive triangulation (leaves at several levels)
+ * returns PG3GPU_ERR_UNSUPPORTED, a malformed one PG3GPU_ERR_INVALID_ARGUMENT. A later map change
+ * through pg3gpu_set_params recomputes the weights from the map. */
+int pg3gpu_save_steerable(pg3gpu_ctx *ctx, const char *path, float max_approx_error);
+int pg3gpu_load_steerable(pg3gpu_ctx *ctx, const char *path);
+
 /* Number of samples per pixel accumulated so far (WasUsed() == (n > 0)). */
 uint64_t pg3gpu_iterations(const pg3gpu_ctx *ctx);
 

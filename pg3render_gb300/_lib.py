@@ -108,6 +108,8 @@ SIGNATURES = {
     "pg3gpu_write_image": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_char_p,
                                           ctypes.c_float]),
     "pg3gpu_save_image": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_float]),
+    "pg3gpu_save_steerable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_float]),
+    "pg3gpu_load_steerable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "pg3gpu_iterations": (ctypes.c_uint64, [ctypes.c_void_p]),
     "pg3gpu_render_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
                                              ctypes.c_void_p]),

@@ -16,7 +16,7 @@ LIB = os.path.join(BUILD, "libpg3gpu.so")
 ROOT = os.path.dirname(HERE)
 
 SOURCES = ["pg3_api.cu", "pg3_host.cpp", "pg3_steerable.cpp", "pg3_megakernel.cu", "pg3_wavefront.cu", "pg3_lbvh.cu", "pg3_probe.cu",
-           "pg3_batch.cu", "pg3_diff.cu", "pg3_steer_build.cu", "pg3_image.cpp"]
+           "pg3_batch.cu", "pg3_diff.cu", "pg3_steer_build.cu", "pg3_image.cpp", "pg3_emssd.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--extended-lambda", "-Xcompiler", "-fPIC",
               "-I", CSRC, "-I", os.path.join(ROOT, "include")]

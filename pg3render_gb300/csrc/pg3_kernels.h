@@ -58,6 +58,8 @@ struct SteerWeightArgs {
     float *vw, *leafW, *nodeW, *rootW;           // outputs (12 / 9 / 72 floats per item, 9)
 };
 cudaError_t launchSteerWeights(const SteerWeightArgs &args, cudaStream_t stream);
+// The leaf, node and whole-sphere weights from the vertex weights already in args.vw.
+cudaError_t launchSteerTreeWeights(const SteerWeightArgs &args, cudaStream_t stream);
 
 // pg3_probe.cu (sampler probes for tests)
 cudaError_t launchProbeBsdf(const SceneView &S, int mat, uint32_t n, const float *wol, uint32_t seed, float *wil,

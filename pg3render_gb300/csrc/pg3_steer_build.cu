@@ -126,10 +126,16 @@ __global__ void rootWeightsKernel(const float *lw, uint32_t nLeaf, float *rootW)
 
 cudaError_t launchSteerWeights(const SteerWeightArgs &a, cudaStream_t st)
 {
-    if (!a.em || !a.vdir || !a.leafTri || !a.leafArea || !a.nodeChild || !a.vw || !a.leafW || !a.nodeW ||
-        !a.rootW || a.numLayers == 0 || a.numLayers > kSteerMaxLayers)
-        return cudaErrorInvalidValue;
+    if (!a.em || !a.vdir || !a.vw) return cudaErrorInvalidValue;
     vertexWeightsKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.em, a.emW, a.emH, a.vdir, a.numVertices, a.vw);
+    return launchSteerTreeWeights(a, st);
+}
+
+cudaError_t launchSteerTreeWeights(const SteerWeightArgs &a, cudaStream_t st)
+{
+    if (!a.leafTri || !a.leafArea || !a.nodeChild || !a.vw || !a.leafW || !a.nodeW || !a.rootW || a.numLayers == 0 ||
+        a.numLayers > kSteerMaxLayers)
+        return cudaErrorInvalidValue;
     leafWeightsKernel<<<(a.numLeaves + 127) / 128, 128, 0, st>>>(a.leafTri, a.leafArea, a.numLeaves, a.vw, a.leafW);
     for (uint32_t l = 0; l < a.numLayers; ++l) {
         const uint32_t n0 = a.layerStart[l], n1 = a.layerStart[l + 1];

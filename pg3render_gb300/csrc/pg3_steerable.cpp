@@ -53,14 +53,16 @@ bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
     out = SteerGeom();
     out.level = level;
 
-    // icosahedron: the 12 cyclic permutations of (0, +-1, +-t), normalised
+    // icosahedron: the 12 cyclic permutations of (+-t, +-1, 0), normalised -- the reference's
+    // vertex set (Geom::UnitIcosahedron, src/geom.hxx:290-312), so both triangulate the sphere
+    // with the same triangles at every level
     const double t = (1.0 + std::sqrt(5.0)) / 2.0;
     std::vector<D3> v;
     for (int s1 = -1; s1 <= 1; s1 += 2)
         for (int s2 = -1; s2 <= 1; s2 += 2) {
-            v.push_back(nrm({0.0, (double)s1, s2 * t}));
-            v.push_back(nrm({(double)s1, s2 * t, 0.0}));
-            v.push_back(nrm({s2 * t, 0.0, (double)s1}));
+            v.push_back(nrm({s2 * t, (double)s1, 0.0}));
+            v.push_back(nrm({(double)s1, 0.0, s2 * t}));
+            v.push_back(nrm({0.0, s2 * t, (double)s1}));
         }
     double emin = 1e9;
     for (size_t i = 0; i < v.size(); ++i)

@@ -19,6 +19,15 @@ from ._lib import (ALG_PATH_TRACING, ALG_PATH_TRACING_NAIVE, EM_CDF, EM_COSINE, 
                    PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT, TRAVERSAL_AUTO, TRAVERSAL_BVH,
                    TRAVERSAL_LIST, Pg3Error)
 
+def steerable_file_name(em_path, level, max_approx_error=5.0, bilinear=True):
+    """The path under which the reference caches the steerable sampler of the map at em_path
+    (EnvironmentMapSteerableSampler::GenerateSaveFilePath, src/em_steerable_sampler.hxx:1596-1646)
+    for a uniform triangulation: minimum = maximum subdivision level, its default debugging
+    parameters (50 samples per dimension, span 1.1, oversampling 0.7) and 6 children per node."""
+    return "%s.%s_e%.2f_sll%d_slu%d_tms%d_ts%.2f_os%.2f_mc%d.v2.1.emssd" % (
+        em_path, "bi" if bilinear else "nn", max_approx_error, level, level, 50, 1.1, 0.7, 6)
+
+
 def write_image(mean_rgb, path, gamma=2.2):
     """Writes an (H, W, 3) mean image as ``.hdr`` or a gamma-encoded 24-bit BMP (no GPU needed)."""
     a = np.ascontiguousarray(mean_rgb, np.float64)
@@ -134,6 +143,16 @@ class GpuPathTracer:
         """The mean image as ``.hdr`` (Radiance RGBE) or, for any other extension, a 24-bit BMP
         with 1/gamma applied (the reference's main program writes gamma 2.2)."""
         _lib.check(self._L.pg3gpu_save_image(self._ctx, os.fsencode(path), gamma), self._ctx)
+
+    def save_steerable(self, path, max_approx_error=5.0):
+        """Writes the steerable sampler's triangulation, vertex weights and tree as a ``.emssd``
+        file of format 2.1, the reference's sampler cache (see :func:`steerable_file_name`)."""
+        _lib.check(self._L.pg3gpu_save_steerable(self._ctx, os.fsencode(path), max_approx_error), self._ctx)
+
+    def load_steerable(self, path):
+        """Replaces the steerable sampler's vertex weights with those of a ``.emssd`` file of the
+        context's uniform subdivision level (written by the reference or by save_steerable)."""
+        _lib.check(self._L.pg3gpu_load_steerable(self._ctx, os.fsencode(path)), self._ctx)
 
     def render_samples(self, algorithm, iteration, spp):
         out = np.zeros((spp, self.height, self.width, 3), np.float32)

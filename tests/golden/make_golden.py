@@ -149,12 +149,37 @@ def make_image_writer():
     print("image_writer done")
 
 
+def make_emssd():
+    """emssd_ref.npz: steerable-sampler data files the reference itself wrote
+    (EnvironmentMapSteerableSampler::SaveToDisk, run by its Init on a map without a cached file)
+    for the 64x32 sky of the environment-map box: a uniform triangulation (minimum = maximum
+    subdivision level 2) and an adaptive one (levels 1-3, approximation error 0.05), with the
+    file names the reference chose and the map they were built from."""
+    scene = S.cornell_env(16, 16, 64, 32)
+    out = {"env_map": scene.env_map.astype(np.float32)}
+    for key, params in (("uniform", ("5", "2", "2")), ("adaptive", ("0.05", "1", "3"))):
+        with tempfile.TemporaryDirectory() as td:
+            em_path = os.path.join(td, "em.bin")
+            scene.write_env_map(em_path)
+            text = scene.to_text(em_path=em_path, algorithm="pt", max_path_length=4)
+            O.reference_render(text, renderers=1, iters=1, seed=1, em_sampler="steerable",
+                               extra=("--em-params",) + params)
+            files = [f for f in os.listdir(td) if f.endswith(".emssd")]
+            assert len(files) == 1, files
+            with open(os.path.join(td, files[0]), "rb") as f:
+                out[key] = np.frombuffer(f.read(), np.uint8).copy()
+            out[key + "_name"] = np.array(files[0])
+    np.savez_compressed(os.path.join(HERE, "emssd_ref.npz"), **out)
+    print("emssd_ref done", {k: v.shape for k, v in out.items()})
+
+
 if __name__ == "__main__":
-    if "image_writer" in sys.argv[1:]:
-        make_image_writer()
-        sys.argv.remove("image_writer")
-        if len(sys.argv) == 1:
-            sys.exit(0)
+    for extra, fn in (("image_writer", make_image_writer), ("emssd", make_emssd)):
+        if extra in sys.argv[1:]:
+            fn()
+            sys.argv.remove(extra)
+            if len(sys.argv) == 1:
+                sys.exit(0)
     names = sys.argv[1:] or (list(CASES) + list(PRESET_CASES))
     for n in [x for x in names if x in PRESET_CASES]:
         make_preset(n)
