@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--sampler", default="auto", choices=["auto", "steerable", "cdf", "cosine"])
     ap.add_argument("--pipeline", default="auto", choices=["auto", "megakernel", "wavefront"])
+    ap.add_argument("--steer-weights", default="projected", choices=["point", "projected"],
+                    help="vertex luminance of the steerable sampler: the map's value at the vertex (the "
+                         "reference's build) or its projection onto the vertex's hat function")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
     # smaller cases of the same workload (profiling captures); the headline uses the defaults
@@ -190,6 +193,68 @@ def cpu_baseline(scene, sampler, threads=None, iters=1):
                 "sample": "%d spp of the %dx%d scene" % (spp, WIDTH, HEIGHT)}
 
 
+def matched_quality(gpu_value, cpu_value, steer_weights, side=128, spps=(16, 256), renders=(4, 2),
+                    conv_spp=16384):
+    """Per-sample quality of the two renderers on the headline scene at side x side: the
+    relative MSE, mean over pixel channels of (x - c)^2 / (c^2 + 0.01), of images of spp samples
+    against a converged image c (this library, CDF sampler, conv_spp samples per pixel), averaged
+    over independent images, for the GPU path (roulette from length 4; steerable sampler with
+    both vertex weightings, and the CDF sampler) and for the reference's own CPU renderer (max
+    length 12 without roulette; its steerable sampler at 1280 triangles and its CDF sampler).
+    The reference's steerable sampler evaluates its pdf from the map instead of the density it
+    samples, so its images converge to a darker limit (bias). At the benchmark's 256 samples per
+    pixel, the ratio of the relative MSEs turns the Msamples/s ratio into an equal-quality speedup:
+    the GPU renders the samples that reach the reference's error in that many times less time."""
+    import numpy as np
+    import pg3render_gb300 as P
+    from pg3render_gb300 import scene as S
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    R = P.renderer
+    sc = S.cornell_env(side, side, EM_W, EM_H, em_seed=7)
+    gpu_cfgs = {"steerable_point": (R.EM_STEERABLE, R.STEER_WEIGHTS_POINT),
+                "steerable_projected": (R.EM_STEERABLE, R.STEER_WEIGHTS_PROJECTED), "cdf": (R.EM_CDF, 0)}
+
+    def gpu_image(key, seed, n):
+        em, w = gpu_cfgs[key]
+        cfg = P.Config(scene=sc, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM, em_sampler=em,
+                       steer_weights=w)
+        with P.GpuPathTracer(cfg, seed=seed) as r:
+            r.RunIteration(R.kPathTracing, 0, n)
+            return r.framebuffer()[0]
+
+    conv = gpu_image("cdf", 99991, conv_spp)
+
+    def rel_mse(img):
+        return float(np.mean((img - conv) ** 2 / (conv ** 2 + 0.01)))
+
+    out = {"side": side, "converged": "this library, CDF sampler, %d spp" % conv_spp}
+    with tempfile.TemporaryDirectory() as td:
+        em_path = os.path.join(td, "em.bin")
+        sc.write_env_map(em_path)
+        text = sc.to_text(em_path=em_path, max_path_length=MAX_PATH)
+        for spp, reps in zip(spps, renders):
+            row = {"renders": reps}
+            for key in gpu_cfgs:
+                row["gpu_" + key] = round(statistics.mean(rel_mse(gpu_image(key, 1000 + k, spp))
+                                                          for k in range(reps)), 6)
+            for name in ("steerable", "cdf"):
+                if O.reference_binary(name):
+                    extra = ["--em-params", "5", "3", "3"] if name == "steerable" else []
+                    row["cpu_reference_" + name] = round(statistics.mean(
+                        rel_mse(O.reference_render(text, renderers=spp, iters=1, seed=2000 + k, em_sampler=name,
+                                                   extra=extra)["mean"]) for k in range(reps)), 6)
+            out["rel_mse_at_%dspp" % spp] = row
+    last = out["rel_mse_at_%dspp" % spps[-1]]
+    mine = last["gpu_steerable_" + steer_weights]
+    if "cpu_reference_steerable" in last and cpu_value and mine > 0:
+        ratio = last["cpu_reference_steerable"] / mine
+        out["headline_sampler"] = "steerable_" + steer_weights
+        out["rel_mse_ratio_cpu_over_gpu_at_%dspp" % spps[-1]] = round(ratio, 4)
+        out["equal_quality_speedup"] = round(gpu_value / cpu_value * ratio, 2)
+    return out
+
+
 # ----------------------------------------------------------------------------- ranks
 SAMPLES_PER_RANK = 1 << 24   # sample-index stride between ranks: disjoint random streams
 
@@ -228,9 +293,10 @@ def run_gpu(args, rank, world, local_rank):
     em_sampler = {"steerable": R.EM_STEERABLE, "cdf": R.EM_CDF, "cosine": R.EM_COSINE}[sampler]
     pipeline = {"auto": R.PIPELINE_AUTO, "megakernel": R.PIPELINE_MEGAKERNEL,
                 "wavefront": R.PIPELINE_WAVEFRONT}[args.pipeline]
+    steer_weights = {"point": R.STEER_WEIGHTS_POINT, "projected": R.STEER_WEIGHTS_PROJECTED}[args.steer_weights]
     cfg = P.Config(scene=scene, algorithm=R.kPathTracing, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM,
                    em_sampler=em_sampler, pipeline=pipeline, base_seed=1234,
-                   max_paths_in_flight=args.paths_in_flight)
+                   max_paths_in_flight=args.paths_in_flight, steer_weights=steer_weights)
     npix = WIDTH * HEIGHT
     paths_per_step = npix * SPP
     sample_base = rank_sample_base(rank)
@@ -311,6 +377,7 @@ def run_gpu(args, rank, world, local_rank):
         "config": {"workload": "cornell_env_%dx%d_%dspp_maxpl12_rr3_em1024x512_%s" % (WIDTH, HEIGHT, SPP, sampler),
                    "width": WIDTH, "height": HEIGHT, "spp": SPP, "max_path_length": MAX_PATH,
                    "rr_min_path_length": RR_FROM, "env_map": [EM_W, EM_H], "em_sampler": sampler,
+                   "steer_weights": args.steer_weights if sampler == "steerable" else None,
                    "pipeline": args.pipeline, "paths_per_step": paths_per_step,
                    "l2": "flushed between steps (256 MiB memset outside the timed events)",
                    "parallelism": "replicas over sample ranges" if world > 1 else "single GPU"},
@@ -320,6 +387,12 @@ def run_gpu(args, rank, world, local_rank):
     line["clocks"] = clk.summary()
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(scene, sampler, iters=args.cpu_iters)
+        if sampler == "steerable":
+            try:
+                line["cpu_baseline"]["matched_quality"] = matched_quality(value, line["cpu_baseline"]["value"],
+                                                                          args.steer_weights)
+            except Exception as e:   # reported, never hidden
+                line["cpu_baseline"]["matched_quality"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if world == 1 and not args.no_secondary:
         line["secondary"] = secondary_metrics()
     return line

@@ -20,6 +20,7 @@ EM_CDF, EM_COSINE, EM_STEERABLE = 0, 1, 2
 TRAVERSAL_AUTO, TRAVERSAL_LIST, TRAVERSAL_BVH = 0, 1, 2
 PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT = 0, 1, 2
 GGX_VNDF_EXACT, GGX_VNDF_REFERENCE_FIT = 0, 1
+STEER_WEIGHTS_POINT, STEER_WEIGHTS_PROJECTED = 0, 1
 
 c_float3 = ctypes.c_float * 3
 
@@ -74,7 +75,7 @@ class Options(ctypes.Structure):
                 ("steer_subdiv_level", ctypes.c_uint32), ("seed", ctypes.c_uint64),
                 ("max_paths_in_flight", ctypes.c_uint32), ("ggx_sampler", ctypes.c_int32),
                 ("splitting_level", ctypes.c_float), ("light_to_bsdf_ratio", ctypes.c_float),
-                ("reserved", ctypes.c_uint32 * 2)]
+                ("steer_weights", ctypes.c_int32), ("reserved", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):

@@ -201,6 +201,7 @@ void pg3gpu_default_options(pg3gpu_options *o)
     o->traversal = PG3GPU_TRAVERSAL_AUTO;
     o->pipeline = PG3GPU_PIPELINE_AUTO;
     o->steer_subdiv_level = 3;
+    o->steer_weights = PG3GPU_STEER_WEIGHTS_PROJECTED;
     o->seed = 1234;
 }
 
@@ -324,12 +325,17 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
         a.numLayers = (uint32_t)g.layerStart.size() - 1;
         for (uint32_t l = 0; l <= a.numLayers; ++l) a.layerStart[l] = g.layerStart[l];
         if ((st = devAlloc(ctx, &a.vw, 12 * (size_t)a.numVertices))) return bail(st);
+        a.projected = (ctx->opts.steer_weights == PG3GPU_STEER_WEIGHTS_PROJECTED) ? 1 : 0;
+        unsigned char *proj = nullptr;
+        if (a.projected && (st = devAlloc(ctx, &proj, projScratchBytes(a.numVertices)))) return bail(st);
+        a.projScratch = proj;
         if ((st = devAlloc(ctx, &a.leafW, 9 * (size_t)a.numLeaves))) return bail(st);
         if ((st = devAlloc(ctx, &a.nodeW, 72 * (size_t)g.numNodes()))) return bail(st);
         a.rootW = reinterpret_cast<float *>(const_cast<float4 *>(sv.leafPlane) + rootAt);
         sv.vw = a.vw;
         sv.nodeW = a.nodeW;
         v.bgShL = a.rootW;   // the background's picking estimate: the sampler's whole integral
+        a.locator = sv;      // geometry and locator tables (vw / nodeW are outputs of this build)
         const cudaError_t e = launchSteerWeights(a, nullptr);
         if (e != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "steerable build: %s", cudaGetErrorString(e)));
         ctx->hasSteer = true;

@@ -137,6 +137,8 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "light-to-BSDF sample ratio must be in (0, 16]");
     if (o.em_sampler != PG3GPU_EM_CDF && o.em_sampler != PG3GPU_EM_COSINE && o.em_sampler != PG3GPU_EM_STEERABLE)
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown environment-map sampler");
+    if (o.steer_weights != PG3GPU_STEER_WEIGHTS_POINT && o.steer_weights != PG3GPU_STEER_WEIGHTS_PROJECTED)
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown steerable vertex weights");
     if (sc.num_materials == 0 || !sc.materials) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "scene has no materials");
     if ((sc.num_triangles && !sc.triangles) || (sc.num_spheres && !sc.spheres) ||
         (sc.num_area_lights && !sc.area_lights) || (sc.num_point_lights && !sc.point_lights))

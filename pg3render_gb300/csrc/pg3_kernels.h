@@ -56,7 +56,14 @@ struct SteerWeightArgs {
     uint32_t layerStart[kSteerMaxLayers + 1];    // tree layers bottom-up, node ranges
     uint32_t numLayers;
     float *vw, *leafW, *nodeW, *rootW;           // outputs (12 / 9 / 72 floats per item, 9)
+    // projected vertex luminance (PG3GPU_STEER_WEIGHTS_PROJECTED): the map projected onto the
+    // triangulation's piecewise-linear hat functions; scratch of projScratchBytes(numVertices)
+    // bytes and the leaf locator (the geometry part of the scene's SteerView)
+    int projected;
+    void *projScratch;
+    SteerView locator;
 };
+size_t projScratchBytes(uint32_t numVertices);
 cudaError_t launchSteerWeights(const SteerWeightArgs &args, cudaStream_t stream);
 // The leaf, node and whole-sphere weights from the vertex weights already in args.vw.
 cudaError_t launchSteerTreeWeights(const SteerWeightArgs &args, cudaStream_t stream);

@@ -8,12 +8,22 @@
 // node weight     nodeW[n][k][c] = the summed weight of child c                    (:3755-3793)
 // whole sphere    rootW[k]  = sum over all leaves of lw[t][k]
 // with Y the 9 real SH basis functions (Ramamoorthi & Hanrahan 2001) and L the luminance of
-// the map's bilinear (tent) lookup in the vertex direction (src/em_image.hxx:95-143).
+// the map's bilinear (tent) lookup in the vertex direction (src/em_image.hxx:95-143): the
+// reference's point sample (PG3GPU_STEER_WEIGHTS_POINT). With PG3GPU_STEER_WEIGHTS_PROJECTED,
+// L is instead the projection of the map's luminance onto the vertex's hat function phi_v (1 at
+// the vertex, 0 at the other vertices, linear over each leaf's plane):
+//   L_v = sum over texels t of lum_t dOmega_t phi_v(d_t) / sum over texels of dOmega_t phi_v(d_t)
+// so that the piecewise-linear approximation keeps the energy of features smaller than a
+// triangle (a sun between vertices), which point samples miss; the sampler's density and pdf
+// stay exactly the ones of pg3_steer.cuh, only the vertex values change. A vertex whose hat
+// function covers no texel centre keeps its point sample.
 // Layouts for vector loads: a vertex's 9 weights padded to 12 floats (three float4), a node's
 // weights coefficient-major over 8 child slots (9 x 8 floats, two float4 per coefficient).
+#include <algorithm>
 #include <climits>
 
 #include "pg3_kernels.h"
+#include "pg3_steer.cuh"
 
 namespace pg3 {
 
@@ -31,8 +41,79 @@ __device__ float texelLum(const float4 *em, uint32_t W, uint32_t H, int x, int y
     return 0.212671f * p.x + 0.715160f * p.y + 0.072169f * p.z;
 }
 
+// Projection of the texels' luminance onto the hat functions of the leaf that contains each
+// texel centre: acc[v] += lum dOmega phi_v, mass[v] += dOmega phi_v, summed in 64-bit fixed point
+// so that the sums, and every render after them, do not depend on the order of the atomics.
+// Scales: a term is at most maxLum * maxOmega (lum) or maxOmega (mass), a vertex sums at most
+// W * H terms, so scale = 1e18 / (W * H * bound) keeps each sum below 2^63 with a resolution of
+// 1e-12 of the largest term.
+struct ProjScratch {
+    unsigned long long *acc, *mass;   // nv each
+    unsigned int *maxLumBits;         // max texel luminance (non-negative float bits)
+};
+
+__device__ float texelLumAt(const float4 *em, uint32_t i)
+{
+    const float4 p = em[i];
+    return fmaxf(0.212671f * p.x + 0.715160f * p.y + 0.072169f * p.z, 0.f);
+}
+
+__global__ void maxLumKernel(const float4 *em, uint32_t n, unsigned int *maxLumBits)
+{
+    float m = 0.f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        m = fmaxf(m, texelLumAt(em, i));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxLumBits, __float_as_uint(m));   // non-negative: bits order as values
+}
+
+__device__ double projScale(uint32_t W, uint32_t H, double bound)
+{
+    return 1e18 / ((double)W * (double)H * fmax(bound, 1e-30));
+}
+
+__global__ void projectLumKernel(const float4 *em, uint32_t W, uint32_t H, SteerView T, ProjScratch P)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * H) return;
+    const uint32_t x = i % W, y = i / W;
+    const float kPi = 3.14159265358979f;
+    // inverse of the lat-long mapping of vertexWeightsKernel (u = 0.5 - atan2(y, x) / 2pi, v = theta / pi)
+    const float theta = ((float)y + 0.5f) * (kPi / (float)H);
+    const float phi = (((float)x + 0.5f) / (float)W - 0.5f) * (2.f * kPi);
+    const float st = sinf(theta);
+    const float3 d = make_float3(st * cosf(phi), -st * sinf(phi), cosf(theta));
+    const double maxOmega = (2.0 * 3.14159265358979 / W) * (3.14159265358979 / H);
+    const float dOmega = (2.f * kPi / (float)W) * (kPi / (float)H) * st;
+    const float lum = texelLumAt(em, i);
+    const int leaf = steerLocate(T, d);
+    if (leaf < 0 || (uint32_t)leaf >= (20u << (2 * T.level))) return;
+    const int4 tri = T.tri[T.levelOff[T.level] + leaf];
+    const float3 A = xyz(T.vdir[tri.x]), B = xyz(T.vdir[tri.y]), C = xyz(T.vdir[tri.z]);
+    const float3 n = cross(B - A, C - A);
+    const float nn = dot(n, n);
+    const float dn = dot(n, d);
+    if (!(nn > 0.f) || !(dn > 0.f)) return;
+    const float3 q = d * (dot(n, A) / dn);          // d meets the leaf's plane
+    float b[3];
+    b[0] = fmaxf(dot(cross(B - q, C - q), n) / nn, 0.f);
+    b[1] = fmaxf(dot(cross(C - q, A - q), n) / nn, 0.f);
+    b[2] = fmaxf(1.f - b[0] - b[1], 0.f);
+    const float bs = b[0] + b[1] + b[2];
+    if (!(bs > 0.f)) return;
+    const double maxLum = (double)__uint_as_float(*P.maxLumBits);
+    const double sA = projScale(W, H, maxLum * maxOmega), sM = projScale(W, H, maxOmega);
+    const int v[3] = {tri.x, tri.y, tri.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double w = (double)dOmega * (double)(b[k] / bs);
+        atomicAdd(&P.acc[v[k]], (unsigned long long)(w * (double)lum * sA + 0.5));
+        atomicAdd(&P.mass[v[k]], (unsigned long long)(w * sM + 0.5));
+    }
+}
+
 __global__ void vertexWeightsKernel(const float4 *em, uint32_t W, uint32_t H, const float4 *vdir, uint32_t nv,
-                                    float *vw)
+                                    ProjScratch proj, int useProj, float *vw)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
@@ -48,7 +129,14 @@ __global__ void vertexWeightsKernel(const float4 *em, uint32_t W, uint32_t H, co
     const float xl = xf - ((float)x0 + 0.5f), yl = yf - ((float)y0 + 0.5f);
     const float top = (1.f - xl) * texelLum(em, W, H, x0, y0) + xl * texelLum(em, W, H, cx, y0);
     const float bot = (1.f - xl) * texelLum(em, W, H, x0, cy) + xl * texelLum(em, W, H, cx, cy);
-    const float L = (1.f - yl) * top + yl * bot;
+    float L = (1.f - yl) * top + yl * bot;
+    if (useProj && proj.mass[i] > 0ull) {
+        const double maxOmega = (2.0 * 3.14159265358979 / W) * (3.14159265358979 / H);
+        const double maxLum = (double)__uint_as_float(*proj.maxLumBits);
+        const double a = (double)proj.acc[i] / projScale(W, H, maxLum * maxOmega);
+        const double m = (double)proj.mass[i] / projScale(W, H, maxOmega);
+        L = (float)(a / m);
+    }
     const float x = d.x, y = d.y, z = d.z;
     float *o = vw + 12 * (size_t)i;
     o[0] = L * 0.282095f;
@@ -124,10 +212,26 @@ __global__ void rootWeightsKernel(const float *lw, uint32_t nLeaf, float *rootW)
 
 }  // namespace
 
+size_t projScratchBytes(uint32_t numVertices) { return 16 * (size_t)numVertices + 16; }
+
 cudaError_t launchSteerWeights(const SteerWeightArgs &a, cudaStream_t st)
 {
-    if (!a.em || !a.vdir || !a.vw) return cudaErrorInvalidValue;
-    vertexWeightsKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.em, a.emW, a.emH, a.vdir, a.numVertices, a.vw);
+    if (!a.em || !a.vdir || !a.vw || (a.projected && !a.projScratch)) return cudaErrorInvalidValue;
+    // projScratch: acc[nv], mass[nv] (64-bit), the max-luminance word; passed to the kernels by
+    // value (no host-side record, so the build can be captured into a CUDA graph)
+    ProjScratch P{};
+    if (a.projected) {
+        P.acc = reinterpret_cast<unsigned long long *>(a.projScratch);
+        P.mass = P.acc + a.numVertices;
+        P.maxLumBits = reinterpret_cast<unsigned int *>(P.mass + a.numVertices);
+        const cudaError_t e = cudaMemsetAsync(a.projScratch, 0, projScratchBytes(a.numVertices), st);
+        if (e != cudaSuccess) return e;
+        const uint32_t texels = a.emW * a.emH;
+        maxLumKernel<<<std::min<uint32_t>((texels + 255) / 256, 1024), 256, 0, st>>>(a.em, texels, P.maxLumBits);
+        projectLumKernel<<<(texels + 255) / 256, 256, 0, st>>>(a.em, a.emW, a.emH, a.locator, P);
+    }
+    vertexWeightsKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.em, a.emW, a.emH, a.vdir, a.numVertices,
+                                                                     P, a.projected, a.vw);
     return launchSteerTreeWeights(a, st);
 }
 

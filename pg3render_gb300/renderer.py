@@ -16,8 +16,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import (ALG_PATH_TRACING, ALG_PATH_TRACING_NAIVE, EM_CDF, EM_COSINE, EM_STEERABLE,  # noqa: F401
-                   PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT, TRAVERSAL_AUTO, TRAVERSAL_BVH,
-                   TRAVERSAL_LIST, Pg3Error)
+                   PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT, STEER_WEIGHTS_POINT,
+                   STEER_WEIGHTS_PROJECTED, TRAVERSAL_AUTO, TRAVERSAL_BVH, TRAVERSAL_LIST, Pg3Error)
 
 def steerable_file_name(em_path, level, max_approx_error=5.0, bilinear=True):
     """The path under which the reference caches the steerable sampler of the map at em_path
@@ -62,6 +62,7 @@ class Config:
     steer_subdiv_level: int = 3
     max_paths_in_flight: int = 0
     ggx_sampler: int = 0                 # GGX_VNDF_EXACT; GGX_VNDF_REFERENCE_FIT = the reference's routine
+    steer_weights: int = 1               # STEER_WEIGHTS_PROJECTED; STEER_WEIGHTS_POINT = the reference's build
 
     def options(self, seed=None):
         o = _lib.Options()
@@ -81,6 +82,7 @@ class Config:
         o.seed = self.base_seed if seed is None else seed
         o.max_paths_in_flight = self.max_paths_in_flight
         o.ggx_sampler = self.ggx_sampler
+        o.steer_weights = self.steer_weights
         return o
 
 

@@ -143,10 +143,11 @@ def test_reference_vertex_weights_are_map_luminance_times_sh():
 
 
 def _ctx(env, sampler=None, level=2, seed=5):
+    # the reference's vertex weights are point samples of the map: the same build here
     sc = S.cornell_env(16, 16, 64, 32)
     sc.env_map = env
     cfg = P.Config(scene=sc, max_path_length=6, em_sampler=sampler if sampler is not None else _lib.EM_STEERABLE,
-                   steer_subdiv_level=level)
+                   steer_subdiv_level=level, steer_weights=_lib.STEER_WEIGHTS_POINT)
     return P.GpuPathTracer(cfg, seed=seed)
 
 

@@ -40,9 +40,9 @@ def _bsdf_scene():
     return s
 
 
-def _env_scene(sampler):
+def _env_scene(sampler, weights=R.STEER_WEIGHTS_POINT):
     s = S.cornell_env(8, 8, 256, 128, em_seed=11)
-    return P.Config(scene=s, max_path_length=12, em_sampler=sampler)
+    return P.Config(scene=s, max_path_length=12, em_sampler=sampler, steer_weights=weights)
 
 
 def _rel(a, b):
@@ -123,15 +123,17 @@ def test_reference_vndf_fit_is_approximate():
     assert stats[1][1] / stats[1][2] > 1.2, stats[1]
 
 
-ENV_CASES = [(R.EM_COSINE, (0.0, 0.0, 1.0)), (R.EM_CDF, (0.0, 0.0, 1.0)),
-             (R.EM_STEERABLE, (0.0, 0.0, 1.0)), (R.EM_STEERABLE, (0.35, -0.2, 0.915))]
+PT, PJ = R.STEER_WEIGHTS_POINT, R.STEER_WEIGHTS_PROJECTED
+ENV_CASES = [(R.EM_COSINE, (0.0, 0.0, 1.0), PT), (R.EM_CDF, (0.0, 0.0, 1.0), PT),
+             (R.EM_STEERABLE, (0.0, 0.0, 1.0), PT), (R.EM_STEERABLE, (0.35, -0.2, 0.915), PT),
+             (R.EM_STEERABLE, (0.0, 0.0, 1.0), PJ), (R.EM_STEERABLE, (-0.6, 0.3, 0.742), PJ)]
 
 
-@pytest.mark.parametrize("sampler,normal", ENV_CASES)
-def test_env_sampler_pdf_consistency(sampler, normal):
+@pytest.mark.parametrize("sampler,normal,weights", ENV_CASES)
+def test_env_sampler_pdf_consistency(sampler, normal, weights):
     nrm = np.asarray(normal, np.float32)
     nrm /= np.linalg.norm(nrm)
-    with P.GpuPathTracer(_env_scene(sampler)) as r:
+    with P.GpuPathTracer(_env_scene(sampler, weights)) as r:
         n = 1 << 18
         o = r.probe_light(0, np.zeros((n, 3)), np.tile(nrm, (n, 1)), seed=9)
     # CDF samples below the horizon carry zero radiance but a valid pdf; compare where upper
@@ -142,11 +144,11 @@ def test_env_sampler_pdf_consistency(sampler, normal):
     assert np.median(rel) <= 1e-6 and np.quantile(rel, 0.999) <= 1e-5, (np.median(rel), np.quantile(rel, 0.999))
 
 
-@pytest.mark.parametrize("sampler,normal", ENV_CASES)
-def test_env_sampler_chi_square(sampler, normal):
+@pytest.mark.parametrize("sampler,normal,weights", ENV_CASES)
+def test_env_sampler_chi_square(sampler, normal, weights):
     nrm = np.asarray(normal, np.float32)
     nrm /= np.linalg.norm(nrm)
-    with P.GpuPathTracer(_env_scene(sampler)) as r:
+    with P.GpuPathTracer(_env_scene(sampler, weights)) as r:
         o = r.probe_light(0, np.zeros((N_CHI, 3)), np.tile(nrm, (N_CHI, 1)), seed=13)
         if sampler == R.EM_CDF:
             # The CDF sampler's pdf is exact per map pixel only (uniform in (u, v) inside a pixel,
@@ -183,17 +185,41 @@ def test_area_light_pdf_consistency():
             assert np.quantile(rel, 0.999) <= 1e-5, np.quantile(rel, 0.999)
 
 
-@pytest.mark.parametrize("pipeline", [R.PIPELINE_WAVEFRONT, R.PIPELINE_MEGAKERNEL])
-def test_steerable_render_converges_to_reference(pipeline):
+@pytest.mark.parametrize("pipeline,weights", [(R.PIPELINE_WAVEFRONT, PT), (R.PIPELINE_MEGAKERNEL, PT),
+                                              (R.PIPELINE_WAVEFRONT, PJ)])
+def test_steerable_render_converges_to_reference(pipeline, weights):
     # the reference's own steerable sampler is not pdf-consistent; its unbiased CDF-sampler
-    # render of the same scene is the image the corrected steerable sampler must reach
+    # render of the same scene is the image the corrected steerable sampler must reach, with
+    # either vertex weighting
     from _util import load_golden, scene_from_golden, z_ok, zscores
     d, text, td = load_golden("cornell_env_32_cdf")
     scene = scene_from_golden(d)
-    cfg = P.Config(scene=scene, max_path_length=12, em_sampler=R.EM_STEERABLE, pipeline=pipeline)
+    cfg = P.Config(scene=scene, max_path_length=12, em_sampler=R.EM_STEERABLE, pipeline=pipeline,
+                   steer_weights=weights)
     spp = 32768
     with P.GpuPathTracer(cfg, seed=123) as r:
         r.RunIteration(R.kPathTracing, 0, spp)
         mean, var, n = r.framebuffer(with_variance=True)
     frac, zm, zs = z_ok(zscores(mean, var / spp, d["mean"], d["var_mean"]))
     assert frac >= 0.999 and abs(zm) < 0.25 and 0.7 < zs < 1.3, (frac, zm, zs)
+
+
+def test_projected_weights_are_reproducible(tmp_path):
+    # the projection sums texel contributions in fixed point: the same scene and seed give the
+    # same vertex weights and the same image, bit for bit, whatever the order of the atomics
+    cfg = _env_scene(R.EM_STEERABLE, PJ)
+    imgs, files = [], []
+    for k in range(2):
+        with P.GpuPathTracer(cfg, seed=3) as r:
+            r.RunIteration(R.kPathTracing, 0, 16)
+            imgs.append(r.framebuffer()[0])
+            f = str(tmp_path / ("w%d.emssd" % k))
+            r.save_steerable(f)
+            files.append(open(f, "rb").read())
+    assert np.array_equal(imgs[0], imgs[1])
+    assert files[0] == files[1]
+    # and the projection is not the point sample (the sky's suns lie between vertices)
+    with P.GpuPathTracer(_env_scene(R.EM_STEERABLE, PT), seed=3) as r:
+        f = str(tmp_path / "point.emssd")
+        r.save_steerable(f)
+        assert open(f, "rb").read() != files[0]
