@@ -238,7 +238,7 @@ extern "C" int pg3gpu_set_params(pg3gpu_ctx *ctx, const float *mp, const float *
                                                                             ctx->nmat, dm, keep ? 1 : 0);
     if (!st && de) {
         setEnvKernel<<<(ntex + 255) / 256, 256, 0, ctx->stream>>>(const_cast<float4 *>(v.em), ntex, de);
-        if (rebuild) {
+        if (rebuild && v.emSampler == kEmCdf) {   // CDF tables exist for the CDF sampler only
             if (!ctx->dRowInt) st = ctxAlloc(ctx, &ctx->dRowInt, v.emH);
             if (!st) {
                 cdfRowsKernel<<<v.emH, kCdfBlock, v.emW * sizeof(float), ctx->stream>>>(
@@ -246,9 +246,10 @@ extern "C" int pg3gpu_set_params(pg3gpu_ctx *ctx, const float *mp, const float *
                 cdfMarginalKernel<<<1, kCdfBlock, v.emH * sizeof(float), ctx->stream>>>(
                     ctx->dRowInt, v.emH, const_cast<float *>(v.emMarg));
             }
-            // the steerable sampler's weights (and with them the background's picking estimate)
-            if (!st && ctx->hasSteer) st = cudaStatus(ctx, launchSteerWeights(ctx->steerArgs, ctx->stream), "steerable build");
         }
+        // the steerable sampler's weights (and with them the background's picking estimate)
+        if (rebuild && !st && ctx->hasSteer)
+            st = cudaStatus(ctx, launchSteerWeights(ctx->steerArgs, ctx->stream), "steerable build");
     }
     if (!st) st = cudaStatus(ctx, cudaGetLastError(), "parameter update");
     if (!temps.empty()) {

@@ -335,7 +335,8 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
                 return bad(PG3GPU_ERR_INVALID_ARGUMENT, "environment map texels must be finite and non-negative");
             out.em[i] = make_float4(p[0], p[1], p[2], 0.f);
         }
-        buildEmCdf(sc.env_map, sc.env_width, sc.env_height, out.emMarg, out.emCond);
+        // the CDF tables serve the CDF sampler only (the device rebuilds them on map updates)
+        if (o.em_sampler == PG3GPU_EM_CDF) buildEmCdf(sc.env_map, sc.env_width, sc.env_height, out.emMarg, out.emCond);
         v.emW = sc.env_width;
         v.emH = sc.env_height;
         if (o.em_sampler == PG3GPU_EM_STEERABLE) {
