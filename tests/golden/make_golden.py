@@ -29,10 +29,11 @@ from pg3render_gb300 import scene as S  # noqa: E402
 
 CASES = {
     # name: (builder, max_path_length, em_sampler, algorithm, renderers, iterations)
-    "cornell_area_32": (lambda: S.cornell_box(32, 32), 8, "cdf", "pt", 64, 128),
+    # the two benchmark scenes at 65536 samples per pixel (64 renderers x 1024 iterations)
+    "cornell_area_32": (lambda: S.cornell_box(32, 32), 8, "cdf", "pt", 64, 1024),
     "cornell_area_32_naive": (lambda: S.cornell_box(32, 32), 8, "cdf", "ptn", 64, 128),
     "cornell_area_32_rr": (lambda: S.cornell_box(32, 32), 0, "cdf", "pt", 64, 128),
-    "cornell_env_32_cdf": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cdf", "pt", 64, 128),
+    "cornell_env_32_cdf": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cdf", "pt", 64, 1024),
     "cornell_env_32_cos": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cosine", "pt", 64, 128),
     # direct illumination, eye light, normal visualiser (one hit; src/direct_illumination.hxx,
     # src/eye_light.hxx, src/normal_visualiser.hxx)

@@ -59,7 +59,10 @@ def test_oracle_matches_reference_golden(name):
            "preset_00": 8192, "preset_03": 8192, "preset_07": 8192, "preset_29": 8192, "preset_01": 32768,
            "preset_05": 32768, "preset_16": 32768, "preset_19": 32768, "preset_31": 32768,
            "preset_38": 32768, "preset_27_dmis": 8192, "preset_27_dlss": 8192, "cornell_mixedsra_32_dmis": 8192,
-           "cornell_mixedsra_32_dbs": 8192}.get(name, 1024)
+           "cornell_mixedsra_32_dbs": 8192,
+           # the benchmark scenes: the oracle's 64k-spp render against the reference's 64k-spp golden
+           # (at 1-8k spp the heavy tails skew the z distribution against so tight a golden)
+           "cornell_area_32": 65536, "cornell_env_32_cdf": 65536}.get(name, 1024)
     o = O.render(text, 32, 32, seed=99, spp=spp, em_sampler=sampler)
     m = o["sum"] / spp
     v = np.maximum(o["sumsq"] / spp - m * m, 0.0) / spp

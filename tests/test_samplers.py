@@ -196,7 +196,7 @@ def test_steerable_render_converges_to_reference(pipeline, weights):
     scene = scene_from_golden(d)
     cfg = P.Config(scene=scene, max_path_length=12, em_sampler=R.EM_STEERABLE, pipeline=pipeline,
                    steer_weights=weights)
-    spp = 32768
+    spp = 65536   # as many samples as the reference's golden
     with P.GpuPathTracer(cfg, seed=123) as r:
         r.RunIteration(R.kPathTracing, 0, spp)
         mean, var, n = r.framebuffer(with_variance=True)

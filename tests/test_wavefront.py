@@ -60,7 +60,7 @@ def test_wavefront_against_reference_golden(name):
     d, text, td = load_golden(name)
     scene = scene_from_golden(d)
     cfg = P.Config(scene=scene, max_path_length=int(d["max_path_length"]), pipeline=R.PIPELINE_WAVEFRONT)
-    spp = 16384
+    spp = max(16384, int(d["spp"]))   # the benchmark scenes' goldens: 65536 samples per pixel
     with P.GpuPathTracer(cfg, seed=77) as r:
         r.RunIteration(R.kPathTracing, 0, spp)
         mean, var, n = r.framebuffer(with_variance=True)
