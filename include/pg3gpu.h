@@ -312,9 +312,10 @@ int pg3gpu_probe_light_pdf(pg3gpu_ctx *ctx, int32_t light, uint32_t n, const flo
 int pg3gpu_export_bvh(pg3gpu_ctx *ctx, uint32_t *num_prims, uint32_t *codes, uint32_t *ids, float *nodes);
 
 /* Allocation-free rendering. No counterpart in the reference.
- * For callers that may not allocate device memory once they are running: a frame
- * loop captured into a CUDA graph (cudaMalloc cannot be captured), or an engine whose
- * device memory belongs to its own allocator after start-up. Renders samples
+ * For callers that may not allocate device memory once they are running: a plugin
+ * inside a host application or engine whose device memory belongs to that host's own
+ * allocator, or a real-time loop with a fixed memory budget that must not fail for lack
+ * of memory half-way through a session. Renders samples
  * `iteration` .. iteration+spp-1 of the context's scene exactly like
  * pg3gpu_run_iteration, but adds them to the caller's device arrays sum_rgb and
  * sumsq_rgb (width*height*3 doubles each; sum and sum of squares; never cleared by

@@ -570,9 +570,10 @@ int pg3gpu_device_framebuffer(pg3gpu_ctx *ctx, const double **sum, const double 
 // ------------------------------------------------------------------------------------------
 // Rendering without device allocations (no counterpart in the reference).
 //
-// For callers that may not allocate device memory once they are running -- a frame loop
-// captured into a CUDA graph (cudaMalloc cannot be captured), or an engine whose device
-// memory belongs to its own allocator after start-up. The per-sample radiance of a launch
+// For callers that may not allocate device memory once they are running -- a plugin inside
+// a host application or engine whose device memory belongs to that host's own allocator, or
+// a real-time loop with a fixed memory budget that must not fail for lack of memory half-way
+// through a session. The per-sample radiance of a launch
 // chunk lives in this file-scope array instead of a cudaMalloc'd buffer; every GPU that
 // loads the library holds it (12 MiB) until the process exits.
 // ------------------------------------------------------------------------------------------

@@ -1,8 +1,9 @@
 """The allocation-free entry point pg3gpu_run_iteration_noalloc (GPU).
 
-Some callers cannot allocate device memory once they run -- a frame loop captured
-into a CUDA graph, where cudaMalloc cannot be captured, or an engine whose device
-memory belongs to its own allocator. For them the library keeps the per-sample
+Some callers cannot allocate device memory once they run -- a plugin inside a host
+application or engine whose device memory belongs to that host's own allocator, or a
+real-time loop with a fixed memory budget that must not run out of memory half-way
+through a session. For them the library keeps the per-sample
 radiance of a launch in a fixed scratch area compiled into it, and the caller
 passes the output arrays. This test calls that entry point through the C ABI
 twice in a row and checks the accumulated result against the regular entry point
