@@ -36,6 +36,40 @@ namespace pg3 {
 
 namespace {
 
+// Programmatic dependent launch between the stage kernels of a bounce: each stage kernel is
+// launched while its predecessor drains, its blocks wait in griddepcontrol.wait until the
+// predecessor has completed and its writes are visible, and only then let their own successor
+// launch. The launch latency and block start-up of ~97 launches per chunk overlap the tail
+// of the previous kernel. griddepcontrol.wait is a no-op in a kernel launched without the
+// attribute, so every other launch path of these kernels is unchanged.
+#ifndef PG3_PDL
+#define PG3_PDL 1
+#endif
+
+PG3_DI void stageEntry()
+{
+#if PG3_PDL
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
+template <typename... Params, typename... Args>
+void launchStage(bool pdl, void (*kernel)(Params...), int grid, size_t smem, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kWaveBlock);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = (PG3_PDL && pdl) ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
+}
+
 template <bool GRAD>
 PG3_DI uint32_t sampleBase(uint32_t sample0, const GradArgs &G)
 {
@@ -48,6 +82,7 @@ __global__ void __launch_bounds__(kWaveBlock) raygenKernel(const __grid_constant
                                                            uint32_t sample0, float *outR, float *outG, float *outB,
                                                            DevStats *stats, GradArgs G)
 {
+    stageEntry();
     sample0 = sampleBase<GRAD>(sample0, G);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint64_t g = base + i;
@@ -77,6 +112,7 @@ __global__ void __launch_bounds__(kWaveBlock) raygenKernel(const __grid_constant
 __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) extendKernel(const __grid_constant__ SceneView S, Queues Q, int cur,
                                                            DevStats *stats)
 {
+    stageEntry();
     const uint32_t n = Q.cnt->ray[cur];
     const float4 *rq = rayQ(Q, cur);
     uint32_t rays = 0;
@@ -129,6 +165,7 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
                 uint32_t sample0, float *outR, float *outG, float *outB, DevStats *stats, GradArgs G)
 {
     extern __shared__ float sGrad[];
+    stageEntry();
     initBlockGrad<GRAD>(sGrad, S.nmat);
     sample0 = sampleBase<GRAD>(sample0, G);
     constexpr int kBucket = bucketOfShade(K);
@@ -182,6 +219,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) shadowKernel
 {
     constexpr int SW = kShadowWords<GRAD>;
     extern __shared__ float sGrad[];
+    stageEntry();
     initBlockGrad<GRAD>(sGrad, S.nmat);
     const uint32_t n = Q.cnt->shadow;
     uint32_t cnt = 0;
@@ -214,6 +252,8 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) shadowKernel
 
 __global__ void advanceKernel(Counters *c, int cur)
 {
+    stageEntry();
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;   // launched with one block of the stage size
     c->ray[cur] = 0;
     for (int b = 0; b < kNumBuckets; ++b) c->bucket[b] = 0;
     c->shadow = 0;
@@ -246,10 +286,10 @@ Queues carve(void *scratch, uint64_t cap, bool grad)
 template <int K, int EMK, bool GRAD>
 void launchShadeKind(const SceneView &S, const Queues &Q, int cur, uint32_t base, uint32_t npix, uint32_t sample0,
                      float *r, float *g, float *b, DevStats *stats, int grid, size_t smem, const GradArgs &G,
-                     cudaStream_t st, int &launched)
+                     cudaStream_t st, bool pdl, int &launched)
 {
     const int blocks = std::max(1, grid / (1024 / kWaveBlock)) * 2 * shadeMinBlocks(K);
-    shadeKernel<K, EMK, GRAD><<<blocks, kWaveBlock, smem, st>>>(S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+    launchStage(pdl, shadeKernel<K, EMK, GRAD>, blocks, smem, st, S, Q, cur, base, npix, sample0, r, g, b, stats, G);
     ++launched;
 }
 
@@ -258,20 +298,20 @@ void launchShadeKind(const SceneView &S, const Queues &Q, int cur, uint32_t base
 template <int EMK, bool GRAD>
 int launchShade(const SceneView &S, uint32_t kindMask, const Queues &Q, int cur, uint32_t base, uint32_t npix,
                 uint32_t sample0, float *r, float *g, float *b, DevStats *stats, int grid, size_t smem,
-                const GradArgs &G, cudaStream_t st)
+                const GradArgs &G, cudaStream_t st, bool pdl)
 {
     int n = 0;
-    launchShadeKind<-1, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+    launchShadeKind<-1, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
     if (kindMask & (1u << kMatLambert))
-        launchShadeKind<kMatLambert, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+        launchShadeKind<kMatLambert, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
     if (kindMask & (1u << kMatGgxConductor))
-        launchShadeKind<kMatGgxConductor, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+        launchShadeKind<kMatGgxConductor, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
     if (kindMask & (1u << kMatGgxDielectric))
-        launchShadeKind<kMatGgxDielectric, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+        launchShadeKind<kMatGgxDielectric, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
     if (kindMask & (1u << kMatPhong))
-        launchShadeKind<kMatPhong, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+        launchShadeKind<kMatPhong, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
     if (kindMask & ((1u << kMatSmoothConductor) | (1u << kMatSmoothDielectric)))
-        launchShadeKind<kShadeSmooth, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, n);
+        launchShadeKind<kShadeSmooth, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
     return n;
 }
 
@@ -303,18 +343,19 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
         *launches += 1;
         for (uint32_t bounce = 0; bounce < maxBounces; ++bounce) {
             const int cur = bounce & 1;
-            extendKernel<<<queryGrid, kWaveBlock, 0, stream>>>(S, Q, cur, stats);
+            const bool pdl = capturing == cudaStreamCaptureStatusNone;
+            launchStage(pdl, extendKernel, queryGrid, 0, stream, S, Q, cur, stats);
             const int emk = (S.bgKind == kBgEnvMap) ? S.emSampler : kEmCosine;   // no map: constant/area paths
             const uint32_t b32 = (uint32_t)base;
             int shades;
             if (emk == kEmCdf)
-                shades = launchShade<kEmCdf, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
+                shades = launchShade<kEmCdf, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
             else if (emk == kEmSteerable)
-                shades = launchShade<kEmSteerable, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
+                shades = launchShade<kEmSteerable, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
             else
-                shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream);
-            shadowKernel<GRAD><<<queryGrid, kWaveBlock, smem, stream>>>(S, Q, r, g, b, stats, G);
-            advanceKernel<<<1, 1, 0, stream>>>(Q.cnt, cur);
+                shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
+            launchStage(pdl, shadowKernel<GRAD>, queryGrid, smem, stream, S, Q, r, g, b, stats, G);
+            launchStage(pdl, advanceKernel, 1, 0, stream, Q.cnt, cur);
             *launches += 3 + shades;
             if (S.maxPL == 0 && (bounce & 7) == 7 && capturing == cudaStreamCaptureStatusNone) {
                 // roulette-ended paths: stop once the queue is empty (checked every 8 bounces)
