@@ -88,11 +88,14 @@ int ensureOutput(pg3gpu_ctx *ctx, uint64_t paths)
     return PG3GPU_OK;
 }
 
-// Wavefront queues for launches of `paths` paths: max_paths_in_flight slots (default 2^22), fewer
-// when a launch has fewer paths; they only grow.
+// Wavefront queues for launches of `paths` paths: max_paths_in_flight slots (default 2^24, the
+// slot-index limit: 292 bytes per slot, 4.6 GiB at most), fewer when a launch has fewer paths;
+// they only grow. A launch chunk then holds all paths of up to 2^24 samples, so the sparse
+// late bounces, where roulette has ended most paths, repeat once per 2^24 paths instead of once
+// per 2^22 (+20% on the 512x512 x 256 spp environment-map benchmark).
 int ensureWave(pg3gpu_ctx *ctx, uint64_t paths)
 {
-    const uint64_t cap = ctx->opts.max_paths_in_flight ? ctx->opts.max_paths_in_flight : (1ull << 22);
+    const uint64_t cap = ctx->opts.max_paths_in_flight ? ctx->opts.max_paths_in_flight : (1ull << 24);
     const uint64_t want = std::min<uint64_t>(cap, paths);
     if (ctx->dWave && ctx->waveCapacity >= want) return PG3GPU_OK;
     ctxFree(ctx, ctx->dWave);
