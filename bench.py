@@ -51,8 +51,8 @@ EM_W, EM_H = 1024, 512
 BYTES_PER_SEGMENT = 360
 BYTES_PER_PATH = 72 + 36
 # DRAM bytes (read + write) per camera path of one launch chunk, measured by ncu over all stage
-# kernels of one step of the 128x128 x 64 spp case of this workload (one chunk of 2^20 paths;
-# profiles/wavefront_cornell_env.md); the chunk's traffic grows with its paths.
+# kernels of one step of the 128x128 x 64 spp case of this workload (one chunk of 2^20 paths);
+# the chunk's traffic grows with its paths.
 NCU_TRAFFIC_PER_PATH = 1043.8
 
 
@@ -193,25 +193,31 @@ def cpu_baseline(scene, sampler, threads=None, iters=1):
                 "sample": "%d spp of the %dx%d scene" % (spp, WIDTH, HEIGHT)}
 
 
-def matched_quality(gpu_value, cpu_value, steer_weights, side=128, spps=(16, 256), renders=(4, 2),
-                    conv_spp=16384):
-    """Per-sample quality of the two renderers on the headline scene at side x side: the
-    relative MSE, mean over pixel channels of (x - c)^2 / (c^2 + 0.01), of images of spp samples
-    against a converged image c (this library, CDF sampler, conv_spp samples per pixel), averaged
-    over independent images, for the GPU path (roulette from length 4; steerable sampler with
-    both vertex weightings, and the CDF sampler) and for the reference's own CPU renderer (max
-    length 12 without roulette; its steerable sampler at 1280 triangles and its CDF sampler).
-    The reference's steerable sampler evaluates its pdf from the map instead of the density it
-    samples, so its images converge to a darker limit (bias). At the benchmark's 256 samples per
-    pixel, the ratio of the relative MSEs turns the Msamples/s ratio into an equal-quality speedup:
-    the GPU renders the samples that reach the reference's error in that many times less time."""
+def matched_quality(gpu_value, cpu_value, steer_weights, spps=(16, 256), renders=(16, 8)):
+    """Per-sample quality of the two renderers on the headline scene (its full 1024x512 sky) at
+    64x64 pixels: the relative MSE, mean over pixel channels of (x - c)^2 / (c^2 + 0.01), of
+    images of spp samples against the converged image c, averaged over independent images. c is
+    the reference's own CPU renderer at 65536 samples per pixel (CDF sampler, max length 12;
+    the committed fixture tests/golden/cornell_env_64_sky1024_cdf.npz, made by
+    tests/golden/make_golden.py). Measured for the GPU path (roulette from length 4; steerable
+    sampler with both vertex weightings, and the CDF sampler) and for the reference's own CPU
+    renderer (max length 12 without roulette; its steerable sampler at 1280 triangles and its
+    CDF sampler). The reference's steerable sampler evaluates its pdf from the map instead of
+    the density it samples, so its images converge to a darker limit (bias). At the benchmark's
+    256 samples per pixel, the ratio of the relative MSEs turns the Msamples/s ratio into an
+    equal-quality speedup: the GPU renders the samples that reach the reference's error in that
+    many times less time."""
     import numpy as np
     import pg3render_gb300 as P
     from pg3render_gb300 import scene as S
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     R = P.renderer
+    golden = np.load(os.path.join(ROOT, "tests", "golden", "cornell_env_64_sky1024_cdf.npz"))
+    conv = golden["mean"]
+    side = conv.shape[0]
     sc = S.cornell_env(side, side, EM_W, EM_H, em_seed=7)
+    sc.env_map = golden["env_map"]   # the map the reference rendered (bit for bit)
     gpu_cfgs = {"steerable_point": (R.EM_STEERABLE, R.STEER_WEIGHTS_POINT),
                 "steerable_projected": (R.EM_STEERABLE, R.STEER_WEIGHTS_PROJECTED), "cdf": (R.EM_CDF, 0)}
 
@@ -223,12 +229,11 @@ def matched_quality(gpu_value, cpu_value, steer_weights, side=128, spps=(16, 256
             r.RunIteration(R.kPathTracing, 0, n)
             return r.framebuffer()[0]
 
-    conv = gpu_image("cdf", 99991, conv_spp)
-
     def rel_mse(img):
         return float(np.mean((img - conv) ** 2 / (conv ** 2 + 0.01)))
 
-    out = {"side": side, "converged": "this library, CDF sampler, %d spp" % conv_spp}
+    out = {"side": side, "converged": "the reference's CPU renderer, CDF sampler, %d spp (max path length 12)"
+           % int(golden["spp"])}
     with tempfile.TemporaryDirectory() as td:
         em_path = os.path.join(td, "em.bin")
         sc.write_env_map(em_path)

@@ -316,20 +316,25 @@ int pg3gpu_export_bvh(pg3gpu_ctx *ctx, uint32_t *num_prims, uint32_t *codes, uin
  * inside a host application or engine whose device memory belongs to that host's own
  * allocator, or a real-time loop with a fixed memory budget that must not fail for lack
  * of memory half-way through a session. Renders samples
- * `iteration` .. iteration+spp-1 of the context's scene exactly like
- * pg3gpu_run_iteration, but adds them to the caller's device arrays sum_rgb and
+ * `iteration` .. iteration+spp-1 of the context's scene like pg3gpu_run_iteration
+ * (same paths, same refusals), but adds them to the caller's device arrays sum_rgb and
  * sumsq_rgb (width*height*3 doubles each; sum and sum of squares; never cleared by
- * this call) instead of the context's framebuffer. The per-sample radiance lives in
- * a scratch area compiled into the library: PG3GPU_NOALLOC_MAX_PATHS paths (12 MiB),
- * held by every GPU that loads the library until the process exits. The call
- * allocates nothing (no cudaMalloc, cudaFree or allocating library routine); images
- * of more than PG3GPU_NOALLOC_MAX_PATHS pixels are rejected with
- * PG3GPU_ERR_INVALID_ARGUMENT. The first call on a device looks up the scratch
- * area's device address: make that first call before any stream capture. All calls
- * share the one scratch area and it keeps the last call's contents (nothing in it
- * needs to start at zero): calls that overlap on the GPU -- on other streams or from
- * other host threads -- race, so the caller must serialise them. Asynchronous, on
- * the context's stream, like pg3gpu_run_iteration. */
+ * this call) instead of the context's framebuffer. It always runs the megakernel
+ * pipeline (one kernel per path; the wavefront pipeline's queues would need device
+ * memory): on the 512x512 environment-map benchmark about a third of the throughput of
+ * pg3gpu_run_iteration, which runs algorithm 7 on the wavefront pipeline. The
+ * per-sample radiance lives in a scratch area compiled into the library:
+ * PG3GPU_NOALLOC_MAX_PATHS paths (12 MiB); a GPU holds it from the first
+ * pg3gpu_create on that device until the process exits, because pg3gpu_create looks up
+ * the area's device address (and so loads it). The call itself then allocates nothing
+ * and makes no lookup (no cudaMalloc, cudaFree, module load or allocating library
+ * routine); images of more than PG3GPU_NOALLOC_MAX_PATHS pixels are rejected with
+ * PG3GPU_ERR_INVALID_ARGUMENT, splitting or clipping options (frame stacks in device
+ * memory) with PG3GPU_ERR_UNSUPPORTED. All calls share the one scratch area and it
+ * keeps the last call's contents (nothing in it needs to start at zero): calls that
+ * overlap on the GPU -- on other streams or from other host threads -- race, so the
+ * caller must serialise them. Asynchronous, on the context's stream, like
+ * pg3gpu_run_iteration. */
 #define PG3GPU_NOALLOC_MAX_PATHS (1u << 20)
 int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration, uint32_t spp,
                                  double *sum_rgb, double *sumsq_rgb);

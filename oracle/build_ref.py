@@ -35,7 +35,20 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 STUBS = os.path.join(HERE, "stubs")
-DEFAULT_REF = "/root/reference"
+
+
+def default_ref_root():
+    """The reference checkout: $PG3_REFERENCE_ROOT, else the `reference_path` of the repository's
+    the benchmark spec (None when neither names one)."""
+    env = os.environ.get("PG3_REFERENCE_ROOT")
+    if env:
+        return env
+    try:
+        import json
+        with open(os.path.join(os.path.dirname(HERE), "BASELINE.json")) as f:
+            return json.load(f).get("reference_path")
+    except (OSError, ValueError):
+        return None
 
 
 def _sub_lines(text, first, last, pattern, repl):
@@ -171,9 +184,9 @@ def _wait(entry):
 
 
 def build(ref_root=None, jobs=3, variants=None):
-    ref_root = ref_root or os.environ.get("PG3_REFERENCE_ROOT", DEFAULT_REF)
+    ref_root = ref_root or default_ref_root()
     os.makedirs(OUT, exist_ok=True)
-    if os.path.isdir(os.path.join(ref_root, "src")):
+    if ref_root and os.path.isdir(os.path.join(ref_root, "src")):
         copy_and_patch(ref_root)
     elif not os.path.isdir(SRC):
         return False

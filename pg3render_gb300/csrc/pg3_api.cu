@@ -144,15 +144,23 @@ void foldTimers(pg3gpu_ctx *ctx)
     ctx->pendingTimers = 0;
 }
 
-// algorithm: 7 runs on the wavefront pipeline (unless the megakernel was chosen), the others
-// on the megakernel
-int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passes)
+// Scene / algorithm combinations the path kernels refuse before any launch (every entry point
+// that renders calls this).
+int checkRenderable(pg3gpu_ctx *ctx, int algorithm)
 {
     if ((ctx->kindMask & (1u << kMatSra)) &&
         (algorithm == PG3GPU_ALG_PATH_TRACING || algorithm == PG3GPU_ALG_PATH_TRACING_NAIVE))
         return fail(ctx, PG3GPU_ERR_UNSUPPORTED,
                     "the SRA layered material has no roulette probability or zero-reflectance test, so the path "
                     "tracers cannot render it (the reference stops with a fatal error, src/materials.hxx:1544-1557)");
+    return PG3GPU_OK;
+}
+
+// algorithm: 7 runs on the wavefront pipeline (unless the megakernel was chosen), the others
+// on the megakernel
+int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passes)
+{
+    if (int st = checkRenderable(ctx, algorithm)) return st;
     const uint32_t npix = ctx->W * ctx->H;
     const uint64_t paths = (uint64_t)passes * npix;
     int st = ensureOutput(ctx, paths);
@@ -276,6 +284,7 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
         return s;
     };
     if (cudaSetDevice(device) != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "cudaSetDevice failed"));
+    if (!forBatch) resolveNoallocScratch(device);
 
     SceneView &v = ctx->view;
     v = hs.view;   // camera, counts, options
@@ -577,8 +586,8 @@ int pg3gpu_device_framebuffer(pg3gpu_ctx *ctx, const double **sum, const double 
 // a host application or engine whose device memory belongs to that host's own allocator, or
 // a real-time loop with a fixed memory budget that must not fail for lack of memory half-way
 // through a session. The per-sample radiance of a launch
-// chunk lives in this file-scope array instead of a cudaMalloc'd buffer; every GPU that
-// loads the library holds it (12 MiB) until the process exits.
+// chunk lives in this file-scope array instead of a cudaMalloc'd buffer; every GPU on which a
+// context is created holds it (12 MiB) from that first context until the process exits.
 // ------------------------------------------------------------------------------------------
 namespace {
 
@@ -587,23 +596,45 @@ static __device__ __align__(256) float g_noallocRadiance[3 * (size_t)kNoAllocMax
 
 constexpr int kNoAllocMaxDevices = 64;
 float *g_noallocAddress[kNoAllocMaxDevices] = {};
+std::string g_noallocError[kNoAllocMaxDevices];
 std::mutex g_noallocMutex;
 
-// Device address of the scratch array on ctx's device. In host code the array's name is a
-// host-side stand-in, not a device address, so it is looked up once per device with that
-// device current (the caller has made it current).
+}  // namespace
+
+// Looks up the scratch array's device address on `device` (which the caller has made current)
+// once per device, when the first context on that device is created. In host code the array's
+// name is a host-side stand-in, not a device address. This file has no kernels, so under lazy
+// module loading the array's module -- and its 12 MiB -- is loaded by this lookup: doing it at
+// context creation keeps the allocation-free call itself free of any module load or allocation.
+// A failed lookup does not fail the context (the regular entry points do not need the array);
+// the allocation-free call then reports the recorded reason.
+void pg3::resolveNoallocScratch(int device)
+{
+    if (device < 0 || device >= kNoAllocMaxDevices) return;
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (g_noallocAddress[device]) return;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocRadiance);
+    if (e != cudaSuccess || !p) {
+        g_noallocError[device] = std::string("cudaGetSymbolAddress of the scratch area: ") + cudaGetErrorString(e);
+        cudaGetLastError();   // not sticky: clear it so the context's next call does not see it
+        return;
+    }
+    g_noallocAddress[device] = static_cast<float *>(p);
+}
+
+namespace {
+
+// The cached device address of the scratch array on ctx's device (looked up at context
+// creation; no CUDA call here).
 int noallocScratch(pg3gpu_ctx *ctx, float **out)
 {
     if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
         return fail(ctx, PG3GPU_ERR_UNSUPPORTED, "device %d: no scratch slot", ctx->device);
     std::lock_guard<std::mutex> lock(g_noallocMutex);
-    if (!g_noallocAddress[ctx->device]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocRadiance);
-        if (e != cudaSuccess || !p)
-            return fail(ctx, PG3GPU_ERR_CUDA, "cudaGetSymbolAddress of the scratch area: %s", cudaGetErrorString(e));
-        g_noallocAddress[ctx->device] = static_cast<float *>(p);
-    }
+    if (!g_noallocAddress[ctx->device])
+        return fail(ctx, PG3GPU_ERR_CUDA, "no scratch area on device %d: %s", ctx->device,
+                    g_noallocError[ctx->device].empty() ? "not looked up" : g_noallocError[ctx->device].c_str());
     *out = g_noallocAddress[ctx->device];
     return PG3GPU_OK;
 }
@@ -625,6 +656,7 @@ extern "C" int pg3gpu_run_iteration_noalloc(pg3gpu_ctx *ctx, int32_t algorithm, 
     if (algorithm == PG3GPU_ALG_PATH_TRACING && ctx->view.treeMode)
         return fail(ctx, PG3GPU_ERR_UNSUPPORTED,
                     "splitting / clipping keep frame stacks in device memory: use pg3gpu_run_iteration");
+    if (int st = checkRenderable(ctx, algorithm)) return st;
     if (spp == 0) return PG3GPU_OK;
     PG3_CUDA(ctx, cudaSetDevice(ctx->device));
     float *scratch = nullptr;

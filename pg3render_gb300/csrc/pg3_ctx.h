@@ -76,6 +76,10 @@ int ctxError(pg3gpu_ctx *ctx, int status, const std::string &msg);
 int createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, bool forBatch,
                   pg3gpu_ctx **out);
 
+// Looks up, once per device, the device address of the allocation-free entry point's scratch
+// array (pg3_api.cu); `device` must be current.
+void resolveNoallocScratch(int device);
+
 inline int cudaStatus(pg3gpu_ctx *ctx, cudaError_t e, const char *what)
 {
     if (e == cudaSuccess) return PG3GPU_OK;

@@ -1,5 +1,6 @@
 """Shared helpers of the tests: golden fixtures, z-tests, oracle scenes."""
 import os
+import re
 import tempfile
 
 import numpy as np
@@ -63,6 +64,9 @@ def scene_from_golden(d):
         s = S.cornell_box_bg(32, 32)
     elif name.startswith("cornell_envarea_"):
         s = S.cornell_env_area(32, 32, 64, 32)
+    elif re.match(r"cornell_env_\d+x\d+_em\d+x\d+$", name):
+        w, h, ew, eh = map(int, re.findall(r"\d+", name))
+        s = S.cornell_env(w, h, ew, eh)
     else:
         s = S.cornell_env(32, 32, 64, 32)
     if s.env_map is not None:

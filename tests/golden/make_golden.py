@@ -35,6 +35,10 @@ CASES = {
     "cornell_area_32_rr": (lambda: S.cornell_box(32, 32), 0, "cdf", "pt", 64, 128),
     "cornell_env_32_cdf": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cdf", "pt", 64, 1024),
     "cornell_env_32_cos": (lambda: S.cornell_env(32, 32, 64, 32), 12, "cosine", "pt", 64, 128),
+    # the environment-map benchmark scene with its full 1024x512 sky (sun lobes of 1-3 degrees,
+    # peak 1e4 x the sky mean) at 64x64 pixels and 65536 samples per pixel (256 renderers x 256
+    # iterations): the image the benchmark's own sampler setup (steerable, roulette) must match
+    "cornell_env_64_sky1024_cdf": (lambda: S.cornell_env(64, 64, 1024, 512), 12, "cdf", "pt", 256, 256),
     # direct illumination, eye light, normal visualiser (one hit; src/direct_illumination.hxx,
     # src/eye_light.hxx, src/normal_visualiser.hxx)
     "cornell_area_32_dbs": (lambda: S.cornell_box(32, 32), 8, "cdf", "dbs", 64, 128),
