@@ -77,7 +77,7 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the batched (64 scenes), forward+adjoint and inverse-rendering measurements")
     ap.add_argument("--only-secondary", default=None,
-                    choices=["batched", "differentiable", "inverse_rendering", "mesh_bvh"],
+                    choices=["batched", "differentiable", "inverse_rendering", "mesh_bvh", "per_iteration"],
                     help="run one secondary measurement alone and print its JSON (profiling captures)")
     ap.add_argument("--mesh-side", type=int, default=512, help="image side of the LBVH mesh measurement")
     ap.add_argument("--mesh-spp", type=int, default=64, help="samples per pixel of the LBVH mesh measurement")
@@ -589,10 +589,64 @@ def mesh_metric(reps=3):
             "timing": "host wall clock of whole runs incl. synchronisation, median of %d" % reps}
 
 
+def per_iteration_metric(iters=256, reps=3):
+    """The call pattern of the reference's own render loop: one pg3gpu_run_iteration per
+    iteration, one sample per pixel each (RunIteration, src/pg3render.cxx:112-128), on the
+    headline scene at 512x512 (the headline's 256 iterations), against one call of all 256.
+    Also the reference's own program with the GPU renderer (oracle/_ref/pg3render_gpu: its
+    Config, its LoadCornellBox scene -s 12 at its fixed 512x512, GpuPathTracer::RunIteration
+    per iteration) where that program is built."""
+    import torch
+    import pg3render_gb300 as P
+    R = P.renderer
+    sc = build_scene()
+    cfg = P.Config(scene=sc, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM, em_sampler=R.EM_STEERABLE)
+    paths = WIDTH * HEIGHT * iters
+    out = {"metric": "Msamples/s, one sample per pixel per call", "side": WIDTH, "iterations": iters}
+    with P.GpuPathTracer(cfg) as r:
+        for k in range(8):
+            r.RunIteration(R.kPathTracing, k, 1)
+        r.RunIteration(R.kPathTracing, 8, iters)
+        r.synchronize()
+        r.reset_stats()
+        for k in range(16):
+            r.RunIteration(R.kPathTracing, 500 + k, 1)
+        launches = r.stats()["kernel_launches"] / 16
+        per, whole = [], []
+        for rep in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(iters):
+                r.RunIteration(R.kPathTracing, (rep + 1) * 1000 + k, 1)
+            r.synchronize()
+            per.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            r.RunIteration(R.kPathTracing, (rep + 1) * 1000, iters)
+            r.synchronize()
+            whole.append(time.perf_counter() - t0)
+    tp, tw = statistics.median(per), statistics.median(whole)
+    out.update(per_call_msamples_per_s=round(paths / tp / 1e6, 1), one_call_msamples_per_s=round(paths / tw / 1e6, 1),
+               per_call_us=round(tp / iters * 1e6, 1), launches_per_call=round(launches, 1),
+               timing="host wall clock of %d calls incl. the final synchronisation, median of %d" % (iters, reps))
+    exe = os.path.join(ROOT, "oracle", "_ref", "pg3render_gpu")
+    if os.path.exists(exe):
+        prog = {}
+        for batch in (1, iters):
+            res = subprocess.run([exe, "-s", "12", "-a", "pt", "-minpl", "1", "-maxpl", "8", "-sb", "1", "-iic", "0",
+                                  "-i", str(iters), "-q", "--batch", str(batch)], capture_output=True, text=True)
+            if res.returncode != 0:
+                prog["error"] = res.stderr.strip()[-300:]
+                break
+            prog["batch_%d" % batch] = json.loads(res.stdout.strip().splitlines()[-1])
+        out["reference_program"] = prog
+    return out
+
+
 def secondary_metrics(only=None):
     out = {}
     for name, fn in (("batched", batched_metric), ("differentiable", differentiable_metric),
-                     ("inverse_rendering", inverse_metric), ("mesh_bvh", mesh_metric)):
+                     ("inverse_rendering", inverse_metric), ("mesh_bvh", mesh_metric),
+                     ("per_iteration", per_iteration_metric)):
         if only and name != only:
             continue
         try:

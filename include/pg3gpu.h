@@ -169,12 +169,29 @@ typedef struct pg3gpu_options {
     float splitting_level;           /* mDbgSplittingLevel in [0, 1] (1: the whole budget at the first vertex) */
     float light_to_bsdf_ratio;       /* mDbgSplittingLightToBrdfSmplRatio, > 0 */
     int32_t steer_weights;           /* PG3GPU_STEER_WEIGHTS_*: vertex luminance of the steerable sampler */
+    uint32_t steer_max_subdiv_level; /* steerable sampler: above steer_subdiv_level, an adaptive triangulation
+                                        between the two levels (the reference's BuildParameters min / max
+                                        subdivision level, src/em_steerable_sampler.hxx:26-98; its defaults are
+                                        4 and 9); 0 or equal: one uniform level */
+    float steer_max_approx_error;    /* adaptive triangulation: a triangle is subdivided where its linear
+                                        approximation misses the map's luminance by more than the factor
+                                        1 + this (the reference's default 5) */
     uint32_t reserved;
 } pg3gpu_options;
 /* With a splitting budget above 1, indirect clipping, or a light-to-BSDF ratio that gives more
  * than one light sample per vertex, algorithm 7 runs the reference's recursive estimator with
  * its tree of sub-paths (src/path_tracer.hxx:167-454) on the megakernel; batches and the
  * differentiable entry points reject these options. */
+
+/* Adaptive steerable triangulations (steer_max_subdiv_level > steer_subdiv_level, at most 12 and
+ * 2^22 leaves) are built on the host at pg3gpu_create from the map with the reference's refinement
+ * rule (TriangulateEm, src/em_steerable_sampler.hxx:2963-3472): every triangle is subdivided down to
+ * the minimum level and, between the levels, wherever the linear interpolation of its vertices'
+ * luminance differs from the map's by more than the factor 1 + steer_max_approx_error at one of its
+ * test samples. Leaves then sit at several levels; the sampler stays exact (its pdf is located
+ * through a quadtree per icosahedron face). The triangulation is kept when pg3gpu_set_params changes
+ * the map (only the weights follow the map). pg3gpu_load_steerable reads the reference's adaptive
+ * files, replacing the context's triangulation by the file's. */
 
 /* Vertex luminance of the steerable sampler's piecewise-linear approximation: the map's value in
  * the vertex direction, as the reference builds it (src/em_steerable_sampler.hxx:3084-3095), or
@@ -310,6 +327,17 @@ int pg3gpu_probe_light_pdf(pg3gpu_ctx *ctx, int32_t light, uint32_t n, const flo
  * max xyz + 0, right box min xyz + child id bits, right box max xyz + 0; child ids >= 0
  * are nodes, < 0 are ~primitive). */
 int pg3gpu_export_bvh(pg3gpu_ctx *ctx, uint32_t *num_prims, uint32_t *codes, uint32_t *ids, float *nodes);
+
+/* Adaptive steerable triangulation of a map (test entry point; needs no GPU): the leaves the
+ * reference's refinement rule (TriangulateEm, src/em_steerable_sampler.hxx:2963-3472) produces for
+ * an RGB float map (width*height*3, row 0 at theta = 0) between min_level and max_level with the
+ * maximum approximation error max_error -- the triangulation pg3gpu_create builds for
+ * steer_max_subdiv_level > steer_subdiv_level. *num_leaves receives the leaf count; for non-NULL
+ * arrays of that many entries, levels[i] the leaf's subdivision level and corners[9 i ..] its three
+ * unit corner directions. */
+int pg3gpu_steer_triangulate(const float *rgb, uint32_t width, uint32_t height, uint32_t min_level,
+                             uint32_t max_level, float max_error, uint32_t *num_leaves, uint32_t *levels,
+                             float *corners);
 
 /* Allocation-free rendering. No counterpart in the reference.
  * For callers that may not allocate device memory once they are running: a plugin

@@ -28,6 +28,7 @@ def build_all(with_ref=True):
         sys.path.insert(0, HERE)
         import build_ref
         build_ref.build()
+        build_ref.build_gpu_shim()
 
 
 if __name__ == "__main__":

@@ -183,6 +183,31 @@ def _wait(entry):
         raise RuntimeError("oracle/_ref: compiling %s failed" % name)
 
 
+GPU_SHIM = os.path.join(OUT, "pg3render_gpu")
+
+
+def build_gpu_shim(force=False):
+    """The reference's command line and render loop with the GPU renderer
+    (pg3render_gb300/shim/pg3render_gpu.cpp + gpu_path_tracer.hxx), compiled against the patched
+    reference headers and linked to the CUDA library -> oracle/_ref/pg3render_gpu. Needs the
+    library built (pg3render_gb300/build.py) and the patched sources in oracle/_ref/src."""
+    root = os.path.dirname(HERE)
+    shim = os.path.join(root, "pg3render_gb300", "shim")
+    libdir = os.path.join(root, "pg3render_gb300", "_build")
+    lib = os.path.join(libdir, "libpg3gpu.so")
+    srcs = [os.path.join(shim, "pg3render_gpu.cpp"), os.path.join(shim, "gpu_path_tracer.hxx"),
+            os.path.join(root, "include", "pg3gpu.h"), lib]
+    if not (os.path.isdir(SRC) and os.path.exists(lib)):
+        return None
+    if not force and os.path.exists(GPU_SHIM) and os.path.getmtime(GPU_SHIM) >= max(os.path.getmtime(f) for f in srcs):
+        return GPU_SHIM
+    cmd = (["g++"] + CXXFLAGS + ["-I" + SRC, "-I" + STUBS, "-I" + shim, "-I" + os.path.join(root, "include"),
+           os.path.join(shim, "pg3render_gpu.cpp"), os.path.join(SRC, "debugging.cxx"),
+           "-L" + libdir, "-lpg3gpu", "-Wl,-rpath," + libdir, "-o", GPU_SHIM])
+    _wait(("pg3render_gpu", subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    return GPU_SHIM
+
+
 def build(ref_root=None, jobs=3, variants=None):
     ref_root = ref_root or default_ref_root()
     os.makedirs(OUT, exist_ok=True)

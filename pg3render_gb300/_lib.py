@@ -75,7 +75,8 @@ class Options(ctypes.Structure):
                 ("steer_subdiv_level", ctypes.c_uint32), ("seed", ctypes.c_uint64),
                 ("max_paths_in_flight", ctypes.c_uint32), ("ggx_sampler", ctypes.c_int32),
                 ("splitting_level", ctypes.c_float), ("light_to_bsdf_ratio", ctypes.c_float),
-                ("steer_weights", ctypes.c_int32), ("reserved", ctypes.c_uint32)]
+                ("steer_weights", ctypes.c_int32), ("steer_max_subdiv_level", ctypes.c_uint32),
+                ("steer_max_approx_error", ctypes.c_float), ("reserved", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -125,6 +126,9 @@ SIGNATURES = {
                                           ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
     "pg3gpu_probe_light_pdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32] + [ctypes.c_void_p] * 4),
     "pg3gpu_export_bvh": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)] + [ctypes.c_void_p] * 3),
+    "pg3gpu_steer_triangulate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                                ctypes.c_uint32, ctypes.c_float, ctypes.POINTER(ctypes.c_uint32),
+                                                ctypes.c_void_p, ctypes.c_void_p]),
     "pg3gpu_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]),
     "pg3gpu_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pg3gpu_diff_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]),

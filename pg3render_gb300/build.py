@@ -48,7 +48,9 @@ def build(force=False, verbose=False, extra_flags=(), out_dir=None):
         obj = os.path.join(bdir, src + ".o")
         cmd = [nvcc] + ARCH + NVCC_FLAGS + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
-            cmd = [nvcc] + NVCC_FLAGS + ["-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
+            # host code without floating-point contraction: the same results on x86 and Arm hosts
+            cmd = [nvcc] + NVCC_FLAGS + ["-Xcompiler", "-ffp-contract=off", "-x", "c++", "-c",
+                                         os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr[-8000:]))

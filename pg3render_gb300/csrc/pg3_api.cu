@@ -192,6 +192,126 @@ int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passe
     return PG3GPU_OK;
 }
 
+// Calls of at most this many paths in one launch chunk replay a captured render graph: their
+// ~90 stage launches cost more than their kernels' work (a 512x512 call of one sample per pixel,
+// the reference's RunIteration pattern, is launch bound).
+#ifndef PG3_CALL_GRAPH_MAX_PATHS
+#define PG3_CALL_GRAPH_MAX_PATHS (1u << 22)
+#endif
+
+bool callGraphEligible(pg3gpu_ctx *ctx, int algorithm, uint32_t spp)
+{
+    const uint64_t paths = (uint64_t)ctx->W * ctx->H * spp;
+    if (PG3_CALL_GRAPH_MAX_PATHS == 0 || paths > PG3_CALL_GRAPH_MAX_PATHS) return false;
+    if (algorithm != PG3GPU_ALG_PATH_TRACING || !ctx->useWavefront || ctx->view.treeMode) return false;
+    // roulette-only paths end when the host sees an empty queue: not a fixed launch sequence
+    if (ctx->view.maxPL == 0 || passesPerChunk(ctx, spp) != spp) return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
+    return true;
+}
+
+void dropCallGraph(pg3gpu_ctx *ctx)
+{
+    if (ctx->callGraphExec) cudaGraphExecDestroy(ctx->callGraphExec);
+    if (ctx->callGraph) cudaGraphDestroy(ctx->callGraph);
+    ctx->callGraphExec = nullptr;
+    ctx->callGraph = nullptr;
+    ctx->callGraphHead = nullptr;
+    ctx->callGraphPasses = 0;
+}
+
+// Captures one launch chunk of `passes` samples per pixel (sample indices from the word
+// dCallBase on) and its accumulation into the framebuffer.
+int captureCallGraph(pg3gpu_ctx *ctx, uint32_t passes)
+{
+    dropCallGraph(ctx);
+    const uint32_t npix = ctx->W * ctx->H;
+    const uint64_t paths = (uint64_t)passes * npix;
+    if (int st = ensureOutput(ctx, paths)) return st;
+    if (int st = ensureWave(ctx, paths)) return st;
+    if (!ctx->dCallBase) {
+        if (int st = devAlloc(ctx, &ctx->dCallBase, 1)) return st;
+    }
+    if (!ctx->graphStream) PG3_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->graphStream, cudaStreamNonBlocking));
+    // the capture stream must not run ahead of work already queued on the context's stream
+    PG3_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    PG3_CUDA(ctx, cudaStreamBeginCapture(ctx->graphStream, cudaStreamCaptureModeThreadLocal));
+    uint64_t launches = 0;
+    cudaError_t e = launchSetWord(ctx->dCallBase, 0u, ctx->graphStream);
+    if (e == cudaSuccess)
+        e = launchWavefront(ctx->view, ctx->kindMask, 0u, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
+                            ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->graphStream, &launches,
+                            nullptr, ctx->dCallBase);
+    if (e == cudaSuccess)
+        e = launchAccumulate(npix, passes, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2], ctx->dSum, ctx->dSumsq,
+                             ctx->graphStream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(ctx->graphStream, &g);
+    if (e == cudaSuccess) e = ee;
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(ctx, PG3GPU_ERR_CUDA, "render graph capture: %s", cudaGetErrorString(e));
+    }
+    cudaGraphNode_t roots[2];
+    size_t nroots = 2;
+    e = cudaGraphGetRootNodes(g, roots, &nroots);
+    if (e == cudaSuccess && nroots != 1) e = cudaErrorInvalidValue;
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(ctx, PG3GPU_ERR_CUDA, "render graph: %s", cudaGetErrorString(e));
+    }
+    ctx->callGraph = g;
+    ctx->callGraphExec = exec;
+    ctx->callGraphHead = roots[0];
+    ctx->callGraphPasses = passes;
+    ctx->callGraphLaunches = launches + 2;   // + the head node and the accumulation
+    std::memcpy(&ctx->callGraphView, &ctx->view, sizeof(SceneView));   // bytes, as runCallGraph compares them
+    const void *bufs[6] = {ctx->dOut[0], ctx->dOut[1], ctx->dOut[2], ctx->dWave, ctx->dSum, ctx->dStats};
+    std::memcpy(ctx->callGraphBufs, bufs, sizeof bufs);
+    return PG3GPU_OK;
+}
+
+// One call through the render graph (captured on first use, and again when the passes, the
+// scene view or a buffer changed).
+int runCallGraph(pg3gpu_ctx *ctx, uint32_t iteration, uint32_t spp)
+{
+    const void *bufs[6] = {ctx->dOut[0], ctx->dOut[1], ctx->dOut[2], ctx->dWave, ctx->dSum, ctx->dStats};
+    if (!ctx->callGraphExec || ctx->callGraphPasses != spp ||
+        std::memcmp(&ctx->callGraphView, &ctx->view, sizeof(SceneView)) != 0 ||
+        std::memcmp(ctx->callGraphBufs, bufs, sizeof bufs) != 0) {
+        if (int st = captureCallGraph(ctx, spp)) return st;
+    }
+    cudaKernelNodeParams p = {};
+    uint32_t *dst = ctx->dCallBase;
+    uint32_t value = iteration;
+    void *args[2] = {&dst, &value};
+    p.func = const_cast<void *>(setWordKernelFunction());
+    p.gridDim = dim3(1);
+    p.blockDim = dim3(1);
+    p.sharedMemBytes = 0;
+    p.kernelParams = args;
+    p.extra = nullptr;
+    PG3_CUDA(ctx, cudaGraphExecKernelNodeSetParams(ctx->callGraphExec, ctx->callGraphHead, &p));
+    if (ctx->pendingTimers == pg3gpu_ctx::kTimerSlots) {
+        cudaStreamSynchronize(ctx->stream);
+        foldTimers(ctx);
+    }
+    const int slot = ctx->pendingTimers++;   // the path-kernel timer spans the whole replay
+    PG3_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    PG3_CUDA(ctx, cudaEventRecord(ctx->tStart[slot], ctx->stream));
+    PG3_CUDA(ctx, cudaGraphLaunch(ctx->callGraphExec, ctx->stream));
+    PG3_CUDA(ctx, cudaEventRecord(ctx->tStop[slot], ctx->stream));
+    PG3_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->timed = true;
+    ctx->iterations += spp;
+    ctx->kernelLaunches += 1;
+    ctx->allLaunches += ctx->callGraphLaunches;
+    return PG3GPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -213,6 +333,8 @@ void pg3gpu_default_options(pg3gpu_options *o)
     o->pipeline = PG3GPU_PIPELINE_AUTO;
     o->steer_subdiv_level = 3;
     o->steer_weights = PG3GPU_STEER_WEIGHTS_PROJECTED;
+    o->steer_max_subdiv_level = 0;
+    o->steer_max_approx_error = 5.f;
     o->seed = 1234;
 }
 
@@ -238,6 +360,10 @@ int pg3gpu_destroy(pg3gpu_ctx *ctx)
     if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->graphStream) cudaStreamSynchronize(ctx->graphStream);
+    if (ctx->callGraphExec) cudaGraphExecDestroy(ctx->callGraphExec);
+    if (ctx->callGraph) cudaGraphDestroy(ctx->callGraph);
+    if (ctx->graphStream) cudaStreamDestroy(ctx->graphStream);
     for (void *p : ctx->allocs) cudaFree(p);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -250,6 +376,95 @@ int pg3gpu_destroy(pg3gpu_ctx *ctx)
 }
 
 }  // extern "C"
+
+int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const float *vwHost)
+{
+    if (!gp) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "steerable tables: no geometry");
+    const SteerGeom &g = *gp;
+    const uint32_t nLeaf = g.numLeaves();
+    const bool uniformOk = !g.adaptive && nLeaf == (20ull << (2 * g.level)) && g.leafGrid == (4u << g.level) &&
+                           g.leafCells.size() == 6ull * g.leafGrid * g.leafGrid;
+    const bool adaptiveOk = g.adaptive && g.qtree.size() >= 5 && g.leafGrid == 0;
+    if ((!uniformOk && !adaptiveOk) || g.leafTri.size() != nLeaf || g.leafPlane.size() != nLeaf ||
+        g.leafEdge.size() != 3ull * nLeaf || g.leafArea.size() != nLeaf || g.layerStart.size() < 2 ||
+        g.layerStart.size() > kSteerMaxLayers + 1 || g.tri.size() < 20 || g.levelOffset.size() < 2)
+        return fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: unexpected leaf count, grid or tree depth");
+    // the previous tables of this context (an adaptive file replaces the triangulation)
+    for (void *p : ctx->steerAllocs) ctxFree(ctx, p);
+    ctx->steerAllocs.clear();
+    const size_t mark = ctx->allocs.size();
+    auto keep = [&](int st) {
+        ctx->steerAllocs.insert(ctx->steerAllocs.end(), ctx->allocs.begin() + (std::ptrdiff_t)mark, ctx->allocs.end());
+        return st;
+    };
+    SceneView &v = ctx->view;
+    SteerView sv{};
+    int st;
+    if ((st = upload(ctx, (float4 **)&sv.vdir, g.vdir))) return keep(st);
+    if ((st = upload(ctx, (int4 **)&sv.tri, g.tri))) return keep(st);
+    if ((st = upload(ctx, (int **)&sv.nodeChild, g.nodeChild))) return keep(st);
+    // leaf planes, then (pg3_steer.cuh) edge normals, leaf-locator cells, whole-sphere weights
+    std::vector<float4> aux = g.leafPlane;
+    aux.insert(aux.end(), g.leafEdge.begin(), g.leafEdge.end());
+    for (const uint4 &c : g.leafCells) {
+        float4 f;
+        std::memcpy(&f, &c, sizeof f);
+        aux.push_back(f);
+    }
+    const size_t rootAt = aux.size();
+    aux.resize(rootAt + 3, make_float4(0.f, 0.f, 0.f, 0.f));
+    if ((st = upload(ctx, (float4 **)&sv.leafPlane, aux))) return keep(st);
+    if ((st = upload(ctx, (int4 **)&sv.leafTri, g.leafTri))) return keep(st);
+    if ((st = upload(ctx, (int4 **)&sv.faceCells, g.faceCells))) return keep(st);
+    if (g.adaptive && (st = upload(ctx, (int4 **)&sv.qtree, g.qtree))) return keep(st);
+    float *rootW = reinterpret_cast<float *>(const_cast<float4 *>(sv.leafPlane) + rootAt);
+    sv.numLeaves = nLeaf;
+    sv.leafGrid = g.leafGrid;
+    sv.level = g.level;
+    for (uint32_t l = 0; !g.adaptive && l + 1 < g.levelOffset.size(); ++l)
+        if (g.levelOffset[l] != 20u * (((1u << (2 * l)) - 1u) / 3u))
+            return fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: unexpected level layout");
+    sv.root = g.root;
+    SteerWeightArgs &a = ctx->steerArgs;
+    a = SteerWeightArgs{};
+    a.em = v.em;
+    a.emW = v.emW;
+    a.emH = v.emH;
+    a.vdir = sv.vdir;
+    a.numVertices = (uint32_t)g.vdir.size();
+    a.leafTri = sv.leafTri;
+    a.numLeaves = nLeaf;
+    if ((st = upload(ctx, (float **)&a.leafArea, g.leafArea))) return keep(st);
+    a.nodeChild = sv.nodeChild;
+    a.numLayers = (uint32_t)g.layerStart.size() - 1;
+    for (uint32_t l = 0; l <= a.numLayers; ++l) a.layerStart[l] = g.layerStart[l];
+    if ((st = devAlloc(ctx, &a.vw, 12 * (size_t)a.numVertices))) return keep(st);
+    a.projected = (ctx->opts.steer_weights == PG3GPU_STEER_WEIGHTS_PROJECTED) ? 1 : 0;
+    unsigned char *proj = nullptr;
+    if (a.projected && (st = devAlloc(ctx, &proj, projScratchBytes(a.numVertices)))) return keep(st);
+    a.projScratch = proj;
+    if ((st = devAlloc(ctx, &a.leafW, 9 * (size_t)nLeaf))) return keep(st);
+    if ((st = devAlloc(ctx, &a.nodeW, 72 * (size_t)g.numNodes()))) return keep(st);
+    a.rootW = rootW;
+    sv.vw = a.vw;
+    sv.nodeW = a.nodeW;
+    a.locator = sv;      // geometry and locator tables (vw / nodeW are outputs of this build)
+    keep(PG3GPU_OK);
+    cudaError_t e;
+    if (vwHost) {
+        e = cudaMemcpy(a.vw, vwHost, 12 * sizeof(float) * (size_t)a.numVertices, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launchSteerTreeWeights(a, nullptr);
+    } else
+        e = launchSteerWeights(a, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "steerable build: %s", cudaGetErrorString(e));
+    v.steer = sv;
+    v.bgShL = a.rootW;   // the background's picking estimate: the sampler's whole integral
+    v.emSampler = g.adaptive ? kEmSteerableAdaptive : kEmSteerable;
+    ctx->steerGeom = gp;
+    ctx->hasSteer = true;
+    return PG3GPU_OK;
+}
 
 // forBatch: a scene instance of a batch (pg3_batch.cu) -- no launch queues, outputs or timers
 int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, bool forBatch,
@@ -300,57 +515,8 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
     if ((st = upload(ctx, (float **)&v.emCond, hs.emCond))) return bail(st);
     if ((st = upload(ctx, (float **)&v.bgShL, hs.bgShL))) return bail(st);
     if (hs.hasSteer) {
-        // geometry from the shared host build; the map-dependent weights are built on the device
-        const SteerGeom &g = *hs.steer;
-        SteerView &sv = v.steer;
-        if ((st = upload(ctx, (float4 **)&sv.vdir, g.vdir))) return bail(st);
-        if ((st = upload(ctx, (int4 **)&sv.tri, g.tri))) return bail(st);
-        if ((st = upload(ctx, (int **)&sv.nodeChild, g.nodeChild))) return bail(st);
-        // leaf planes, then (pg3_steer.cuh) edge normals, leaf-locator cells, whole-sphere weights
-        std::vector<float4> aux = g.leafPlane;
-        aux.insert(aux.end(), g.leafEdge.begin(), g.leafEdge.end());
-        for (const uint4 &c : g.leafCells) {
-            float4 f;
-            std::memcpy(&f, &c, sizeof f);
-            aux.push_back(f);
-        }
-        const size_t rootAt = aux.size();
-        aux.resize(rootAt + 3, make_float4(0.f, 0.f, 0.f, 0.f));
-        if (g.leafPlane.size() != (20ull << (2 * g.level)) || g.leafGrid != (4u << g.level) ||
-            g.layerStart.size() < 2 || g.layerStart.size() > kSteerMaxLayers + 1)
-            return bail(fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: unexpected leaf count, grid or tree depth"));
-        if ((st = upload(ctx, (float4 **)&sv.leafPlane, aux))) return bail(st);
-        if ((st = upload(ctx, (int4 **)&sv.faceCells, g.faceCells))) return bail(st);
-        sv.level = g.level;
-        for (size_t l = 0; l < g.levelOffset.size() && l < 8; ++l) sv.levelOff[l] = g.levelOffset[l];
-        sv.root = g.root;
-        SteerWeightArgs &a = ctx->steerArgs;
-        a.em = v.em;
-        a.emW = v.emW;
-        a.emH = v.emH;
-        a.vdir = sv.vdir;
-        a.numVertices = (uint32_t)g.vdir.size();
-        a.leafTri = sv.tri + g.levelOffset[g.level];
-        a.numLeaves = g.numLeaves();
-        if ((st = upload(ctx, (float **)&a.leafArea, g.leafArea))) return bail(st);
-        a.nodeChild = sv.nodeChild;
-        a.numLayers = (uint32_t)g.layerStart.size() - 1;
-        for (uint32_t l = 0; l <= a.numLayers; ++l) a.layerStart[l] = g.layerStart[l];
-        if ((st = devAlloc(ctx, &a.vw, 12 * (size_t)a.numVertices))) return bail(st);
-        a.projected = (ctx->opts.steer_weights == PG3GPU_STEER_WEIGHTS_PROJECTED) ? 1 : 0;
-        unsigned char *proj = nullptr;
-        if (a.projected && (st = devAlloc(ctx, &proj, projScratchBytes(a.numVertices)))) return bail(st);
-        a.projScratch = proj;
-        if ((st = devAlloc(ctx, &a.leafW, 9 * (size_t)a.numLeaves))) return bail(st);
-        if ((st = devAlloc(ctx, &a.nodeW, 72 * (size_t)g.numNodes()))) return bail(st);
-        a.rootW = reinterpret_cast<float *>(const_cast<float4 *>(sv.leafPlane) + rootAt);
-        sv.vw = a.vw;
-        sv.nodeW = a.nodeW;
-        v.bgShL = a.rootW;   // the background's picking estimate: the sampler's whole integral
-        a.locator = sv;      // geometry and locator tables (vw / nodeW are outputs of this build)
-        const cudaError_t e = launchSteerWeights(a, nullptr);
-        if (e != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "steerable build: %s", cudaGetErrorString(e)));
-        ctx->hasSteer = true;
+        // geometry from the host build; the map-dependent weights are built on the device
+        if ((st = uploadSteer(ctx, hs.steer, nullptr))) return bail(st);
     }
     if ((st = devAlloc(ctx, &ctx->dErr, 1))) return bail(st);
     if (cudaMemset(ctx->dErr, 0, sizeof(unsigned int)) != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "memset"));
@@ -424,6 +590,10 @@ int pg3gpu_run_iteration(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration,
         return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "unknown algorithm %d", (int)algorithm);
     if (spp == 0) return PG3GPU_OK;
     cudaSetDevice(ctx->device);
+    if (callGraphEligible(ctx, algorithm, spp)) {
+        if (int st = checkRenderable(ctx, algorithm)) return st;
+        return runCallGraph(ctx, iteration, spp);
+    }
     const uint32_t npix = ctx->W * ctx->H;
     const uint32_t per = passesPerChunk(ctx, spp);
     PG3_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));

@@ -482,6 +482,7 @@ void launchStep(const pg3gpu_batch *b, const StepShape &s, cudaStream_t st, int 
     batchExtend<<<s.grid, s.block, s.smem, st>>>(b->dViews, n, b->B, b->dCtl, b->dStats);
     if (b->emk == kEmCdf) launchShadeBatch<kEmCdf>(b, s, st);
     else if (b->emk == kEmSteerable) launchShadeBatch<kEmSteerable>(b, s, st);
+    else if (b->emk == kEmSteerableAdaptive) launchShadeBatch<kEmSteerableAdaptive>(b, s, st);
     else launchShadeBatch<kEmCosine>(b, s, st);
     batchShadow<<<s.grid, s.block, s.smem, st>>>(b->dViews, b->dInst, n, b->B, b->dCtl, b->dStats);
     batchAdvance<<<1, 1, 0, st>>>(b->B, b->dCtl, b->dErr, b->handle, useGraph);

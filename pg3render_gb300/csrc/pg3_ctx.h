@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -11,6 +12,7 @@
 #include "../../include/pg3gpu.h"
 #include "pg3_kernels.h"
 #include "pg3_scene_view.h"
+#include "pg3_steerable.h"
 
 struct pg3gpu_ctx {
     using SceneView = pg3::SceneView;
@@ -47,6 +49,19 @@ struct pg3gpu_ctx {
     uint64_t kernelLaunches = 0, allLaunches = 0;
     std::string lastError;
 
+    // render graph of small calls (pg3gpu_run_iteration of one launch chunk): the whole chunk --
+    // queues reset, camera rays, every bounce's stage kernels, accumulation -- captured once and
+    // replayed per call with the call's first sample index set in its head node
+    cudaStream_t graphStream = nullptr;
+    cudaGraph_t callGraph = nullptr;
+    cudaGraphExec_t callGraphExec = nullptr;
+    cudaGraphNode_t callGraphHead = nullptr;
+    uint32_t callGraphPasses = 0;
+    uint64_t callGraphLaunches = 0;      // kernel launches one replay makes
+    uint32_t *dCallBase = nullptr;       // device word: the replay's first sample index
+    SceneView callGraphView{};           // the scene view the graph was captured with
+    const void *callGraphBufs[6] = {};   // and its buffers (a change of either re-captures it)
+
     // recursive estimator (splitting / clipping): frame stacks of the megakernel's threads
     TreeFrame *dTree = nullptr;
     uint32_t treeDepth = 0;
@@ -61,6 +76,8 @@ struct pg3gpu_ctx {
     float *dRowInt = nullptr;                       // environment-map CDF build: per-row integrals
     bool hasSteer = false;                          // steerable sampler: its device build inputs/outputs
     pg3::SteerWeightArgs steerArgs{};
+    std::shared_ptr<const pg3::SteerGeom> steerGeom;   // its geometry (host copy)
+    std::vector<void *> steerAllocs;                // its device tables (replaced by an adaptive file)
     uint32_t diffIteration = 0, diffSpp = 0;        // samples the stored radiance belongs to
     const uint32_t *dSampleOffset = nullptr;        // caller's device word added to sample indices
     bool diffValid = false;
@@ -75,6 +92,10 @@ int ctxError(pg3gpu_ctx *ctx, int status, const std::string &msg);
 // pg3gpu_create; forBatch leaves out the launch queues, per-path outputs and timers.
 int createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, bool forBatch,
                   pg3gpu_ctx **out);
+
+// Uploads a steerable sampler's geometry (replacing any earlier one of the context) and builds its
+// weights on the device: from the context's map, or from vwHost (12 floats per vertex) when given.
+int uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> geom, const float *vwHost);
 
 // Looks up, once per device, the device address of the allocation-free entry point's scratch
 // array (pg3_api.cu); `device` must be current.

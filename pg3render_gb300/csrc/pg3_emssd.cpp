@@ -12,13 +12,14 @@
 //     opening with a uint32 flag (1 triangle node): a set node has a uint32 child count and its
 //     children; a triangle node its uint32 subdivision level and 3 uint32 vertex indices.
 //
-// This library's sampler uses one uniform subdivision level (minimum = maximum level of the
-// reference's build), so it writes that triangulation (its shared vertices, its 6-ary tree) and
-// reads files whose leaf triangles are exactly those of its own level, in any vertex numbering or
-// tree order (the reference stores a vertex once per triangle that creates it). A file of an
-// adaptive triangulation (leaves at several levels) is refused with PG3GPU_ERR_UNSUPPORTED.
-// Reading replaces the context's vertex weights and rebuilds the leaf, node and whole-sphere
-// weights on the device; a later change of the map (pg3gpu_set_params) recomputes them from it.
+// Writing stores the context's triangulation (uniform or adaptive: each leaf with its level, the
+// vertices shared, its 6-ary tree) with its build parameters. Reading accepts any file whose leaves
+// are triangles of the icosahedron's 4-way subdivision covering the sphere, in any vertex numbering
+// or tree order (the reference stores a vertex once per triangle that creates it): a file with
+// exactly the context's uniform level replaces only the vertex weights; any other file (an
+// adaptive triangulation, the reference's default build, or another level) replaces the context's
+// triangulation with the file's. Either way the leaf, node and whole-sphere weights are rebuilt on
+// the device; a later change of the map (pg3gpu_set_params) recomputes the weights from it.
 #include <algorithm>
 #include <array>
 #include <climits>
@@ -89,20 +90,20 @@ int ctxFail(pg3gpu_ctx *ctx, int status, const std::string &msg) { return ctxErr
 
 const SteerGeom *contextGeometry(pg3gpu_ctx *ctx, std::string &err)
 {
-    if (!ctx->hasSteer) {
+    if (!ctx->hasSteer || !ctx->steerGeom) {
         err = "the context has no steerable sampler (environment map with em_sampler PG3GPU_EM_STEERABLE)";
         return nullptr;
     }
-    return steerGeometry(ctx->view.steer.level, err);
+    return ctx->steerGeom.get();
 }
 
 // Depth-first writer of the 6-ary tree (nodeChild: >= 0 node, < 0 ~leaf, INT_MIN none).
 void writeNode(Writer &w, const SteerGeom &g, int item, bool isLeaf)
 {
     if (isLeaf) {
-        const int4 t = g.tri[g.levelOffset[g.level] + (uint32_t)item];
+        const int4 t = g.leafTri[(uint32_t)item];
         w.u32(1u);
-        w.u32(g.level);
+        w.u32((uint32_t)t.w);   // the leaf's subdivision level
         w.u32((uint32_t)t.x);
         w.u32((uint32_t)t.y);
         w.u32((uint32_t)t.z);
@@ -210,9 +211,9 @@ int pg3gpu_save_steerable(pg3gpu_ctx *ctx, const char *path, float max_approx_er
         return ctxFail(ctx, PG3GPU_ERR_CUDA, "save_steerable: reading the vertex weights failed");
     Writer w;
     w.bytes(kHeader, sizeof kHeader);   // with the terminating zero
-    w.f32(max_approx_error);
-    w.u32(g.level);                     // minimum = maximum subdivision level
-    w.u32(g.level);
+    w.f32(g.adaptive ? g.maxApproxError : max_approx_error);
+    w.u32(g.minLevel);                  // uniform: minimum = maximum subdivision level
+    w.u32(g.maxLevel);
     w.u32(50u);                         // the reference's defaults of its debugging parameters
     w.f32(1.1f);                        // (BuildParameters, src/em_steerable_sampler.hxx:30-57)
     w.f32(0.7f);
@@ -251,7 +252,7 @@ int pg3gpu_load_steerable(pg3gpu_ctx *ctx, const char *path)
         return bad("not a steerable sampler data file of format 2.1");
     Reader r(b);
     r.o = sizeof kHeader;
-    r.f32();                                   // max approximation error: no role for one level
+    const float fileError = r.f32();
     const uint32_t minLevel = r.u32(), maxLevel = r.u32();
     r.u32();
     r.f32();
@@ -273,38 +274,48 @@ int pg3gpu_load_steerable(pg3gpu_ctx *ctx, const char *path)
     if (!readNode(r, nv, leaves, sets, 0)) return bad("malformed tree");
     if (sets != nSets || leaves.size() != nTris) return bad("tree node counts disagree with the header");
     if (r.o != b.size()) return bad("trailing bytes after the tree");
-    bool oneLevel = minLevel == maxLevel;
-    for (const FileLeaf &l : leaves) oneLevel = oneLevel && l.level == g.level;
-    if (!oneLevel || leaves.size() != g.numLeaves())
-        return ctxFail(ctx, PG3GPU_ERR_UNSUPPORTED,
-                       "load_steerable: the file's triangulation (subdivision levels " + std::to_string(minLevel) + "-" +
-                           std::to_string(maxLevel) + ", " + std::to_string(leaves.size()) +
-                           " leaves) is not the uniform level " + std::to_string(g.level) + " of this context");
-    // file vertices -> ours; every leaf of the file must be one of ours, each exactly once
-    const std::vector<int> map = matchVertices(g, dirs);
-    std::map<std::array<int, 3>, uint32_t> ours;
-    const uint32_t off = g.levelOffset[g.level];
-    for (uint32_t t = 0; t < g.numLeaves(); ++t) {
-        const int4 v = g.tri[off + t];
-        std::array<int, 3> k = {v.x, v.y, v.z};
-        std::sort(k.begin(), k.end());
-        ours[k] = t;
-    }
-    std::vector<char> seen(g.numLeaves(), 0);
-    for (const FileLeaf &l : leaves) {
-        std::array<int, 3> k;
-        for (int j = 0; j < 3; ++j) {
-            k[j] = map[l.v[j]];
-            if (k[j] < 0) return bad("a vertex direction is not one of the level's vertices");
+    bool sameLevel = !g.adaptive && leaves.size() == g.numLeaves();
+    for (const FileLeaf &l : leaves) sameLevel = sameLevel && l.level == g.level;
+    std::shared_ptr<SteerGeom> fileGeom;   // the file's own triangulation, when it is not the context's
+    if (sameLevel) {
+        // file vertices -> ours; every leaf of the file must be one of ours, each exactly once
+        const std::vector<int> map = matchVertices(g, dirs);
+        std::map<std::array<int, 3>, uint32_t> ours;
+        for (uint32_t t = 0; t < g.numLeaves(); ++t) {
+            const int4 v = g.leafTri[t];
+            std::array<int, 3> k = {v.x, v.y, v.z};
+            std::sort(k.begin(), k.end());
+            ours[k] = t;
         }
-        std::sort(k.begin(), k.end());
-        auto it = ours.find(k);
-        if (it == ours.end() || seen[it->second]) return bad("a leaf triangle is not one of the level's triangles");
-        seen[it->second] = 1;
+        std::vector<char> seen(g.numLeaves(), 0);
+        for (const FileLeaf &l : leaves) {
+            std::array<int, 3> k;
+            for (int j = 0; j < 3; ++j) {
+                k[j] = map[l.v[j]];
+                if (k[j] < 0) return bad("a vertex direction is not one of the level's vertices");
+            }
+            std::sort(k.begin(), k.end());
+            auto it = ours.find(k);
+            if (it == ours.end() || seen[it->second]) return bad("a leaf triangle is not one of the level's triangles");
+            seen[it->second] = 1;
+        }
+    } else {
+        std::vector<std::array<float, 9>> corners(leaves.size());
+        std::vector<uint32_t> levels(leaves.size());
+        for (size_t i = 0; i < leaves.size(); ++i) {
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) corners[i][3 * j + k] = dirs[3 * (size_t)leaves[i].v[j] + k];
+            levels[i] = leaves[i].level;
+        }
+        std::string gerr;
+        fileGeom = steerGeometryFromLeaves(corners, levels, minLevel, maxLevel, fileError, gerr);
+        if (!fileGeom) return bad(gerr);
     }
+    const SteerGeom &tg = fileGeom ? *fileGeom : g;   // the triangulation the weights belong to
+    const std::vector<int> map = matchVertices(tg, dirs);
     // weights of our vertices from the file's (a vertex stored several times carries one value)
-    std::vector<float> vw(12 * g.vdir.size(), 0.f);
-    std::vector<char> have(g.vdir.size(), 0);
+    std::vector<float> vw(12 * tg.vdir.size(), 0.f);
+    std::vector<char> have(tg.vdir.size(), 0);
     for (uint32_t i = 0; i < nv; ++i) {
         const int v = map[i];
         if (v < 0) continue;
@@ -319,6 +330,12 @@ int pg3gpu_load_steerable(pg3gpu_ctx *ctx, const char *path)
     }
     for (size_t v = 0; v < have.size(); ++v)
         if (!have[v]) return bad("a vertex of the triangulation has no weight in the file");
+    if (fileGeom) {
+        cudaSetDevice(ctx->device);
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+            return ctxFail(ctx, PG3GPU_ERR_CUDA, "load_steerable: synchronising the context's stream failed");
+        return uploadSteer(ctx, fileGeom, vw.data());
+    }
     const SteerWeightArgs &a = ctx->steerArgs;
     cudaSetDevice(ctx->device);
     if (cudaMemcpyAsync(a.vw, vw.data(), vw.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
@@ -326,4 +343,28 @@ int pg3gpu_load_steerable(pg3gpu_ctx *ctx, const char *path)
     const cudaError_t e = launchSteerTreeWeights(a, ctx->stream);
     if (e == cudaSuccess && cudaStreamSynchronize(ctx->stream) == cudaSuccess) return PG3GPU_OK;
     return ctxFail(ctx, PG3GPU_ERR_CUDA, std::string("load_steerable: rebuilding the tree weights: ") + cudaGetErrorString(e));
+}
+
+int pg3gpu_steer_triangulate(const float *rgb, uint32_t width, uint32_t height, uint32_t min_level,
+                             uint32_t max_level, float max_error, uint32_t *num_leaves, uint32_t *levels,
+                             float *corners)
+{
+    if (!rgb || !num_leaves) return PG3GPU_ERR_INVALID_ARGUMENT;
+    std::string err;
+    const std::shared_ptr<SteerGeom> g = steerAdaptiveGeometry(rgb, width, height, min_level, max_level, max_error, err);
+    if (!g) return ctxError(nullptr, PG3GPU_ERR_INVALID_ARGUMENT, "steer_triangulate: " + err);
+    *num_leaves = g->numLeaves();
+    for (uint32_t i = 0; i < g->numLeaves(); ++i) {
+        const int4 t = g->leafTri[i];
+        if (levels) levels[i] = (uint32_t)t.w;
+        if (corners) {
+            const int v[3] = {t.x, t.y, t.z};
+            for (int j = 0; j < 3; ++j) {
+                corners[9 * (size_t)i + 3 * j] = g->vdir[(size_t)v[j]].x;
+                corners[9 * (size_t)i + 3 * j + 1] = g->vdir[(size_t)v[j]].y;
+                corners[9 * (size_t)i + 3 * j + 2] = g->vdir[(size_t)v[j]].z;
+            }
+        }
+    }
+    return PG3GPU_OK;
 }

@@ -122,8 +122,10 @@ PG3_DI float3 bgEmission(const SceneView &S, float3 dir, bool wantPdf, const Fra
     if (S.bgKind == kBgEnvMap) {
         const float3 L = emEvaluateDir(S, dir);
         if (wantPdf)
-            pdf = (em == kEmCdf) ? emCdfPdf(S, dir)
-                  : (em == kEmSteerable) ? steerPdf(S.steer, dir, pf.z) : cosSpherePdfFront(toLocal(pf, dir));
+            pdf = (em == kEmCdf)                 ? emCdfPdf(S, dir)
+                  : (em == kEmSteerable)         ? steerPdf<false>(S.steer, dir, pf.z)
+                  : (em == kEmSteerableAdaptive) ? steerPdf<true>(S.steer, dir, pf.z)
+                                                 : cosSpherePdfFront(toLocal(pf, dir));
         return L;
     }
     if (wantPdf) pdf = cosSpherePdfFront(toLocal(pf, dir));
@@ -140,7 +142,11 @@ PG3_DI void bgSample(const SceneView &S, const Frame &f, float u0, float u1, flo
         return;
     }
     if (S.bgKind == kBgEnvMap && em == kEmSteerable) {
-        steerSample(S, f.z, u0, u1, u2, wig, pdfW, radCos);
+        steerSample<false>(S, f.z, u0, u1, u2, wig, pdfW, radCos);
+        return;
+    }
+    if (S.bgKind == kBgEnvMap && em == kEmSteerableAdaptive) {
+        steerSample<true>(S, f.z, u0, u1, u2, wig, pdfW, radCos);
         return;
     }
     const float3 wil = sampleCosHemisphere(u0, u1, pdfW);   // cosine sampler, front side only

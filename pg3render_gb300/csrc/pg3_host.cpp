@@ -139,6 +139,12 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown environment-map sampler");
     if (o.steer_weights != PG3GPU_STEER_WEIGHTS_POINT && o.steer_weights != PG3GPU_STEER_WEIGHTS_PROJECTED)
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown steerable vertex weights");
+    const bool adaptive = o.steer_max_subdiv_level > o.steer_subdiv_level;
+    if (adaptive && (o.steer_max_subdiv_level > kSteerMaxAdaptiveLevel || !(o.steer_max_approx_error > 0.f) ||
+                     !std::isfinite(o.steer_max_approx_error)))
+        return bad(PG3GPU_ERR_INVALID_ARGUMENT,
+                   "adaptive steerable triangulation: maximum subdivision level must be <= 12 and the maximum "
+                   "approximation error finite and > 0");
     if (sc.num_materials == 0 || !sc.materials) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "scene has no materials");
     if ((sc.num_triangles && !sc.triangles) || (sc.num_spheres && !sc.spheres) ||
         (sc.num_area_lights && !sc.area_lights) || (sc.num_point_lights && !sc.point_lights))
@@ -340,7 +346,15 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         v.emW = sc.env_width;
         v.emH = sc.env_height;
         if (o.em_sampler == PG3GPU_EM_STEERABLE) {
-            out.steer = steerGeometry(o.steer_subdiv_level, err);
+            if (adaptive) {
+                // the map-dependent triangulation of this context
+                out.steer = steerAdaptiveGeometry(sc.env_map, sc.env_width, sc.env_height, o.steer_subdiv_level,
+                                                  o.steer_max_subdiv_level, o.steer_max_approx_error, err);
+            } else {
+                // the shared geometry of the level (process lifetime; not owned here)
+                const SteerGeom *g = steerGeometry(o.steer_subdiv_level, err);
+                if (g) out.steer = std::shared_ptr<const SteerGeom>(std::shared_ptr<const SteerGeom>(), g);
+            }
             if (!out.steer) return PG3GPU_ERR_INVALID_ARGUMENT;
             out.hasSteer = true;   // the picking estimate is the sampler's own whole integral (device)
         } else {
@@ -349,7 +363,8 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
     } else if (sc.background != PG3GPU_BG_NONE && sc.background != PG3GPU_BG_CONSTANT) {
         return bad(PG3GPU_ERR_INVALID_ARGUMENT, "unknown background kind");
     }
-    v.emSampler = o.em_sampler;
+    v.emSampler = (o.em_sampler == PG3GPU_EM_STEERABLE && out.steer && out.steer->adaptive) ? kEmSteerableAdaptive
+                                                                                             : o.em_sampler;
     v.algorithm = o.algorithm;
     v.splitBudget = (float)o.splitting_budget;
     v.splitLevel = o.splitting_level;

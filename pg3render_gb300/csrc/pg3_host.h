@@ -2,6 +2,7 @@
 // light table and the environment-map sampling tables, in device layout.
 #pragma once
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -25,8 +26,9 @@ struct HostScene {
     std::vector<float4> em;
     std::vector<float> emMarg, emCond;
     std::vector<float> bgShL;            // 9 SH coefficients of the map's luminance (picking estimate)
-    const SteerGeom *steer = nullptr;    // steerable sampler geometry (shared, process lifetime); its
-                                         // weights are built on the device
+    std::shared_ptr<const SteerGeom> steer;   // steerable sampler geometry (uniform levels: the shared,
+                                              // process-lifetime build; adaptive: this scene's); its
+                                              // weights are built on the device
     bool hasSteer = false;
     uint32_t kindMask = 0;               // material kinds present (bit per PG3GPU_MAT_* kind)
     uint32_t numPointLights = 0;

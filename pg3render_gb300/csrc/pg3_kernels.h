@@ -26,6 +26,10 @@ cudaError_t launchMegakernel(const SceneView &S, int algorithm, uint32_t sample0
 cudaError_t megakernelOccupancy(int algorithm, int *blocksPerSm);
 cudaError_t launchAccumulate(uint32_t npix, uint32_t passes, const float *r, const float *g, const float *b,
                              double *sum, double *sumsq, cudaStream_t stream);
+// One thread stores `value` to *dst (the head node of a captured render graph, whose parameter
+// each replay sets to the call's first sample index).
+cudaError_t launchSetWord(uint32_t *dst, uint32_t value, cudaStream_t stream);
+const void *setWordKernelFunction();
 
 // pg3_lbvh.cu
 size_t lbvhScratchBytes(uint32_t numPrims);
@@ -40,7 +44,7 @@ size_t wavefrontBytes(uint64_t capacity, bool grad);
 cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch,
                             uint64_t capacity, int gridBlocks, cudaStream_t stream, uint64_t *launches,
-                            const GradArgs *grad = nullptr);
+                            const GradArgs *grad = nullptr, const uint32_t *sampleOffset = nullptr);
 
 // pg3_steer_build.cu: the steerable sampler's map-dependent tables from the device texels
 constexpr uint32_t kSteerMaxLayers = 16;

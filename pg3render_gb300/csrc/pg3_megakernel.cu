@@ -77,6 +77,16 @@ __global__ void __launch_bounds__(256) accumulateKernel(uint32_t npix, uint32_t 
     }
 }
 
+__global__ void setWordKernel(uint32_t *dst, uint32_t value) { *dst = value; }
+
+cudaError_t launchSetWord(uint32_t *dst, uint32_t value, cudaStream_t stream)
+{
+    setWordKernel<<<1, 1, 0, stream>>>(dst, value);
+    return cudaGetLastError();
+}
+
+const void *setWordKernelFunction() { return reinterpret_cast<const void *>(setWordKernel); }
+
 cudaError_t launchMegakernel(const SceneView &S, int algorithm, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                              float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,
                              cudaStream_t stream, TreeFrame *tree, uint32_t treeDepth)

@@ -17,7 +17,9 @@ enum : int {
     kMatPhong = 3, kMatSmoothConductor = 4, kMatSmoothDielectric = 5, kMatSra = 6, kNumMatKinds = 7
 };
 enum : int { kBgNone = 0, kBgConstant = 1, kBgEnvMap = 2 };
-enum : int { kEmCdf = 0, kEmCosine = 1, kEmSteerable = 2 };
+// kEmSteerableAdaptive: the steerable sampler over an adaptive triangulation (an internal sampler
+// id; the options name it PG3GPU_EM_STEERABLE with a maximum subdivision level above the minimum)
+enum : int { kEmCdf = 0, kEmCosine = 1, kEmSteerable = 2, kEmSteerableAdaptive = 3 };
 
 struct DevMaterial {          // 80 bytes
     int kind;
@@ -59,16 +61,20 @@ struct BvhNode {
 
 // Steerable sampler tables (host build in pg3_steerable.cpp, sampling in pg3_steer.cuh).
 struct SteerView {
-    const float4 *vdir;       // per vertex: unit direction xyz
+    const float4 *vdir;       // per vertex: unit direction xyz (w: the antipodal vertex, uniform levels)
     const float *vw;          // per vertex: 9 SH basis values scaled by the map's luminance (padded to 12)
-    const int4 *tri;          // vertex ids of the triangles of every subdivision level
+    const int4 *tri;          // vertex ids of the triangles of every subdivision level (adaptive: level 0)
     const float *nodeW;       // per 6-ary tree node: 9 coefficients x 8 child slots of summed weights
     const int *nodeChild;     // per node: 8 child slots (>= 0 node, < 0 ~leaf, INT_MIN none)
     const float4 *leafPlane;  // per leaf: unit plane normal, distance from the origin; followed in the
-                              // same allocation by the leaf-locator tables (pg3_steer.cuh)
+                              // same allocation by the leaf-locator tables and the whole-sphere
+                              // weights (pg3_steer.cuh)
     const int4 *faceCells;    // cube-map cells: up to 4 candidate level-0 faces (-1 none)
-    uint32_t level;           // leaf subdivision level
-    uint32_t levelOff[8];     // first entry of each level in `tri` (level <= 7)
+    const int4 *leafTri;      // per leaf: vertex ids (w: subdivision level)
+    const int4 *qtree;        // adaptive: face codes and the subdivided triangles (pg3_steerable.h)
+    uint32_t numLeaves, leafGrid;
+    uint32_t level;           // leaf subdivision level (adaptive: the deepest leaf's); uniform levels keep
+                              // the triangles of every level in `tri`, level l from 20 (4^l - 1) / 3 on
     int root;
 };
 

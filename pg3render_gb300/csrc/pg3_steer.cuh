@@ -11,9 +11,11 @@
 // then p with density proportional to g_T on the planar triangle, then w = p/|p|;
 // its pdf is exactly base(w). Directions below the horizon are mirrored through
 // the origin as in the reference (:2196-2208), so the returned pdf is
-// base(w) + base(-w) for both sampled and evaluated directions. The triangulation is
+// base(w) + base(-w) for both sampled and evaluated directions. A uniform triangulation is
 // centrally symmetric: -w lies in the leaf of the antipodal vertices at the same barycentric
-// coordinates and the same r / d_T, so base(-w) needs only those vertices' values.
+// coordinates and the same r / d_T, so base(-w) needs only those vertices' values. An adaptive
+// triangulation (leaves at several levels, the reference's default build) is not: there -w is
+// located on its own, through the quadtree of its icosahedron face (the ADAPTIVE variants).
 #pragma once
 
 #include <climits>
@@ -23,6 +25,7 @@
 namespace pg3 {
 
 constexpr int kSteerCellsDev = 8;   // must equal kSteerCells of the host build
+constexpr uint32_t kSteerMaxAdaptiveDepth = 12;   // must equal kSteerMaxAdaptiveLevel of the host build
 
 PG3_DI void steerCoeffs(float3 n, float c[9])
 {
@@ -47,10 +50,10 @@ PG3_DI float dot9(const float *__restrict__ w, const float c[9])
 }
 
 // Tables that follow the leaf planes in one allocation (pg3gpu_create): per leaf 3 inward edge
-// normals, the leaf-locator cube map (6 x grid^2 cells of up to 8 16-bit leaf ids), and the
-// 9 weights of the whole sphere. Leaves = 20 * 4^level, grid = 4 * 2^level.
-PG3_DI uint32_t steerLeaves(const SteerView &T) { return 20u << (2 * T.level); }
-PG3_DI uint32_t steerGrid(const SteerView &T) { return 4u << T.level; }
+// normals, the leaf-locator cube map (6 x grid^2 cells of up to 8 16-bit leaf ids; uniform
+// levels only, grid 0 for adaptive triangulations), and the 9 weights of the whole sphere.
+PG3_DI uint32_t steerLeaves(const SteerView &T) { return T.numLeaves; }
+PG3_DI uint32_t steerGrid(const SteerView &T) { return T.leafGrid; }
 PG3_DI const float4 *steerEdges(const SteerView &T) { return T.leafPlane + steerLeaves(T); }
 PG3_DI const uint4 *steerCells(const SteerView &T)
 {
@@ -117,10 +120,9 @@ PG3_DI int cubeCell(int face, float u, float v, int G)
     return (face * G + iv) * G + iu;
 }
 
-// Leaf containing direction w through the hierarchy: a cube-map cell gives at most eight
-// candidate icosahedron faces (all 20 are scanned if none contains w), then one of four
-// children per subdivision level by three great-circle tests.
-PG3_DI int steerLocateFaces(const SteerView &T, float3 w)
+// The icosahedron face containing direction w: a cube-map cell gives at most eight candidate
+// faces (all 20 are scanned if none contains w).
+PG3_DI int steerFace(const SteerView &T, float3 w)
 {
     float fu, fv;
     const int cell = cubeCell(cubeFace(w, fu, fv), fu, fv, kSteerCellsDev);
@@ -138,17 +140,47 @@ PG3_DI int steerLocateFaces(const SteerView &T, float3 w)
             if (m > bestMin) { bestMin = m; best = f; }
         }
     }
-    int local = best;
+    return best;
+}
+
+// Which of the four children of a subdivided triangle (children (A,ab,ca), (ab,B,bc), (ca,bc,C),
+// (ab,bc,ca)) contains w: three great-circle tests against the edge midpoints.
+PG3_DI int steerChild(float3 w, float3 ab, float3 bc, float3 ca)
+{
+    if (dot(w, cross(ab, ca)) >= 0.f) return 0;
+    if (dot(w, cross(bc, ab)) >= 0.f) return 1;
+    if (dot(w, cross(ca, bc)) >= 0.f) return 2;
+    return 3;
+}
+
+// Leaf containing direction w through the uniform hierarchy: its face, then one of four
+// children per subdivision level.
+PG3_DI int steerLocateFaces(const SteerView &T, float3 w)
+{
+    int local = steerFace(T, w);
     for (uint32_t l = 0; l < T.level; ++l) {
-        const int4 mid = __ldg(&T.tri[T.levelOff[l + 1] + 4 * local + 3]);   // (ab, bc, ca)
+        const uint32_t off = 20u * (((1u << (2 * (l + 1))) - 1u) / 3u);   // first triangle of level l+1
+        const int4 mid = __ldg(&T.tri[off + 4 * local + 3]);   // (ab, bc, ca)
         const float3 ab = vdir(T, mid.x), bc = vdir(T, mid.y), ca = vdir(T, mid.z);
-        int child = 3;
-        if (dot(w, cross(ab, ca)) >= 0.f) child = 0;
-        else if (dot(w, cross(bc, ab)) >= 0.f) child = 1;
-        else if (dot(w, cross(ca, bc)) >= 0.f) child = 2;
-        local = 4 * local + child;
+        local = 4 * local + steerChild(w, ab, bc, ca);
     }
     return local;
+}
+
+// Leaf containing direction w in an adaptive triangulation: its face, then the quadtree of the
+// face's subdivided triangles down to a leaf (bounded by the deepest level).
+PG3_DI int steerLocateAdaptive(const SteerView &T, float3 w)
+{
+    const int f = steerFace(T, w);
+    const int4 fc = __ldg(&T.qtree[f >> 2]);
+    int code = (f & 3) == 0 ? fc.x : (f & 3) == 1 ? fc.y : (f & 3) == 2 ? fc.z : fc.w;
+    for (uint32_t depth = 0; depth <= kSteerMaxAdaptiveDepth && code >= 0; ++depth) {
+        const int4 mid = __ldg(&T.qtree[5 + 2 * code]);
+        const int4 ch = __ldg(&T.qtree[5 + 2 * code + 1]);
+        const int c = steerChild(w, vdir(T, mid.x), vdir(T, mid.y), vdir(T, mid.z));
+        code = c == 0 ? ch.x : c == 1 ? ch.y : c == 2 ? ch.z : ch.w;
+    }
+    return code < 0 ? ~code : 0;
 }
 
 // Leaf containing direction w: the leaf-locator cell lists every leaf that can touch it, so
@@ -180,12 +212,34 @@ PG3_DI int steerLocate(const SteerView &T, float3 w)
 
 PG3_DI int antipode(float4 v) { return __float_as_int(v.w); }
 
-// base(w) + base(-w): w's leaf, w's barycentric coordinates there, and the values of the
-// leaf's vertices and of their antipodes.
+// base(w) of one direction: its leaf, the point where w meets the leaf's plane, the linear
+// interpolation of the leaf's vertex values there.
+PG3_DI float steerBasePdf(const SteerView &T, int leaf, float3 w, const float c[9], float Z)
+{
+    const int4 tri = __ldg(&T.leafTri[leaf]);
+    const float4 pl = __ldg(&T.leafPlane[leaf]);
+    const float dw = dot(xyz(pl), w);
+    if (!(dw > 0.f)) return 0.f;
+    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
+    const float3 p = w * (pl.w / dw);
+    const float3 n = cross(B - A, C - A);
+    const float nn = dot(n, n);
+    const float b0 = dot(cross(B - p, C - p), n) / nn;
+    const float b1 = dot(cross(C - p, A - p), n) / nn;
+    const float b2 = 1.f - b0 - b1;
+    const float g = b0 * vval(T, tri.x, c) + b1 * vval(T, tri.y, c) + b2 * vval(T, tri.z, c);
+    return steerLeafPdf(T, leaf, p, g, Z);
+}
+
+// base(w) + base(-w). Uniform levels: w's leaf, w's barycentric coordinates there, and the values
+// of the leaf's vertices and of their antipodes. Adaptive: -w is located in its own leaf.
+template <bool ADAPTIVE>
 PG3_DI float steerPairPdf(const SteerView &T, float3 w, const float c[9], float Z)
 {
+    if (ADAPTIVE)
+        return steerBasePdf(T, steerLocateAdaptive(T, w), w, c, Z) + steerBasePdf(T, steerLocateAdaptive(T, -w), -w, c, Z);
     const int leaf = steerLocate(T, w);
-    const int4 tri = __ldg(&T.tri[T.levelOff[T.level] + leaf]);
+    const int4 tri = __ldg(&T.leafTri[leaf]);
     const float4 pl = __ldg(&T.leafPlane[leaf]);
     const float3 nT = xyz(pl);
     const float dw = dot(nT, w);
@@ -204,6 +258,7 @@ PG3_DI float steerPairPdf(const SteerView &T, float3 w, const float c[9], float 
 }
 
 // Pdf of the mirrored-hemisphere sampler for a direction above the surface (front side).
+template <bool ADAPTIVE = false>
 PG3_DI float steerPdf(const SteerView &T, float3 w, float3 n)
 {
     if (dot(w, n) < 0.f) return 0.f;
@@ -211,10 +266,11 @@ PG3_DI float steerPdf(const SteerView &T, float3 w, float3 n)
     steerCoeffs(n, c);
     const float Z = steerTotal(T, c);
     if (!(Z > 0.f)) return 0.f;
-    return steerPairPdf(T, w, c, Z);
+    return steerPairPdf<ADAPTIVE>(T, w, c, Z);
 }
 
 // Samples a direction in the upper hemisphere of n. Returns false when the map is black.
+template <bool ADAPTIVE = false>
 PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float u2, float3 &wig, float &pdf,
                         float3 &radCos)
 {
@@ -277,7 +333,7 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     // exact sample of the linear density on the planar triangle: pick corner i with
     // probability v_i / sum, then barycentric b_i from its marginal 6b(1-b) (inverse of
     // 3b^2 - 2b^3), the other two uniformly along the remaining segment
-    const int4 tri = __ldg(&T.tri[T.levelOff[T.level] + leaf]);
+    const int4 tri = __ldg(&T.leafTri[leaf]);
     const float4 A4 = __ldg(&T.vdir[tri.x]), B4 = __ldg(&T.vdir[tri.y]), C4 = __ldg(&T.vdir[tri.z]);
     const float v0 = vval(T, tri.x, c), v1 = vval(T, tri.y, c), v2 = vval(T, tri.z, c);
     const float vs = v0 + v1 + v2;
@@ -292,9 +348,15 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     else { b2 = bi; b0 = bj; b1 = bk; }
     const float3 p = xyz(A4) * b0 + xyz(B4) * b1 + xyz(C4) * b2;
     const float3 w0 = normalize(p);
-    // -w0 lies in the antipodal leaf at the same barycentric coordinates
-    const float ga = b0 * vval(T, antipode(A4), c) + b1 * vval(T, antipode(B4), c) + b2 * vval(T, antipode(C4), c);
-    pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) + steerLeafPdf(T, leaf, p, ga, Z);
+    if (ADAPTIVE) {
+        // -w0 lies in a leaf of its own
+        pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) +
+              steerBasePdf(T, steerLocateAdaptive(T, -w0), -w0, c, Z);
+    } else {
+        // -w0 lies in the antipodal leaf at the same barycentric coordinates
+        const float ga = b0 * vval(T, antipode(A4), c) + b1 * vval(T, antipode(B4), c) + b2 * vval(T, antipode(C4), c);
+        pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) + steerLeafPdf(T, leaf, p, ga, Z);
+    }
     float cosIn = dot(w0, n);
     wig = w0;
     if (cosIn < 0.f) { wig = -w0; cosIn = -cosIn; }

@@ -86,9 +86,9 @@ __global__ void projectLumKernel(const float4 *em, uint32_t W, uint32_t H, Steer
     const double maxOmega = (2.0 * 3.14159265358979 / W) * (3.14159265358979 / H);
     const float dOmega = (2.f * kPi / (float)W) * (kPi / (float)H) * st;
     const float lum = texelLumAt(em, i);
-    const int leaf = steerLocate(T, d);
-    if (leaf < 0 || (uint32_t)leaf >= (20u << (2 * T.level))) return;
-    const int4 tri = T.tri[T.levelOff[T.level] + leaf];
+    const int leaf = T.qtree ? steerLocateAdaptive(T, d) : steerLocate(T, d);
+    if (leaf < 0 || (uint32_t)leaf >= T.numLeaves) return;
+    const int4 tri = T.leafTri[leaf];
     const float3 A = xyz(T.vdir[tri.x]), B = xyz(T.vdir[tri.y]), C = xyz(T.vdir[tri.z]);
     const float3 n = cross(B - A, C - A);
     const float nn = dot(n, n);

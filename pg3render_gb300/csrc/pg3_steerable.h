@@ -27,9 +27,18 @@
 // * pdf evaluation locates a direction's leaf through the subdivision hierarchy
 //   (20 faces, then one of 4 children per level) instead of reading the
 //   environment map, so evaluated pdf == sampled pdf.
+//
+// Adaptive triangulations (the reference's default build: subdivision between a minimum and a
+// maximum level wherever the linear approximation of the map's luminance misses the map by more
+// than a relative error, src/em_steerable_sampler.hxx:2963-3472) have leaves at several levels.
+// Their geometry depends on the map, so it is built per context (steerAdaptiveGeometry) or read
+// from a file of the reference (steerGeometryFromLeaves); a quadtree per icosahedron face locates
+// a direction's leaf, and the triangulation is no longer centrally symmetric.
 #pragma once
 
+#include <array>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -38,7 +47,15 @@
 namespace pg3 {
 
 struct SteerGeom {
-    uint32_t level = 0;
+    uint32_t level = 0;                // uniform: the leaves' level; adaptive: the maximum leaf level
+    bool adaptive = false;
+    uint32_t minLevel = 0, maxLevel = 0;   // build parameters (uniform: both = level)
+    float maxApproxError = 5.f;
+    std::vector<int4> leafTri;         // vertex ids of every leaf (w: the leaf's subdivision level)
+    std::vector<int4> qtree;           // adaptive: the 20 face codes (5 int4), then per subdivided
+                                       // triangle two int4: its edge midpoints (ab, bc, ca) and its
+                                       // 4 child codes (children (A,ab,ca), (ab,B,bc), (ca,bc,C),
+                                       // (ab,bc,ca)); a code >= 0 is a subdivided triangle, < 0 ~leaf
     std::vector<float4> vdir;          // vertex directions; w: the id of the antipodal vertex (int bits;
                                        // the subdivided icosahedron is centrally symmetric)
     std::vector<int4> tri;             // vertex ids of every triangle of every level (level 0 first)
@@ -65,5 +82,27 @@ constexpr uint32_t kSteerLeafNone = 0xffffu, kSteerLeafMany = 0xfffeu;
 // The geometry of subdivision level `level` (<= 7), built on first use and kept for the life of
 // the process (thread-safe). Returns null with a message in err on failure.
 const SteerGeom *steerGeometry(uint32_t level, std::string &err);
+
+constexpr uint32_t kSteerMaxAdaptiveLevel = 12;
+constexpr uint32_t kSteerMaxAdaptiveLeaves = 1u << 22;
+
+// Adaptive triangulation of an RGB float map (W x H, row 0 at theta = 0) by the reference's
+// refinement rule (TriangulateEm, src/em_steerable_sampler.hxx:2963-3472): a triangle below
+// minLevel is subdivided, one at maxLevel is kept, and in between it is subdivided when the
+// linear interpolation of its vertices' luminance differs from the map's bilinear luminance by
+// more than the factor 1 + maxError at any of its test samples.
+std::shared_ptr<SteerGeom> steerAdaptiveGeometry(const float *rgb, uint32_t W, uint32_t H, uint32_t minLevel,
+                                                 uint32_t maxLevel, float maxError, std::string &err);
+
+// The geometry of a given set of leaves (a file of the reference): every leaf must be a triangle
+// of the icosahedron's 4-way subdivision at its stated level, the leaves must cover the sphere
+// exactly once. corners: three unit directions per leaf. Built adaptive (quadtree locator).
+std::shared_ptr<SteerGeom> steerGeometryFromLeaves(const std::vector<std::array<float, 9>> &corners,
+                                                   const std::vector<uint32_t> &levels, uint32_t minLevel,
+                                                   uint32_t maxLevel, float maxError, std::string &err);
+
+// Luminance of the map's bilinear (tent) lookup in direction d, as the reference's
+// EnvironmentMapImage::Evaluate (src/em_image.hxx:95-150) with Dir2LatLong (src/geom.hxx:78-95).
+float emLuminanceDir(const float *rgb, uint32_t W, uint32_t H, float dx, float dy, float dz);
 
 }  // namespace pg3

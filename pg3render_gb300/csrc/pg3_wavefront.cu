@@ -70,10 +70,12 @@ void launchStage(bool pdl, void (*kernel)(Params...), int grid, size_t smem, cud
     cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
 }
 
+// The first sample index of a launch: sample0, plus a device word when one is given (a captured
+// graph replays with a new word: a differentiable-rendering graph, a per-call render graph).
 template <bool GRAD>
 PG3_DI uint32_t sampleBase(uint32_t sample0, const GradArgs &G)
 {
-    return (GRAD && G.sampleOffset) ? sample0 + *G.sampleOffset : sample0;
+    return G.sampleOffset ? sample0 + *G.sampleOffset : sample0;
 }
 
 template <bool GRAD>
@@ -352,6 +354,8 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
                 shades = launchShade<kEmCdf, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
             else if (emk == kEmSteerable)
                 shades = launchShade<kEmSteerable, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
+            else if (emk == kEmSteerableAdaptive)
+                shades = launchShade<kEmSteerableAdaptive, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
             else
                 shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
             launchStage(pdl, shadowKernel<GRAD>, queryGrid, smem, stream, S, Q, r, g, b, stats, G);
@@ -379,13 +383,15 @@ size_t wavefrontBytes(uint64_t cap, bool grad)
 
 cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch, uint64_t capacity,
-                            int gridBlocks, cudaStream_t stream, uint64_t *launches, const GradArgs *grad)
+                            int gridBlocks, cudaStream_t stream, uint64_t *launches, const GradArgs *grad,
+                            const uint32_t *sampleOffset)
 {
     if (capacity > kMaxSlots || numPaths > 0xffffffffull) return cudaErrorInvalidValue;
     if (grad)
         return runWavefront<true>(S, kindMask, sample0, numPaths, npix, outR, outG, outB, stats, scratch, capacity,
                                   gridBlocks, stream, launches, *grad);
     GradArgs none{};
+    none.sampleOffset = sampleOffset;
     return runWavefront<false>(S, kindMask, sample0, numPaths, npix, outR, outG, outB, stats, scratch, capacity,
                                gridBlocks, stream, launches, none);
 }

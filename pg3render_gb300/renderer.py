@@ -63,6 +63,8 @@ class Config:
     max_paths_in_flight: int = 0
     ggx_sampler: int = 0                 # GGX_VNDF_EXACT; GGX_VNDF_REFERENCE_FIT = the reference's routine
     steer_weights: int = 1               # STEER_WEIGHTS_PROJECTED; STEER_WEIGHTS_POINT = the reference's build
+    steer_max_subdiv_level: int = 0      # > steer_subdiv_level: adaptive triangulation between the levels
+    steer_max_approx_error: float = 5.0  # adaptive triangulation: the reference's maximum approximation error
 
     def options(self, seed=None):
         o = _lib.Options()
@@ -83,6 +85,8 @@ class Config:
         o.max_paths_in_flight = self.max_paths_in_flight
         o.ggx_sampler = self.ggx_sampler
         o.steer_weights = self.steer_weights
+        o.steer_max_subdiv_level = self.steer_max_subdiv_level
+        o.steer_max_approx_error = self.steer_max_approx_error
         return o
 
 

@@ -15,6 +15,8 @@
 //                    variance (W*H*3 doubles each, row 0 at the top)
 //   --batch N        N iterations per RunIterations call instead of one RunIteration each
 //   --device D       CUDA device
+//   --dump-scene P   write the scene as GpuPathTracer translates it (JSON) and exit without
+//                    rendering (needs no GPU)
 // It prints one JSON line: seconds of the render loop (first call to the synchronised
 // framebuffer), samples and Msamples/s.
 #include "config.hxx"
@@ -34,12 +36,77 @@ void Fail(const std::string &msg)
     std::exit(2);
 }
 
+void PutFloats(FILE *f, const float *v, int n)
+{
+    std::fputc('[', f);
+    for (int i = 0; i < n; ++i) std::fprintf(f, "%s%.9g", i ? ", " : "", v[i]);
+    std::fputc(']', f);
+}
+
+// The translated scene description as JSON (field names of include/pg3gpu.h).
+void DumpScene(const gpu_shim::SceneDesc &d, const char *path)
+{
+    FILE *f = std::fopen(path, "w");
+    if (!f) Fail(std::string("cannot write ") + path);
+    const pg3gpu_camera &c = d.desc.camera;
+    std::fprintf(f, "{\"camera\": {\"position\": ");
+    PutFloats(f, c.position, 3);
+    std::fprintf(f, ", \"forward\": ");
+    PutFloats(f, c.forward, 3);
+    std::fprintf(f, ", \"up\": ");
+    PutFloats(f, c.up, 3);
+    std::fprintf(f, ", \"width\": %u, \"height\": %u, \"hfov_deg\": %.9g},\n", c.width, c.height, c.hfov_deg);
+    std::fprintf(f, "\"materials\": [");
+    for (size_t i = 0; i < d.materials.size(); ++i) {
+        const pg3gpu_material &m = d.materials[i];
+        std::fprintf(f, "%s\n {\"kind\": %d, \"albedo\": ", i ? "," : "", m.kind);
+        PutFloats(f, m.albedo, 3);
+        std::fprintf(f, ", \"alpha\": %.9g, \"ior\": %.9g, \"ior_outer\": %.9g, \"absorb\": %.9g, \"glossy\": ",
+                     m.alpha, m.ior, m.ior_outer, m.absorb);
+        PutFloats(f, m.glossy, 3);
+        std::fprintf(f, ", \"phong_exponent\": %.9g, \"inner_kind\": %d, \"inner_alpha\": %.9g, \"inner_ior\": %.9g, "
+                     "\"medium_attenuation\": ", m.phong_exponent, m.inner_kind, m.inner_alpha, m.inner_ior);
+        PutFloats(f, m.medium_attenuation, 3);
+        std::fprintf(f, ", \"medium_thickness\": %.9g}", m.medium_thickness);
+    }
+    std::fprintf(f, "],\n\"triangles\": [");
+    for (size_t i = 0; i < d.triangles.size(); ++i) {
+        std::fprintf(f, "%s\n {\"p\": ", i ? "," : "");
+        PutFloats(f, d.triangles[i].p, 9);
+        std::fprintf(f, ", \"material\": %d}", d.triangles[i].material);
+    }
+    std::fprintf(f, "],\n\"spheres\": [");
+    for (size_t i = 0; i < d.spheres.size(); ++i) {
+        std::fprintf(f, "%s\n {\"center\": ", i ? "," : "");
+        PutFloats(f, d.spheres[i].center, 3);
+        std::fprintf(f, ", \"radius\": %.9g, \"material\": %d}", d.spheres[i].radius, d.spheres[i].material);
+    }
+    std::fprintf(f, "],\n\"area_lights\": [");
+    for (size_t i = 0; i < d.areaLights.size(); ++i) {
+        std::fprintf(f, "%s\n {\"triangle\": %u, \"radiance\": ", i ? "," : "", d.areaLights[i].triangle);
+        PutFloats(f, d.areaLights[i].radiance, 3);
+        std::fputc('}', f);
+    }
+    std::fprintf(f, "],\n\"point_lights\": [");
+    for (size_t i = 0; i < d.pointLights.size(); ++i) {
+        std::fprintf(f, "%s\n {\"position\": ", i ? "," : "");
+        PutFloats(f, d.pointLights[i].position, 3);
+        std::fprintf(f, ", \"power\": ");
+        PutFloats(f, d.pointLights[i].power, 3);
+        std::fputc('}', f);
+    }
+    std::fprintf(f, "],\n\"background\": %d, \"background_radiance\": ", d.desc.background);
+    PutFloats(f, d.desc.background_radiance, 3);
+    std::fprintf(f, ", \"env_width\": %u, \"env_height\": %u}\n", d.desc.env_width, d.desc.env_height);
+    std::fclose(f);
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
 {
     int resW = 0, resH = 0, batch = 1, device = 0;
-    std::string outPath;
+    std::string outPath, dumpPath;
     int sceneId = 0, emId = Scene::kEMDefault;
     std::vector<const char *> refArgs{argv[0]};
     for (int i = 1; i < argc; ++i) {
@@ -60,6 +127,9 @@ int main(int argc, char **argv)
         } else if (a == "--device") {
             need(1);
             device = std::atoi(argv[++i]);
+        } else if (a == "--dump-scene") {
+            need(1);
+            dumpPath = argv[++i];
         } else {
             if (a == "-s" && i + 1 < argc) sceneId = std::atoi(argv[i + 1]);
             if (a == "-em" && i + 1 < argc) emId = std::atoi(argv[i + 1]);
@@ -77,6 +147,13 @@ int main(int argc, char **argv)
         scene->LoadCornellBox(Vec2i(resW, resH), config.mAuxDbgParams, g_SceneConfigs[sceneId],
                               Scene::EnvironmentMapType(emId));
         config.mScene = scene;
+    }
+    if (!dumpPath.empty()) {
+        gpu_shim::SceneDesc d;
+        gpu_shim::TranslateScene(*config.mScene, d);
+        DumpScene(d, dumpPath.c_str());
+        delete config.mScene;
+        return 0;
     }
     Framebuffer fb;
     config.mFramebuffer = &fb;

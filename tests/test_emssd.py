@@ -6,7 +6,10 @@ adaptive one (levels 1-3). The CPU tests read the reference's files with a reade
 from the format (src/em_steerable_sampler.hxx:1659-1745, 1796-1960) and pin the vertex weights
 the library builds on the device (luminance of the map's bilinear lookup times the 9 SH basis
 values of the vertex direction) against the reference's; the GPU tests write and read files
-through the C ABI."""
+through the C ABI. The library's own adaptive triangulation (the reference's refinement rule,
+restated on the host) reproduces the reference's adaptive file leaf for leaf; the reference's
+adaptive file loads and renders what the reference's render of the same scene shows."""
+import ctypes
 import os
 import struct
 
@@ -142,12 +145,88 @@ def test_reference_vertex_weights_are_map_luminance_times_sh():
     np.testing.assert_allclose(u["weights"], want, rtol=1e-5, atol=1e-6 * scale)
 
 
-def _ctx(env, sampler=None, level=2, seed=5):
+def write_file(params, dirs, weights, leaves):
+    """A format-2.1 file of the given leaves (level, 3 vertex indices) under a flat chain of
+    6-child set nodes (the reader accepts any tree)."""
+    out = bytearray(HEADER)
+    out += struct.pack("<fIIIffI", *params)
+    out += struct.pack("<I", len(dirs))
+    for d, w in zip(dirs, weights):
+        out += struct.pack("<12f", *np.concatenate([d, w]).astype(np.float32))
+    nodes = [("leaf", tuple(l)) for l in leaves]
+    sets = 0
+    while len(nodes) > 1:
+        nodes = [("set", nodes[i:i + 6]) for i in range(0, len(nodes), 6)]
+        sets += len(nodes)
+    out += struct.pack("<II", sets, len(leaves))
+
+    def emit(n):
+        nonlocal out
+        if n[0] == "leaf":
+            out += struct.pack("<IIIII", 1, *n[1])
+        else:
+            out += struct.pack("<II", 0, len(n[1]))
+            for c in n[1]:
+                emit(c)
+    emit(nodes[0])
+    return bytes(out)
+
+
+def triangulate(em, lo, hi, err):
+    """The library's adaptive triangulation (pg3gpu_steer_triangulate): levels, corners."""
+    L = _lib.load()
+    em = np.ascontiguousarray(em, np.float32)
+    n = ctypes.c_uint32()
+    _lib.check(L.pg3gpu_steer_triangulate(em.ctypes.data, em.shape[1], em.shape[0], lo, hi, err, ctypes.byref(n),
+                                          None, None))
+    lv = np.zeros(n.value, np.uint32)
+    cr = np.zeros((n.value, 9), np.float32)
+    _lib.check(L.pg3gpu_steer_triangulate(em.ctypes.data, em.shape[1], em.shape[0], lo, hi, err, ctypes.byref(n),
+                                          lv.ctypes.data, cr.ctypes.data))
+    return lv, cr
+
+
+def test_adaptive_triangulation_is_the_references():
+    # the reference's adaptive file (levels 1-3, error 0.05) and the library's build of the same
+    # map and parameters: the same leaves, at the same levels, with bit-identical corners
+    z = _fixture()
+    ref = parse(z["adaptive"].tobytes())
+    err, lo, hi = ref["params"][0], ref["params"][1], ref["params"][2]
+    lv, cr = triangulate(z["env_map"], lo, hi, err)
+    assert len(lv) == len(ref["leaves"])
+    mine = {}
+    for level, c in zip(lv, cr):
+        tri = sorted(tuple(np.float32(x) for x in c[3 * j:3 * j + 3]) for j in range(3))
+        mine[tuple(tri)] = int(level)
+    for level, a, b, c in ref["leaves"]:
+        tri = sorted(tuple(np.float32(x) for x in ref["dirs"][i]) for i in (a, b, c))
+        assert mine.get(tuple(tri)) == level
+    # leaves tile the sphere: planar areas sum to the subdivided icosahedron's below 4 pi
+    assert sorted(set(lv.tolist())) == [1, 2, 3]
+
+
+def test_adaptive_triangulation_parameters():
+    sky = S.synthetic_sky(256, 128, seed=7)
+    lv, _ = triangulate(sky, 4, 9, 5.0)                  # the reference's default build parameters
+    assert lv.min() == 4 and lv.max() > 6                # refined around the suns only
+    assert len(lv) < 20 * 4 ** 6
+    lv2, _ = triangulate(sky, 3, 3, 5.0)                 # minimum = maximum: the uniform level
+    assert len(lv2) == 20 * 4 ** 3 and set(lv2.tolist()) == {3}
+    with pytest.raises(P.Pg3Error):
+        triangulate(sky, 5, 4, 5.0)
+    with pytest.raises(P.Pg3Error):
+        triangulate(sky, 4, 13, 5.0)
+
+
+def _ctx(env, sampler=None, level=2, seed=5, adaptive=None):
     # the reference's vertex weights are point samples of the map: the same build here
     sc = S.cornell_env(16, 16, 64, 32)
     sc.env_map = env
+    kw = {}
+    if adaptive:
+        kw = dict(steer_max_subdiv_level=adaptive[0], steer_max_approx_error=adaptive[1])
     cfg = P.Config(scene=sc, max_path_length=6, em_sampler=sampler if sampler is not None else _lib.EM_STEERABLE,
-                   steer_subdiv_level=level, steer_weights=_lib.STEER_WEIGHTS_POINT)
+                   steer_subdiv_level=level, steer_weights=_lib.STEER_WEIGHTS_POINT, **kw)
     return P.GpuPathTracer(cfg, seed=seed)
 
 
@@ -206,26 +285,76 @@ def test_round_trip_is_byte_identical(tmp_path):
 
 
 @pytest.mark.gpu
+def test_loading_the_reference_adaptive_file(tmp_path):
+    # the reference's adaptive file replaces a uniform context's triangulation; the library's own
+    # adaptive build of the same map and parameters renders the same image (same leaves, same
+    # point-sampled weights), and saving writes the file's triangulation back
+    z = _fixture()
+    src = str(tmp_path / str(z["adaptive_name"]))
+    open(src, "wb").write(z["adaptive"].tobytes())
+    ref = parse(z["adaptive"].tobytes())
+    out = str(tmp_path / "again.emssd")
+    with _ctx(z["env_map"], level=1, adaptive=(3, 0.05)) as built, _ctx(z["env_map"]) as loaded:
+        loaded.load_steerable(src)
+        loaded.save_steerable(out)
+        for r in (built, loaded):
+            r.RunIteration(P.renderer.kPathTracing, 0, 256)
+        a, b = built.framebuffer()[0], loaded.framebuffer()[0]
+    again = parse(open(out, "rb").read())
+    assert leaf_set(again) == leaf_set(ref)
+    assert sorted(again["leaves"][:, 0].tolist()) == sorted(ref["leaves"][:, 0].tolist())
+    assert again["params"][:3] == ref["params"][:3]
+    wl, wr = by_direction(again), by_direction(ref)
+    assert wl.keys() == wr.keys()
+    for k in wr:
+        assert np.array_equal(wl[k].astype(np.float32), wr[k].astype(np.float32))
+    assert abs(a.sum() / b.sum() - 1) < 1e-3
+    assert np.isclose(a, b, rtol=1e-3, atol=1e-4 * a.max()).mean() > 0.99
+
+
+@pytest.mark.gpu
+def test_loaded_adaptive_file_renders_the_reference_image():
+    # the reference's adaptive sampler file of the environment-map box's 64x32 sky, loaded and
+    # rendered at as many samples as the reference's golden of that scene (CDF sampler) holds
+    import tempfile
+    from _util import load_golden, scene_from_golden, z_ok, zscores
+    z = _fixture()
+    d, text, td = load_golden("cornell_env_32_cdf")
+    scene = scene_from_golden(d)
+    assert np.array_equal(scene.env_map, z["env_map"])
+    cfg = P.Config(scene=scene, max_path_length=12, em_sampler=_lib.EM_STEERABLE, steer_subdiv_level=1,
+                   steer_weights=_lib.STEER_WEIGHTS_POINT)
+    spp = 65536
+    with tempfile.TemporaryDirectory() as tmp, P.GpuPathTracer(cfg, seed=77) as r:
+        src = os.path.join(tmp, str(z["adaptive_name"]))
+        open(src, "wb").write(z["adaptive"].tobytes())
+        r.load_steerable(src)
+        r.RunIteration(P.renderer.kPathTracing, 0, spp)
+        mean, var, n = r.framebuffer(with_variance=True)
+    frac, zm, zs = z_ok(zscores(mean, var / spp, d["mean"], d["var_mean"]))
+    assert frac >= 0.999 and abs(zm) < 0.25 and 0.7 < zs < 1.3, (frac, zm, zs)
+
+
+@pytest.mark.gpu
 def test_files_the_library_cannot_use_are_refused(tmp_path):
     z = _fixture()
-    adaptive = str(tmp_path / "adaptive.emssd")
-    open(adaptive, "wb").write(z["adaptive"].tobytes())
     cut = str(tmp_path / "cut.emssd")
     open(cut, "wb").write(z["uniform"].tobytes()[:-7])
-    uniform = str(tmp_path / "uniform.emssd")
-    open(uniform, "wb").write(z["uniform"].tobytes())
+    # a triangulation with a hole (one leaf missing) and one with two overlapping leaves
+    u = parse(z["uniform"].tobytes())
+    hole = str(tmp_path / "hole.emssd")
+    open(hole, "wb").write(write_file(u["params"], u["dirs"], u["weights"], u["leaves"][1:]))
+    twice = str(tmp_path / "twice.emssd")
+    open(twice, "wb").write(write_file(u["params"], u["dirs"], u["weights"],
+                                       np.concatenate([u["leaves"], u["leaves"][:1]])))
     with _ctx(z["env_map"]) as r:
-        with pytest.raises(P.Pg3Error) as e:
-            r.load_steerable(adaptive)
-        assert e.value.status == _lib.ERR_UNSUPPORTED
-        for bad in (cut, str(tmp_path / "missing.emssd")):
+        for bad in (cut, hole, twice, str(tmp_path / "missing.emssd")):
             with pytest.raises(P.Pg3Error) as e:
                 r.load_steerable(bad)
-            assert e.value.status == _lib.ERR_INVALID_ARGUMENT
-    with _ctx(z["env_map"], level=3) as r:             # level 2 file, level 3 context
-        with pytest.raises(P.Pg3Error) as e:
-            r.load_steerable(uniform)
-        assert e.value.status == _lib.ERR_UNSUPPORTED
+            assert e.value.status == _lib.ERR_INVALID_ARGUMENT, bad
+        # the context still renders with its own triangulation
+        r.RunIteration(P.renderer.kPathTracing, 0, 4)
+        assert r.framebuffer()[0].sum() > 0
     with _ctx(z["env_map"], sampler=_lib.EM_CDF) as r:  # no steerable sampler
         with pytest.raises(P.Pg3Error) as e:
             r.save_steerable(str(tmp_path / "x.emssd"))

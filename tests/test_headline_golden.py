@@ -27,6 +27,14 @@ SETUPS = {
                                     rr_min_path_length=4),
     "steerable_point_rr4": dict(em_sampler=R.EM_STEERABLE, steer_weights=R.STEER_WEIGHTS_POINT,
                                 rr_min_path_length=4),
+    # adaptive triangulations: the reference's default build (levels 4-9, error 5) with its vertex
+    # weights, and with projected weights
+    "steerable_adaptive_point_rr4": dict(em_sampler=R.EM_STEERABLE, steer_weights=R.STEER_WEIGHTS_POINT,
+                                         steer_subdiv_level=4, steer_max_subdiv_level=9, steer_max_approx_error=5.0,
+                                         rr_min_path_length=4),
+    "steerable_adaptive_projected_rr4": dict(em_sampler=R.EM_STEERABLE, steer_weights=R.STEER_WEIGHTS_PROJECTED,
+                                             steer_subdiv_level=4, steer_max_subdiv_level=9,
+                                             steer_max_approx_error=5.0, rr_min_path_length=4),
     "cdf_rr4": dict(em_sampler=R.EM_CDF, rr_min_path_length=4),
     "cdf": dict(em_sampler=R.EM_CDF),
     "cdf_rr4_megakernel": dict(em_sampler=R.EM_CDF, rr_min_path_length=4, pipeline=R.PIPELINE_MEGAKERNEL),

@@ -40,9 +40,15 @@ def _bsdf_scene():
     return s
 
 
-def _env_scene(sampler, weights=R.STEER_WEIGHTS_POINT):
+def _env_scene(sampler, weights=R.STEER_WEIGHTS_POINT, adaptive=None):
+    """adaptive: (minimum level, maximum level, maximum approximation error) of an adaptive
+    steerable triangulation (leaves at several levels), None for one uniform level."""
     s = S.cornell_env(8, 8, 256, 128, em_seed=11)
-    return P.Config(scene=s, max_path_length=12, em_sampler=sampler, steer_weights=weights)
+    kw = {}
+    if adaptive:
+        kw = dict(steer_subdiv_level=adaptive[0], steer_max_subdiv_level=adaptive[1],
+                  steer_max_approx_error=adaptive[2])
+    return P.Config(scene=s, max_path_length=12, em_sampler=sampler, steer_weights=weights, **kw)
 
 
 def _rel(a, b):
@@ -124,16 +130,21 @@ def test_reference_vndf_fit_is_approximate():
 
 
 PT, PJ = R.STEER_WEIGHTS_POINT, R.STEER_WEIGHTS_PROJECTED
-ENV_CASES = [(R.EM_COSINE, (0.0, 0.0, 1.0), PT), (R.EM_CDF, (0.0, 0.0, 1.0), PT),
-             (R.EM_STEERABLE, (0.0, 0.0, 1.0), PT), (R.EM_STEERABLE, (0.35, -0.2, 0.915), PT),
-             (R.EM_STEERABLE, (0.0, 0.0, 1.0), PJ), (R.EM_STEERABLE, (-0.6, 0.3, 0.742), PJ)]
+# adaptive steerable triangulations: the reference's default build parameters (levels 4-9,
+# error 5) and a deeper refinement with leaves on five levels
+REF_DEFAULT, DEEP = (4, 9, 5.0), (2, 7, 0.5)
+ENV_CASES = [(R.EM_COSINE, (0.0, 0.0, 1.0), PT, None), (R.EM_CDF, (0.0, 0.0, 1.0), PT, None),
+             (R.EM_STEERABLE, (0.0, 0.0, 1.0), PT, None), (R.EM_STEERABLE, (0.35, -0.2, 0.915), PT, None),
+             (R.EM_STEERABLE, (0.0, 0.0, 1.0), PJ, None), (R.EM_STEERABLE, (-0.6, 0.3, 0.742), PJ, None),
+             (R.EM_STEERABLE, (0.0, 0.0, 1.0), PT, REF_DEFAULT), (R.EM_STEERABLE, (0.35, -0.2, 0.915), PT, DEEP),
+             (R.EM_STEERABLE, (-0.6, 0.3, 0.742), PJ, REF_DEFAULT)]
 
 
-@pytest.mark.parametrize("sampler,normal,weights", ENV_CASES)
-def test_env_sampler_pdf_consistency(sampler, normal, weights):
+@pytest.mark.parametrize("sampler,normal,weights,adaptive", ENV_CASES)
+def test_env_sampler_pdf_consistency(sampler, normal, weights, adaptive):
     nrm = np.asarray(normal, np.float32)
     nrm /= np.linalg.norm(nrm)
-    with P.GpuPathTracer(_env_scene(sampler, weights)) as r:
+    with P.GpuPathTracer(_env_scene(sampler, weights, adaptive)) as r:
         n = 1 << 18
         o = r.probe_light(0, np.zeros((n, 3)), np.tile(nrm, (n, 1)), seed=9)
     # CDF samples below the horizon carry zero radiance but a valid pdf; compare where upper
@@ -144,11 +155,11 @@ def test_env_sampler_pdf_consistency(sampler, normal, weights):
     assert np.median(rel) <= 1e-6 and np.quantile(rel, 0.999) <= 1e-5, (np.median(rel), np.quantile(rel, 0.999))
 
 
-@pytest.mark.parametrize("sampler,normal,weights", ENV_CASES)
-def test_env_sampler_chi_square(sampler, normal, weights):
+@pytest.mark.parametrize("sampler,normal,weights,adaptive", ENV_CASES)
+def test_env_sampler_chi_square(sampler, normal, weights, adaptive):
     nrm = np.asarray(normal, np.float32)
     nrm /= np.linalg.norm(nrm)
-    with P.GpuPathTracer(_env_scene(sampler, weights)) as r:
+    with P.GpuPathTracer(_env_scene(sampler, weights, adaptive)) as r:
         o = r.probe_light(0, np.zeros((N_CHI, 3)), np.tile(nrm, (N_CHI, 1)), seed=13)
         if sampler == R.EM_CDF:
             # The CDF sampler's pdf is exact per map pixel only (uniform in (u, v) inside a pixel,

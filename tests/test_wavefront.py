@@ -66,3 +66,29 @@ def test_wavefront_against_reference_golden(name):
         mean, var, n = r.framebuffer(with_variance=True)
     frac, zm, zs = z_ok(zscores(mean, var / spp, d["mean"], d["var_mean"]))
     assert frac >= 0.999 and abs(zm) < 0.25 and 0.7 < zs < 1.3, (frac, zm, zs)
+
+
+@pytest.mark.parametrize("sampler", [R.EM_STEERABLE, R.EM_CDF])
+def test_small_calls_replay_a_render_graph(sampler):
+    # Calls of up to 2^22 paths in one launch chunk (the reference's RunIteration pattern: one
+    # sample per pixel per call) replay a captured graph of the chunk's launches, with the call's
+    # first sample index set in its head node. The image is the one of the same samples launched
+    # directly (pg3gpu_render_samples), summed per pixel in sample order: bit for bit.
+    scene = S.cornell_env(48, 40, 128, 64)
+    cfg = P.Config(scene=scene, max_path_length=12, rr_min_path_length=4, em_sampler=sampler)
+    with P.GpuPathTracer(cfg, seed=3) as r:
+        for k in range(12):
+            r.RunIteration(R.kPathTracing, k, 1)
+        r.RunIteration(R.kPathTracing, 12, 3)      # another sample count: captured anew
+        r.RunIteration(R.kPathTracing, 15, 1)
+        mean, var, n = r.framebuffer(with_variance=True)
+        st = r.stats()
+    with P.GpuPathTracer(cfg, seed=3) as d:
+        samples = d.render_samples(R.kPathTracing, 0, 16).astype(np.float64)
+    assert n == 16
+    acc = np.zeros(samples.shape[1:])
+    for k in range(16):
+        acc += samples[k]
+    assert np.array_equal(mean, acc / 16)
+    assert st["paths"] == 16 * 48 * 40
+    assert st["kernel_launches"] > 14 * 40      # every replay counts its stage launches
