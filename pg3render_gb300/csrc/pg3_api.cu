@@ -198,6 +198,11 @@ int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passe
 #ifndef PG3_CALL_GRAPH_MAX_PATHS
 #define PG3_CALL_GRAPH_MAX_PATHS (1u << 22)
 #endif
+// The stage launches inside the render graph keep their programmatic dependencies (a stage's
+// blocks start while its predecessor drains and wait in griddepcontrol.wait).
+#ifndef PG3_CALL_GRAPH_PDL
+#define PG3_CALL_GRAPH_PDL 1
+#endif
 
 bool callGraphEligible(pg3gpu_ctx *ctx, int algorithm, uint32_t spp)
 {
@@ -242,7 +247,7 @@ int captureCallGraph(pg3gpu_ctx *ctx, uint32_t passes)
     if (e == cudaSuccess)
         e = launchWavefront(ctx->view, ctx->kindMask, 0u, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
                             ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->graphStream, &launches,
-                            nullptr, ctx->dCallBase);
+                            nullptr, ctx->dCallBase, PG3_CALL_GRAPH_PDL != 0);
     if (e == cudaSuccess)
         e = launchAccumulate(npix, passes, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2], ctx->dSum, ctx->dSumsq,
                              ctx->graphStream);

@@ -44,7 +44,8 @@ size_t wavefrontBytes(uint64_t capacity, bool grad);
 cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch,
                             uint64_t capacity, int gridBlocks, cudaStream_t stream, uint64_t *launches,
-                            const GradArgs *grad = nullptr, const uint32_t *sampleOffset = nullptr);
+                            const GradArgs *grad = nullptr, const uint32_t *sampleOffset = nullptr,
+                            bool pdlInCapture = false);
 
 // pg3_steer_build.cu: the steerable sampler's map-dependent tables from the device texels
 constexpr uint32_t kSteerMaxLayers = 16;

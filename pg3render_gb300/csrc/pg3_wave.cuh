@@ -78,6 +78,25 @@ PG3_DI float4 *rayQ(const Queues &Q, int q) { return q ? Q.ray[1] : Q.ray[0]; }
 PG3_DI float4 *stQ(const Queues &Q, int q) { return q ? Q.st[1] : Q.st[0]; }
 PG3_DI uint32_t *bucketQ(const Queues &Q, int b) { return Q.bucket[0] + (size_t)b * Q.bucketStride; }
 
+// Append by the lanes that call it (the active lanes of a warp are grouped; each group's leader
+// reserves its slots): usable inside divergent code, unlike warpAppend.
+PG3_DI uint32_t activeAppend(uint32_t *counter)
+{
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// Shadow records are appended where the light sample is taken (PG3_EARLY_SHADOW), so that the
+// record's 12 floats are not held through the BSDF sample until the end of the vertex.
+#ifndef PG3_EARLY_SHADOW
+#define PG3_EARLY_SHADOW 0
+#endif
+
 // Warp-aggregated append: lanes with `want` get consecutive slots of *counter.
 PG3_DI uint32_t warpAppend(uint32_t *counter, bool want)
 {
@@ -321,6 +340,22 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
                             e = delta * beta * br.att * (fabsf(dot(wig, nrm)) * w);
                         o.s4 = make_float4(e.x, e.y, e.z, __int_as_float(matId));
                     }
+                }
+                if (PG3_EARLY_SHADOW) {
+                    constexpr int SW = kShadowWords<GRAD>;
+                    const uint32_t sp = activeAppend(&Q.cnt->shadow);
+                    if (sp >= Q.cap) atomicOr(Q.err, kErrQueueOverflow);
+                    else {
+                        float4 *d = Q.shadow + (size_t)SW * sp;
+                        d[0] = o.s0;
+                        d[1] = o.s1;
+                        d[2] = o.s2;
+                        if (GRAD) {
+                            d[3] = o.s3;
+                            d[4] = o.s4;
+                        }
+                    }
+                    o.shadow = false;
                 }
             }
         }

@@ -14,7 +14,8 @@
 //                     Russian roulette, BSDF sample -> next ray queue
 //     shadow          any-hit test of every shadow record; unoccluded records
 //                     add their contribution to the path's radiance
-//     advance         zero the counters consumed by this bounce
+// The counters a bounce has consumed are reset by the next stage that no longer reads them:
+// shadow zeroes the ray queue's and the buckets' counters, the next extend the shadow counter.
 // Each stage kernel holds only its own material's code, which keeps it inside
 // the instruction cache, and a warp shades hits of one material kind only.
 // Launches are persistent grids that stride over the counts they read from
@@ -115,6 +116,9 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) extendKernel
                                                            DevStats *stats)
 {
     stageEntry();
+    // the previous bounce's shadow records are consumed: its counter starts the new bounce at zero
+    // (no stage reads or appends shadow records while rays are extended)
+    if (blockIdx.x == 0 && threadIdx.x == 0) Q.cnt->shadow = 0;
     const uint32_t n = Q.cnt->ray[cur];
     const float4 *rq = rayQ(Q, cur);
     uint32_t rays = 0;
@@ -216,12 +220,19 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
 
 template <bool GRAD>
 __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) shadowKernel(const __grid_constant__ SceneView S, Queues Q,
-                                                           float *outR, float *outG, float *outB, DevStats *stats,
-                                                           GradArgs G)
+                                                           int cur, float *outR, float *outG, float *outB,
+                                                           DevStats *stats, GradArgs G)
 {
     constexpr int SW = kShadowWords<GRAD>;
     extern __shared__ float sGrad[];
     stageEntry();
+    // this bounce's ray queue and buckets are consumed (extend and the shade kernels have
+    // completed): their counters start at zero for the next bounce's appends. No stage of the
+    // shadow pass reads them.
+    if (blockIdx.x == 0 && threadIdx.x < 1 + kNumBuckets) {
+        if (threadIdx.x == 0) Q.cnt->ray[cur] = 0;
+        else Q.cnt->bucket[threadIdx.x - 1] = 0;
+    }
     initBlockGrad<GRAD>(sGrad, S.nmat);
     const uint32_t n = Q.cnt->shadow;
     uint32_t cnt = 0;
@@ -250,15 +261,6 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) shadowKernel
     }
     countWarp(&stats->shadowRays, cnt);
     flushBlockGrad<GRAD>(sGrad, S.nmat, G.gMat);
-}
-
-__global__ void advanceKernel(Counters *c, int cur)
-{
-    stageEntry();
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;   // launched with one block of the stage size
-    c->ray[cur] = 0;
-    for (int b = 0; b < kNumBuckets; ++b) c->bucket[b] = 0;
-    c->shadow = 0;
 }
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -320,7 +322,7 @@ int launchShade(const SceneView &S, uint32_t kindMask, const Queues &Q, int cur,
 template <bool GRAD>
 cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix, float *outR,
                          float *outG, float *outB, DevStats *stats, void *scratch, uint64_t capacity, int gridBlocks,
-                         cudaStream_t stream, uint64_t *launches, const GradArgs &G0)
+                         cudaStream_t stream, uint64_t *launches, const GradArgs &G0, bool pdlInCapture = false)
 {
     Queues Q = carve(scratch, capacity, GRAD);
     Q.err = S.errorFlag;
@@ -345,7 +347,7 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
         *launches += 1;
         for (uint32_t bounce = 0; bounce < maxBounces; ++bounce) {
             const int cur = bounce & 1;
-            const bool pdl = capturing == cudaStreamCaptureStatusNone;
+            const bool pdl = capturing == cudaStreamCaptureStatusNone || pdlInCapture;
             launchStage(pdl, extendKernel, queryGrid, 0, stream, S, Q, cur, stats);
             const int emk = (S.bgKind == kBgEnvMap) ? S.emSampler : kEmCosine;   // no map: constant/area paths
             const uint32_t b32 = (uint32_t)base;
@@ -358,9 +360,8 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
                 shades = launchShade<kEmSteerableAdaptive, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
             else
                 shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
-            launchStage(pdl, shadowKernel<GRAD>, queryGrid, smem, stream, S, Q, r, g, b, stats, G);
-            launchStage(pdl, advanceKernel, 1, 0, stream, Q.cnt, cur);
-            *launches += 3 + shades;
+            launchStage(pdl, shadowKernel<GRAD>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
+            *launches += 2 + shades;
             if (S.maxPL == 0 && (bounce & 7) == 7 && capturing == cudaStreamCaptureStatusNone) {
                 // roulette-ended paths: stop once the queue is empty (checked every 8 bounces)
                 uint32_t left = 0;
@@ -384,7 +385,7 @@ size_t wavefrontBytes(uint64_t cap, bool grad)
 cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                             float *outR, float *outG, float *outB, DevStats *stats, void *scratch, uint64_t capacity,
                             int gridBlocks, cudaStream_t stream, uint64_t *launches, const GradArgs *grad,
-                            const uint32_t *sampleOffset)
+                            const uint32_t *sampleOffset, bool pdlInCapture)
 {
     if (capacity > kMaxSlots || numPaths > 0xffffffffull) return cudaErrorInvalidValue;
     if (grad)
@@ -393,7 +394,7 @@ cudaError_t launchWavefront(const SceneView &S, uint32_t kindMask, uint32_t samp
     GradArgs none{};
     none.sampleOffset = sampleOffset;
     return runWavefront<false>(S, kindMask, sample0, numPaths, npix, outR, outG, outB, stats, scratch, capacity,
-                               gridBlocks, stream, launches, none);
+                               gridBlocks, stream, launches, none, pdlInCapture);
 }
 
 }  // namespace pg3

@@ -7,6 +7,11 @@ image rendered with hidden, seeded values. Every iteration renders the current p
 step; the whole iteration -- parameter upload with the environment-map CDF rebuilt on the
 device, forward, loss, adjoint, optimiser, and the advance of the sample offset so that each
 replay draws new samples -- is one captured CUDA graph. Texels are optimised in log space.
+
+One view of the box does not determine a sky: albedo times illumination is a scale ambiguity,
+and the map absorbs the render noise. ``optimize_env=False`` keeps the map at its hidden values
+(the materials are then identifiable); ``env_smoothness`` adds a penalty on the squared
+differences of neighbouring log texels, which keeps the recovered map from fitting noise.
 """
 import math
 import time
@@ -30,10 +35,11 @@ def _hidden_scene(side, em, seed):
 
 
 def run(steps=500, lr=1e-2, side=128, spp=16, target_spp=1024, em=(256, 128), seed=0, max_path_length=12,
-        rr_min_path_length=4, eval_spp=256, optimize_env=True, device=0):
+        rr_min_path_length=4, eval_spp=256, optimize_env=True, env_smoothness=0.0, device=0):
     """Returns a dict: losses against the hidden-parameter render, parameter errors before and
     after, and the device time per iteration. With optimize_env False the map keeps its hidden
-    values and only the materials are recovered."""
+    values and only the materials are recovered; env_smoothness > 0 weights the penalty on
+    neighbouring log-texel differences (added to the image loss)."""
     import torch
     torch.cuda.set_device(device)
     hidden, lam, ggx = _hidden_scene(side, em, seed)
@@ -71,7 +77,12 @@ def run(steps=500, lr=1e-2, side=128, spp=16, target_spp=1024, em=(256, 128), se
             opt.zero_grad(set_to_none=False)
             img = diff.render(dr, mats, torch.exp(theta) if optimize_env else None, iteration=0, spp=spp)
             loss = ((img - target) ** 2).mean()
-            loss.backward()
+            total = loss
+            if optimize_env and env_smoothness > 0:
+                dv = theta[1:] - theta[:-1]
+                du = theta[:, 1:] - theta[:, :-1]
+                total = loss + env_smoothness * ((dv ** 2).mean() + (du ** 2).mean())
+            total.backward()
             opt.step()
             with torch.no_grad():
                 mats.copy_(torch.where(mask > 0, mats.clamp(0.001, 1.0), mats))
@@ -116,6 +127,7 @@ def run(steps=500, lr=1e-2, side=128, spp=16, target_spp=1024, em=(256, 128), se
         after = evaluate()
         ms = t0.elapsed_time(t1) / max(1, steps - 3)
         return dict(steps=steps, side=side, spp=spp, target_spp=target_spp, env=list(e_true.shape),
+                    optimize_env=optimize_env, env_smoothness=env_smoothness,
                     iteration_ms=ms, wall_s=wall, before=before, after=after, loss_trace=losses,
                     materials_true=m_true[lam + ggx].tolist(), materials_found=mats.detach().cpu().numpy()[lam + ggx].tolist())
     finally:
