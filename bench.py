@@ -570,8 +570,8 @@ def inverse_metric():
 def mesh_metric(reps=3):
     """The environment-map box with its spheres as triangle meshes (two icospheres of 20480
     triangles each, 40968 triangles in all), 512x512 x 64 spp by default, steerable sampler: every
-    closest-hit and any-hit query runs through the device LBVH (the list loop would test every
-    triangle)."""
+    closest-hit and any-hit query runs through a BVH built on the device (the list loop would test
+    every triangle), the binary LBVH and the 4-wide BVH collapsed from it (the default)."""
     import torch
     import pg3render_gb300 as P
     from pg3render_gb300 import scene as S
@@ -579,25 +579,28 @@ def mesh_metric(reps=3):
     side = MESH_SIDE
     sc = S.cornell_env_mesh(side, side, 1024, 512, level=5)
     spp = MESH_SPP
-    cfg = P.Config(scene=sc, max_path_length=12, rr_min_path_length=4, em_sampler=R.EM_STEERABLE,
-                   traversal=R.TRAVERSAL_BVH)
-    with P.GpuPathTracer(cfg) as r:
-        r.RunIteration(R.kPathTracing, 0, spp)
-        r.synchronize()
-        ts = []
-        for rep in range(reps):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            r.RunIteration(R.kPathTracing, (rep + 1) * spp, spp)
-            r.synchronize()
-            ts.append(time.perf_counter() - t0)
-        st = r.stats()
-    t = statistics.median(ts)
     paths = side * side * spp
-    return {"metric": "Msamples/s (LBVH traversal)", "triangles": len(sc.triangles), "side": side, "spp": spp,
-            "msamples_per_s": round(paths / t / 1e6, 1), "ms_per_run": round(t * 1e3, 2),
-            "segments_per_path": round(st["extension_rays"] / max(1, st["paths"]), 3),
-            "timing": "host wall clock of whole runs incl. synchronisation, median of %d" % reps}
+    out = {"metric": "Msamples/s (BVH traversal)", "triangles": len(sc.triangles), "side": side, "spp": spp,
+           "timing": "host wall clock of whole runs incl. synchronisation, median of %d" % reps}
+    for name, trav in (("lbvh_binary", R.TRAVERSAL_BVH), ("bvh4", R.TRAVERSAL_BVH4)):
+        cfg = P.Config(scene=sc, max_path_length=12, rr_min_path_length=4, em_sampler=R.EM_STEERABLE,
+                       traversal=trav)
+        with P.GpuPathTracer(cfg) as r:
+            r.RunIteration(R.kPathTracing, 0, spp)
+            r.synchronize()
+            ts = []
+            for rep in range(reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                r.RunIteration(R.kPathTracing, (rep + 1) * spp, spp)
+                r.synchronize()
+                ts.append(time.perf_counter() - t0)
+            st = r.stats()
+        t = statistics.median(ts)
+        out[name] = {"msamples_per_s": round(paths / t / 1e6, 1), "ms_per_run": round(t * 1e3, 2),
+                     "segments_per_path": round(st["extension_rays"] / max(1, st["paths"]), 3)}
+    out["msamples_per_s"] = out["bvh4"]["msamples_per_s"]
+    return out
 
 
 def per_iteration_metric(iters=256, reps=3):

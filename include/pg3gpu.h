@@ -77,7 +77,10 @@ enum {
 enum { PG3GPU_BG_NONE = 0, PG3GPU_BG_CONSTANT = 1, PG3GPU_BG_ENVMAP = 2 };
 /* Environment-map light samplers (compile-time choice in src/hard_config.hxx:17-18, run-time here). */
 enum { PG3GPU_EM_CDF = 0, PG3GPU_EM_COSINE = 1, PG3GPU_EM_STEERABLE = 2 };
-enum { PG3GPU_TRAVERSAL_AUTO = 0, PG3GPU_TRAVERSAL_LIST = 1, PG3GPU_TRAVERSAL_BVH = 2 };
+/* Ray queries: AUTO takes the primitive list up to 32 primitives and the 4-wide BVH above; LIST
+ * tests every primitive in order (the reference's GeometryList, src/scene_graph.hxx:33-82); BVH
+ * the binary LBVH built on the device; BVH4 the 4-wide BVH collapsed from it (same hits). */
+enum { PG3GPU_TRAVERSAL_AUTO = 0, PG3GPU_TRAVERSAL_LIST = 1, PG3GPU_TRAVERSAL_BVH = 2, PG3GPU_TRAVERSAL_BVH4 = 3 };
 enum { PG3GPU_PIPELINE_AUTO = 0, PG3GPU_PIPELINE_MEGAKERNEL = 1, PG3GPU_PIPELINE_WAVEFRONT = 2 };
 
 /* ---- scene description (copied at create time) ------------------------- */

@@ -17,7 +17,7 @@ ALG_PATH_TRACING_NAIVE, ALG_PATH_TRACING = 6, 7
 MAT_LAMBERT, MAT_GGX_CONDUCTOR, MAT_GGX_DIELECTRIC = 0, 1, 2
 BG_NONE, BG_CONSTANT, BG_ENVMAP = 0, 1, 2
 EM_CDF, EM_COSINE, EM_STEERABLE = 0, 1, 2
-TRAVERSAL_AUTO, TRAVERSAL_LIST, TRAVERSAL_BVH = 0, 1, 2
+TRAVERSAL_AUTO, TRAVERSAL_LIST, TRAVERSAL_BVH, TRAVERSAL_BVH4 = 0, 1, 2, 3
 PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT = 0, 1, 2
 GGX_VNDF_EXACT, GGX_VNDF_REFERENCE_FIT = 0, 1
 STEER_WEIGHTS_POINT, STEER_WEIGHTS_PROJECTED = 0, 1

@@ -1,6 +1,7 @@
 // C ABI of the hot path (include/pg3gpu.h): context life cycle, scene upload,
 // light-sampling tables, iteration scheduling and framebuffer readback.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -382,6 +383,81 @@ int pg3gpu_destroy(pg3gpu_ctx *ctx)
 
 }  // extern "C"
 
+namespace {
+
+int floatBitsAsInt(float f)
+{
+    int i;
+    std::memcpy(&i, &f, sizeof i);
+    return i;
+}
+
+// The 4-wide BVH of a binary LBVH (root = node 0): every wide node takes its binary node's
+// children, with each inner child replaced by that child's own two children, so a wide node has
+// up to 4 children and the tree half the binary tree's levels. Wide nodes are numbered breadth
+// first (root 0). Returns false if a child id is out of range or a node is reached twice.
+bool collapseBvh4(const std::vector<BvhNode> &bin, std::vector<BvhNode4> &out)
+{
+    const int n = (int)bin.size();
+    out.clear();
+    if (n < 1) return false;
+    std::vector<int> queue{0};
+    std::vector<char> seen((size_t)n, 0);
+    seen[0] = 1;
+    for (size_t qi = 0; qi < queue.size(); ++qi) {
+        const BvhNode &b = bin[(size_t)queue[qi]];
+        int id[4];
+        float4 lo[4], hi[4];
+        int cnt = 0;
+        const float4 los[2] = {b.lo_l, b.lo_r}, his[2] = {b.hi_l, b.hi_r};
+        for (int side = 0; side < 2; ++side) {
+            const int c = floatBitsAsInt(los[side].w);
+            if (c >= 0) {
+                if (c >= n) return false;
+                const BvhNode &g = bin[(size_t)c];
+                const float4 glo[2] = {g.lo_l, g.lo_r}, ghi[2] = {g.hi_l, g.hi_r};
+                for (int gs = 0; gs < 2; ++gs) {
+                    id[cnt] = floatBitsAsInt(glo[gs].w);
+                    lo[cnt] = glo[gs];
+                    hi[cnt] = ghi[gs];
+                    ++cnt;
+                }
+            } else {
+                id[cnt] = c;
+                lo[cnt] = los[side];
+                hi[cnt] = his[side];
+                ++cnt;
+            }
+        }
+        BvhNode4 w;
+        const float big = 3.0e38f;
+        float *lx = &w.lox.x, *hx = &w.hix.x, *ly = &w.loy.x, *hy = &w.hiy.x, *lz = &w.loz.x, *hz = &w.hiz.x;
+        int *ch = &w.child.x;
+        for (int k = 0; k < 4; ++k) {
+            if (k < cnt) {
+                lx[k] = lo[k].x; ly[k] = lo[k].y; lz[k] = lo[k].z;
+                hx[k] = hi[k].x; hy[k] = hi[k].y; hz[k] = hi[k].z;
+                if (id[k] >= 0) {
+                    if (id[k] >= n || seen[(size_t)id[k]]) return false;
+                    seen[(size_t)id[k]] = 1;
+                    ch[k] = (int)queue.size();
+                    queue.push_back(id[k]);
+                } else
+                    ch[k] = id[k];
+            } else {
+                lx[k] = ly[k] = lz[k] = big;
+                hx[k] = hy[k] = hz[k] = -big;
+                ch[k] = INT_MIN;
+            }
+        }
+        w.pad = make_float4(0.f, 0.f, 0.f, 0.f);
+        out.push_back(w);
+    }
+    return true;
+}
+
+}  // namespace
+
 int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const float *vwHost)
 {
     if (!gp) return fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "steerable tables: no geometry");
@@ -541,9 +617,26 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
         if (e != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "LBVH build: %s", cudaGetErrorString(e)));
         v.bvh = nodes;
         v.bvhRoot = 0;
+        ctx->dBvhBinary = nodes;
     }
     const int trav = opts->traversal;
-    v.useBvh = (nprim >= 2) && (trav == PG3GPU_TRAVERSAL_BVH || (trav == PG3GPU_TRAVERSAL_AUTO && nprim > 32));
+    if (trav < PG3GPU_TRAVERSAL_AUTO || trav > PG3GPU_TRAVERSAL_BVH4)
+        return bail(fail(ctx, PG3GPU_ERR_INVALID_ARGUMENT, "unknown traversal %d", trav));
+    // (batch instances traverse the binary LBVH: the batch's query kernels carry no wide traversal)
+    const bool bvh = nprim >= 2 && (trav == PG3GPU_TRAVERSAL_BVH || trav == PG3GPU_TRAVERSAL_BVH4 ||
+                                    (trav == PG3GPU_TRAVERSAL_AUTO && nprim > 32));
+    const bool wide = bvh && !forBatch && trav != PG3GPU_TRAVERSAL_BVH;
+    v.useBvh = wide ? 2 : bvh ? 1 : 0;
+    if (wide) {
+        std::vector<BvhNode> bin(nprim - 1);
+        if (cudaMemcpy(bin.data(), ctx->dBvhBinary, sizeof(BvhNode) * bin.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return bail(fail(ctx, PG3GPU_ERR_CUDA, "reading the LBVH"));
+        std::vector<BvhNode4> w;
+        if (!collapseBvh4(bin, w)) return bail(fail(ctx, PG3GPU_ERR_CUDA, "LBVH: malformed tree"));
+        BvhNode4 *dw = nullptr;
+        if ((st = upload(ctx, &dw, w))) return bail(st);
+        v.bvh = reinterpret_cast<const BvhNode *>(dw);
+    }
 
     if ((st = devAlloc(ctx, &ctx->dSum, (size_t)ctx->W * ctx->H * 3))) return bail(st);
     if ((st = devAlloc(ctx, &ctx->dSumsq, (size_t)ctx->W * ctx->H * 3))) return bail(st);
@@ -969,6 +1062,6 @@ extern "C" int pg3gpu_export_bvh(pg3gpu_ctx *ctx, uint32_t *num_prims, uint32_t 
     PG3_CUDA(ctx, cudaSetDevice(ctx->device));
     if (codes) PG3_CUDA(ctx, cudaMemcpy(codes, ctx->dBvhCodes, 4 * (size_t)n, cudaMemcpyDeviceToHost));
     if (ids) PG3_CUDA(ctx, cudaMemcpy(ids, ctx->dBvhIds, 4 * (size_t)n, cudaMemcpyDeviceToHost));
-    if (nodes) PG3_CUDA(ctx, cudaMemcpy(nodes, ctx->view.bvh, sizeof(BvhNode) * (size_t)(n - 1), cudaMemcpyDeviceToHost));
+    if (nodes) PG3_CUDA(ctx, cudaMemcpy(nodes, ctx->dBvhBinary, sizeof(BvhNode) * (size_t)(n - 1), cudaMemcpyDeviceToHost));
     return PG3GPU_OK;
 }

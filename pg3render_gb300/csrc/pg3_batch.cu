@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kWaveBlock) batchExtend(const SceneView *views
         int bucket = -1;
         if (i < n) {
             const uint32_t id = __float_as_uint(rq[2 * i + 1].w) >> kSlotBits;
-            bucket = extendOne(sv[id], B.q, rq, i);
+            bucket = extendOne<-2>(sv[id], B.q, rq, i);
             ++rays;
         }
         bucketAppend(B.q, bucket, i);
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kWaveBlock) batchShadow(const SceneView *views
             slot = tag & kSlotMask;
             const uint32_t id = tag >> kSlotBits;
             ++cnt;
-            if (!occludedAny(sv[id], xyz(s0), xyz(s1), s0.w)) {
+            if (!occludedAny<-2>(sv[id], xyz(s0), xyz(s1), s0.w)) {
                 B.outR[slot] += c.x;
                 B.outG[slot] += c.y;
                 B.outB[slot] += c.z;

@@ -28,6 +28,7 @@ struct pg3gpu_ctx {
     uint32_t kindMask = 0;               // material kinds of the scene (bit per kind)
     uint32_t numPointLights = 0;
     uint32_t *dBvhCodes = nullptr, *dBvhIds = nullptr;   // sorted Morton codes / primitive ids of the LBVH
+    const pg3::BvhNode *dBvhBinary = nullptr;             // its binary nodes (view.bvh may hold the 4-wide tree)
     double *dSum = nullptr, *dSumsq = nullptr;
     float *dOut[3] = {nullptr, nullptr, nullptr};
     uint64_t outCapacity = 0;            // paths per launch chunk

@@ -59,6 +59,15 @@ struct BvhNode {
     float4 hi_r;              // right child box max xyz, unused
 };
 
+// A node of the 4-wide BVH collapsed from the binary LBVH (every node takes its binary node's
+// grandchildren): the boxes of its up to 4 children coordinate-major, one float4 per bound, so
+// the four slab tests read 6 vector loads; child ids >= 0 are nodes, < 0 ~primitive, INT_MIN none.
+struct BvhNode4 {
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4 child;
+    float4 pad;
+};
+
 // Steerable sampler tables (host build in pg3_steerable.cpp, sampling in pg3_steer.cuh).
 struct SteerView {
     const float4 *vdir;       // per vertex: unit direction xyz (w: the antipodal vertex, uniform levels)
@@ -92,9 +101,9 @@ struct SceneView {
     uint32_t ntri, nsph;
 
     // acceleration structure (null when the list loop is used)
-    const BvhNode *bvh;
+    const BvhNode *bvh;       // useBvh 1: the binary LBVH; 2: BvhNode4 records (the 4-wide BVH)
     uint32_t bvhRoot;         // root node id (valid when nprims > 1)
-    int useBvh;
+    int useBvh;               // 0: the primitive list, 1: the binary LBVH, 2: the 4-wide BVH
 
     // materials and lights
     const DevMaterial *mats;

@@ -9,6 +9,8 @@
 // towards the lower primitive index exactly as the list loop breaks them.
 #pragma once
 
+#include <climits>
+
 #include "pg3_device.cuh"
 
 namespace pg3 {
@@ -142,13 +144,157 @@ PG3_DI bool occludedBvh(const SceneView &S, float3 pt, float3 dir, float dist)
     return false;
 }
 
+// ------------------------------------------------------------------------------------------
+// 4-wide BVH (BvhNode4): half the levels of the binary tree, four slab tests per node from
+// coordinate-major boxes. The children's entry distances order the pushes (farthest first), so
+// the nearest inner child is visited next; leaves are tested as they are met, with the same tie
+// rule as the list loop, so both trees return the same hit.
+// ------------------------------------------------------------------------------------------
+PG3_DI const BvhNode4 *bvh4(const SceneView &S) { return reinterpret_cast<const BvhNode4 *>(S.bvh); }
+
+// Slab test of the 4 children of a wide node; mask bit k set when child k is hit (entry t in te[k]).
+PG3_DI uint32_t slabHit4(const BvhNode4 &n, float3 org, float3 inv, float tmin, float tmax, float te[4])
+{
+    const float lx[4] = {n.lox.x, n.lox.y, n.lox.z, n.lox.w}, hx[4] = {n.hix.x, n.hix.y, n.hix.z, n.hix.w};
+    const float ly[4] = {n.loy.x, n.loy.y, n.loy.z, n.loy.w}, hy[4] = {n.hiy.x, n.hiy.y, n.hiy.z, n.hiy.w};
+    const float lz[4] = {n.loz.x, n.loz.y, n.loz.z, n.loz.w}, hz[4] = {n.hiz.x, n.hiz.y, n.hiz.z, n.hiz.w};
+    const int ch[4] = {n.child.x, n.child.y, n.child.z, n.child.w};
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float t;
+        if (ch[k] != INT_MIN &&
+            slabHit(make_float3(lx[k], ly[k], lz[k]), make_float3(hx[k], hy[k], hz[k]), org, inv, tmin, tmax, t))
+            mask |= 1u << k;
+        te[k] = t;
+    }
+    return mask;
+}
+
+PG3_DI bool intersectBvh4(const SceneView &S, float3 org, float3 dir, float tmin, Hit &h)
+{
+    const uint32_t nprim = S.ntri + S.nsph;
+    float tmax = 1e36f;
+    int best = -1;
+    if (nprim == 1) {
+        if (hitPrim(S, 0, org, dir, tmin, tmax)) best = 0;
+        h.t = tmax; h.prim = best;
+        return best >= 0;
+    }
+    const float3 inv = make_float3(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
+    const BvhNode4 *nodes = bvh4(S);
+    int stack[kBvhStackSize];
+    int sp = 0;
+    int node = 0;
+    // a well-formed tree has fewer than nprim nodes, each visited at most once
+    for (uint32_t guard = 0;; ++guard) {
+        if (guard >= nprim) { atomicOr(S.errorFlag, kErrTraversalStack); break; }
+        const BvhNode4 nd = nodes[node];
+        float te[4];
+        const uint32_t mask = slabHit4(nd, org, inv, tmin, bvhPad(tmax), te);
+        const int ch[4] = {nd.child.x, nd.child.y, nd.child.z, nd.child.w};
+        // inner children hit, ordered by entry distance (at most 4: insertion into registers)
+        int id[4] = {-1, -1, -1, -1};
+        float dt[4] = {0.f, 0.f, 0.f, 0.f};
+        int cnt = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (!(mask & (1u << k))) continue;
+            if (ch[k] < 0) {
+                const uint32_t p = (uint32_t)(~ch[k]);
+                float t = tieBound(tmax, p, best);
+                if (hitPrim(S, p, org, dir, tmin, t)) { tmax = t; best = (int)p; }
+            } else {
+                // keep id/dt sorted nearest first
+                int c = ch[k];
+                float tc = te[k];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (j < cnt && tc < dt[j]) {
+                        const int ci = id[j];
+                        const float ct = dt[j];
+                        id[j] = c;
+                        dt[j] = tc;
+                        c = ci;
+                        tc = ct;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (j == cnt) { id[j] = c; dt[j] = tc; }
+                ++cnt;
+            }
+        }
+        // push the farther ones (farthest first), continue with the nearest
+#pragma unroll
+        for (int j = 3; j >= 1; --j) {
+            if (j < cnt) {
+                if (sp < kBvhStackSize) stack[sp++] = id[j];
+                else atomicOr(S.errorFlag, kErrTraversalStack);
+            }
+        }
+        if (cnt > 0) node = id[0];
+        else {
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    h.t = tmax;
+    h.prim = best;
+    return best >= 0;
+}
+
+PG3_DI bool occludedBvh4(const SceneView &S, float3 pt, float3 dir, float dist)
+{
+    const float3 org = pt + dir * kEpsRay;
+    const float tmax0 = dist - 2.f * kEpsRay;
+    const uint32_t nprim = S.ntri + S.nsph;
+    if (nprim == 1) { float t = tmax0; return hitPrim(S, 0, org, dir, 0.f, t); }
+    const float3 inv = make_float3(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
+    const BvhNode4 *nodes = bvh4(S);
+    int stack[kBvhStackSize];
+    int sp = 0;
+    int node = 0;
+    for (uint32_t guard = 0;; ++guard) {
+        if (guard >= nprim) { atomicOr(S.errorFlag, kErrTraversalStack); break; }
+        const BvhNode4 nd = nodes[node];
+        float te[4];
+        const uint32_t mask = slabHit4(nd, org, inv, 0.f, bvhPad(tmax0), te);
+        const int ch[4] = {nd.child.x, nd.child.y, nd.child.z, nd.child.w};
+        int next = -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (!(mask & (1u << k))) continue;
+            if (ch[k] < 0) {
+                float t = tmax0;
+                if (hitPrim(S, (uint32_t)(~ch[k]), org, dir, 0.f, t)) return true;
+            } else if (next < 0) next = ch[k];
+            else if (sp < kBvhStackSize) stack[sp++] = ch[k];
+            else atomicOr(S.errorFlag, kErrTraversalStack);
+        }
+        if (next < 0) {
+            if (sp == 0) break;
+            node = stack[--sp];
+        } else node = next;
+    }
+    return false;
+}
+
+// TRAV: 0 the primitive list, 1 the binary LBVH, 2 the 4-wide BVH; -1 reads S.useBvh; -2 reads it
+// among the list and the binary LBVH only (the batch pipeline, whose instances never use the wide
+// tree, keeps its query kernels free of the wide traversal's registers).
+template <int TRAV = -1>
 PG3_DI bool intersectClosest(const SceneView &S, float3 org, float3 dir, float tmin, Hit &h)
 {
-    return S.useBvh ? intersectBvh(S, org, dir, tmin, h) : intersectList(S, org, dir, tmin, h);
+    const int t = (TRAV >= 0) ? TRAV : (TRAV == -2 ? (S.useBvh ? 1 : 0) : S.useBvh);
+    return t == 2 ? intersectBvh4(S, org, dir, tmin, h)
+                  : t == 1 ? intersectBvh(S, org, dir, tmin, h) : intersectList(S, org, dir, tmin, h);
 }
+template <int TRAV = -1>
 PG3_DI bool occludedAny(const SceneView &S, float3 pt, float3 dir, float dist)
 {
-    return S.useBvh ? occludedBvh(S, pt, dir, dist) : occludedList(S, pt, dir, dist);
+    const int t = (TRAV >= 0) ? TRAV : (TRAV == -2 ? (S.useBvh ? 1 : 0) : S.useBvh);
+    return t == 2 ? occludedBvh4(S, pt, dir, dist) : t == 1 ? occludedBvh(S, pt, dir, dist) : occludedList(S, pt, dir, dist);
 }
 
 }  // namespace pg3

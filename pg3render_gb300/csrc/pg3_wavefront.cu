@@ -111,8 +111,22 @@ __global__ void __launch_bounds__(kWaveBlock) raygenKernel(const __grid_constant
 #ifndef PG3_QUERY_MIN_BLOCKS
 #define PG3_QUERY_MIN_BLOCKS 6
 #endif
+// ... for the binary LBVH, and for the 4-wide BVH, whose node records and sorted children need
+// more registers
+#ifndef PG3_LBVH_QUERY_MIN_BLOCKS
+#define PG3_LBVH_QUERY_MIN_BLOCKS 6
+#endif
+#ifndef PG3_BVH4_QUERY_MIN_BLOCKS
+#define PG3_BVH4_QUERY_MIN_BLOCKS 4
+#endif
+// TRAV: 0 the primitive list, 1 the binary LBVH, 2 the 4-wide BVH (SceneView::useBvh)
+constexpr int queryMinBlocks(int TRAV)
+{
+    return TRAV == 0 ? PG3_QUERY_MIN_BLOCKS : TRAV == 1 ? PG3_LBVH_QUERY_MIN_BLOCKS : PG3_BVH4_QUERY_MIN_BLOCKS;
+}
 
-__global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) extendKernel(const __grid_constant__ SceneView S, Queues Q, int cur,
+template <int TRAV>
+__global__ void __launch_bounds__(kWaveBlock, queryMinBlocks(TRAV)) extendKernel(const __grid_constant__ SceneView S, Queues Q, int cur,
                                                            DevStats *stats)
 {
     stageEntry();
@@ -131,7 +145,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) extendKernel
                 prefetchL1(rq + 2 * (size_t)(i + stride));
                 prefetchL1(rq + 2 * (size_t)(i + stride) + 1);
             }
-            bucket = extendOne(S, Q, rq, i);
+            bucket = extendOne<TRAV>(S, Q, rq, i);
             ++rays;
         }
         bucketAppend(Q, bucket, i);
@@ -218,8 +232,8 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
     flushBlockGrad<GRAD>(sGrad, S.nmat, G.gMat);
 }
 
-template <bool GRAD>
-__global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) shadowKernel(const __grid_constant__ SceneView S, Queues Q,
+template <bool GRAD, int TRAV>
+__global__ void __launch_bounds__(kWaveBlock, queryMinBlocks(TRAV)) shadowKernel(const __grid_constant__ SceneView S, Queues Q,
                                                            int cur, float *outR, float *outG, float *outB,
                                                            DevStats *stats, GradArgs G)
 {
@@ -249,7 +263,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_QUERY_MIN_BLOCKS) shadowKernel
             }
             const float4 s0 = rec[0], s1 = rec[1];
             ++cnt;
-            if (!occludedAny(S, xyz(s0), xyz(s1), s0.w)) {
+            if (!occludedAny<TRAV>(S, xyz(s0), xyz(s1), s0.w)) {
                 const float4 c = rec[2];
                 const uint32_t slot = __float_as_uint(s1.w) & kSlotMask;
                 outR[slot] += c.x;
@@ -328,7 +342,9 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
     Q.err = S.errorFlag;
     const uint32_t maxBounces = S.maxPL > 0 ? S.maxPL : kMaxPathLengthHard;
     // (gridBlocks is SMs x the shade kernels' 1024 threads per SM)
-    const int queryGrid = std::max(1, gridBlocks / (1024 / kWaveBlock)) * PG3_QUERY_MIN_BLOCKS;
+    const int trav = S.useBvh;
+    const int queryGrid = std::max(1, gridBlocks / (1024 / kWaveBlock)) *
+                          (trav == 2 ? queryMinBlocks(2) : trav == 1 ? queryMinBlocks(1) : queryMinBlocks(0));
     const size_t smem = GRAD ? 16 * (size_t)S.nmat : 0;
     cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(stream, &capturing);
@@ -348,7 +364,9 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
         for (uint32_t bounce = 0; bounce < maxBounces; ++bounce) {
             const int cur = bounce & 1;
             const bool pdl = capturing == cudaStreamCaptureStatusNone || pdlInCapture;
-            launchStage(pdl, extendKernel, queryGrid, 0, stream, S, Q, cur, stats);
+            if (trav == 2) launchStage(pdl, extendKernel<2>, queryGrid, 0, stream, S, Q, cur, stats);
+            else if (trav == 1) launchStage(pdl, extendKernel<1>, queryGrid, 0, stream, S, Q, cur, stats);
+            else launchStage(pdl, extendKernel<0>, queryGrid, 0, stream, S, Q, cur, stats);
             const int emk = (S.bgKind == kBgEnvMap) ? S.emSampler : kEmCosine;   // no map: constant/area paths
             const uint32_t b32 = (uint32_t)base;
             int shades;
@@ -360,7 +378,9 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
                 shades = launchShade<kEmSteerableAdaptive, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
             else
                 shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
-            launchStage(pdl, shadowKernel<GRAD>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
+            if (trav == 2) launchStage(pdl, shadowKernel<GRAD, 2>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
+            else if (trav == 1) launchStage(pdl, shadowKernel<GRAD, 1>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
+            else launchStage(pdl, shadowKernel<GRAD, 0>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
             *launches += 2 + shades;
             if (S.maxPL == 0 && (bounce & 7) == 7 && capturing == cudaStreamCaptureStatusNone) {
                 // roulette-ended paths: stop once the queue is empty (checked every 8 bounces)

@@ -17,7 +17,8 @@ import numpy as np
 from . import _lib
 from ._lib import (ALG_PATH_TRACING, ALG_PATH_TRACING_NAIVE, EM_CDF, EM_COSINE, EM_STEERABLE,  # noqa: F401
                    PIPELINE_AUTO, PIPELINE_MEGAKERNEL, PIPELINE_WAVEFRONT, STEER_WEIGHTS_POINT,
-                   STEER_WEIGHTS_PROJECTED, TRAVERSAL_AUTO, TRAVERSAL_BVH, TRAVERSAL_LIST, Pg3Error)
+                   STEER_WEIGHTS_PROJECTED, TRAVERSAL_AUTO, TRAVERSAL_BVH, TRAVERSAL_BVH4, TRAVERSAL_LIST,
+                   Pg3Error)
 
 def steerable_file_name(em_path, level, max_approx_error=5.0, bilinear=True):
     """The path under which the reference caches the steerable sampler of the map at em_path

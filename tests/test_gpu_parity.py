@@ -270,11 +270,26 @@ def test_against_reference_golden(name):
 
 
 def test_bvh_and_list_traversal_identical():
+    # the list loop, the binary LBVH and the 4-wide BVH collapsed from it return the same hits
     scene = S.cornell_box(24, 24)
     outs = []
-    for trav in (P.renderer.TRAVERSAL_LIST, P.renderer.TRAVERSAL_BVH):
+    for trav in (P.renderer.TRAVERSAL_LIST, P.renderer.TRAVERSAL_BVH, P.renderer.TRAVERSAL_BVH4):
         with P.GpuPathTracer(_cfg(scene, 8, traversal=trav), seed=5) as r:
             outs.append(r.render_samples(P.renderer.kPathTracing, 0, 4))
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("level", [3, 5])
+def test_wide_and_binary_bvh_identical_on_meshes(level):
+    # icosphere meshes (1288 and 20488 triangles): every closest-hit and any-hit query through the
+    # 4-wide BVH finds what the binary LBVH finds, so the samples agree bit for bit
+    scene = S.cornell_env_mesh(32, 32, 64, 32, level=level)
+    outs = []
+    for trav in (P.renderer.TRAVERSAL_BVH, P.renderer.TRAVERSAL_BVH4):
+        cfg = _cfg(scene, 12, P.renderer.kPathTracing, P.renderer.EM_STEERABLE, traversal=trav, rr_min_path_length=4)
+        with P.GpuPathTracer(cfg, seed=9) as r:
+            outs.append(r.render_samples(P.renderer.kPathTracing, 0, 8))
+            r.synchronize()   # no traversal-stack or guard flag
     assert np.array_equal(outs[0], outs[1])
 
 
