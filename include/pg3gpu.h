@@ -77,9 +77,10 @@ enum {
 enum { PG3GPU_BG_NONE = 0, PG3GPU_BG_CONSTANT = 1, PG3GPU_BG_ENVMAP = 2 };
 /* Environment-map light samplers (compile-time choice in src/hard_config.hxx:17-18, run-time here). */
 enum { PG3GPU_EM_CDF = 0, PG3GPU_EM_COSINE = 1, PG3GPU_EM_STEERABLE = 2 };
-/* Ray queries: AUTO takes the primitive list up to 32 primitives and the 4-wide BVH above; LIST
+/* Ray queries: AUTO takes the primitive list up to 32 primitives and the binary LBVH above; LIST
  * tests every primitive in order (the reference's GeometryList, src/scene_graph.hxx:33-82); BVH
- * the binary LBVH built on the device; BVH4 the 4-wide BVH collapsed from it (same hits). */
+ * the binary LBVH built on the device; BVH4 the 4-wide BVH collapsed from it (same hits; about 3%
+ * slower than the binary tree on a 40968-triangle mesh; batches use the binary tree). */
 enum { PG3GPU_TRAVERSAL_AUTO = 0, PG3GPU_TRAVERSAL_LIST = 1, PG3GPU_TRAVERSAL_BVH = 2, PG3GPU_TRAVERSAL_BVH4 = 3 };
 enum { PG3GPU_PIPELINE_AUTO = 0, PG3GPU_PIPELINE_MEGAKERNEL = 1, PG3GPU_PIPELINE_WAVEFRONT = 2 };
 
@@ -225,6 +226,14 @@ typedef struct pg3gpu_stats {
                                         (CUDA events on the context's stream) */
     uint64_t path_kernel_launches;   /* path-kernel launches since reset */
     uint64_t kernel_launches;        /* all kernel launches of this library since reset */
+    /* Lengths of the paths that ended (all reasons but the safety limit), as the reference's
+     * RendererIntrospectionData collects them (src/renderer.hxx:80-118): bin b counts lengths
+     * 2^b - 1 .. 2^(b+1) - 2, i.e. floor(log2(length + 1)) = b; a path that leaves to the
+     * background counts the length of its last vertex. Filled by the wavefront pipeline (algorithm
+     * 7, the default); the megakernel pipelines and batches leave them 0. */
+    uint64_t length_histogram[16];
+    uint32_t min_path_length;        /* shortest and longest of those lengths (0 / 0: none) */
+    uint32_t max_path_length;
 } pg3gpu_stats;
 
 typedef struct pg3gpu_ctx pg3gpu_ctx;

@@ -85,7 +85,9 @@ class Stats(ctypes.Structure):
                 ("terminated_by_background", ctypes.c_uint64), ("terminated_by_blocker", ctypes.c_uint64),
                 ("terminated_by_max_limit", ctypes.c_uint64), ("terminated_by_safety_limit", ctypes.c_uint64),
                 ("last_iteration_ms", ctypes.c_double), ("path_kernel_ms", ctypes.c_double),
-                ("path_kernel_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
+                ("path_kernel_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+                ("length_histogram", ctypes.c_uint64 * 16), ("min_path_length", ctypes.c_uint32),
+                ("max_path_length", ctypes.c_uint32)]
 
 
 class BatchTuning(ctypes.Structure):

@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
             const uint32_t npix = __ldg(&inst[id].npix);
             const uint32_t pixel = local % npix, sample = __ldg(&inst[id].sample0) + local / npix;
             float3 L;
-            shadeVertex<K, EMK, false>(sv[id], B.q, idx, r0, r1, stQ(B.q, cur) + 3 * (size_t)idx, slot, tag, pixel, sample,
+            shadeVertex<K, EMK, false, false>(sv[id], B.q, idx, r0, r1, stQ(B.q, cur) + 3 * (size_t)idx, slot, tag, pixel, sample,
                                        pc, o, L, G, nullptr, f3(0.f));
             if (!isZero(L)) {
                 B.outR[slot] += L.x;

@@ -138,6 +138,7 @@ struct SceneView {
 };
 
 // Per-launch counters (PathTerminationReason histogram + ray totals).
+constexpr int kLenBins = 16;   // path-length histogram bins: bin b holds lengths 2^b - 1 .. 2^(b+1) - 2
 struct DevStats {
     unsigned long long paths;
     unsigned long long extRays;
@@ -147,6 +148,8 @@ struct DevStats {
     unsigned long long byBlocker;
     unsigned long long byMax;
     unsigned long long bySafety;
+    unsigned long long lenHist[kLenBins];   // lengths of the paths ended by all but the safety limit
+    unsigned int minLenC, maxLen;           // ~(shortest length) (0: none yet) and the longest length
 };
 
 // Adjoint inputs and outputs of one path-replay launch (pg3_wave.cuh).

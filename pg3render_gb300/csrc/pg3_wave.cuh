@@ -232,7 +232,10 @@ struct ShadeOut {
 
 // acc: the path's radiance accumulated before this vertex (GRAD adjoint only).
 // st: the entry's path state record (3 float4).
-template <int K, int EMK, bool GRAD>
+// EARLY: append the shadow record where the light sample is taken (PG3_EARLY_SHADOW); a caller
+// that still edits the record after the vertex (the batch pipeline marks a path's last light
+// sample) takes it in `o` instead.
+template <int K, int EMK, bool GRAD, bool EARLY = (PG3_EARLY_SHADOW != 0)>
 PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float4 r0, float4 r1, const float4 *st,
                         uint32_t slot, uint32_t tag, uint32_t pixel, uint32_t sample, PathCounters &pc, ShadeOut &o,
                         float3 &L, const GradArgs &G, float *sGrad, float3 acc, const NextEntry &nx = NextEntry())
@@ -342,7 +345,7 @@ PG3_DI void shadeVertex(const SceneView &S, const Queues &Q, uint32_t idx, float
                         o.s4 = make_float4(e.x, e.y, e.z, __int_as_float(matId));
                     }
                 }
-                if (PG3_EARLY_SHADOW) {
+                if (EARLY) {
                     constexpr int SW = kShadowWords<GRAD>;
                     const uint32_t sp = activeAppend(&Q.cnt->shadow);
                     if (sp >= Q.cap) atomicOr(Q.err, kErrQueueOverflow);

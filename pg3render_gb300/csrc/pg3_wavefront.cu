@@ -179,10 +179,26 @@ constexpr int shadeMinBlocks(int K)
                                       : PG3_SHADE_MIN_BLOCKS;
 }
 
+// Path lengths of this launch's terminations into the histogram of the reference's introspection
+// data (RendererIntrospectionData::AddCorePathLength, src/renderer.hxx:80-118: bins of
+// floor(log2(length + 1)), the safety limit left out). Every path of a bounce has the same length.
+PG3_DI void countLengths(DevStats *st, uint32_t len, uint32_t n)
+{
+    const uint32_t s = __reduce_add_sync(0xffffffffu, n);
+    if ((threadIdx.x & 31) == 0 && s) {
+        const int bin = min(31 - __clz(len + 1), kLenBins - 1);
+        atomicAdd(&st->lenHist[bin], (unsigned long long)s);
+        atomicMax(&st->minLenC, ~len);
+        atomicMax(&st->maxLen, len);
+    }
+}
+
+// pathLen: the length of the paths whose vertices this bounce shades (bounce + 1)
 template <int K, int EMK, bool GRAD>
 __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
     shadeKernel(const __grid_constant__ SceneView S, Queues Q, int cur, uint32_t base0, uint32_t npix,
-                uint32_t sample0, float *outR, float *outG, float *outB, DevStats *stats, GradArgs G)
+                uint32_t sample0, float *outR, float *outG, float *outB, DevStats *stats, GradArgs G,
+                uint32_t pathLen)
 {
     extern __shared__ float sGrad[];
     stageEntry();
@@ -229,6 +245,8 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
     countWarp(&stats->byMax, pc.maxl);
     countWarp(&stats->bySafety, pc.safety);
     countWarp(&stats->byRR, pc.rr);
+    // a path leaving to the background has the length of its last vertex (src/path_tracer.hxx:428)
+    countLengths(stats, K < 0 ? pathLen - 1 : pathLen, pc.rr + pc.bg + pc.blocker + pc.maxl);
     flushBlockGrad<GRAD>(sGrad, S.nmat, G.gMat);
 }
 
@@ -304,10 +322,11 @@ Queues carve(void *scratch, uint64_t cap, bool grad)
 template <int K, int EMK, bool GRAD>
 void launchShadeKind(const SceneView &S, const Queues &Q, int cur, uint32_t base, uint32_t npix, uint32_t sample0,
                      float *r, float *g, float *b, DevStats *stats, int grid, size_t smem, const GradArgs &G,
-                     cudaStream_t st, bool pdl, int &launched)
+                     cudaStream_t st, bool pdl, int &launched, uint32_t pathLen)
 {
     const int blocks = std::max(1, grid / (1024 / kWaveBlock)) * 2 * shadeMinBlocks(K);
-    launchStage(pdl, shadeKernel<K, EMK, GRAD>, blocks, smem, st, S, Q, cur, base, npix, sample0, r, g, b, stats, G);
+    launchStage(pdl, shadeKernel<K, EMK, GRAD>, blocks, smem, st, S, Q, cur, base, npix, sample0, r, g, b, stats, G,
+                pathLen);
     ++launched;
 }
 
@@ -316,20 +335,20 @@ void launchShadeKind(const SceneView &S, const Queues &Q, int cur, uint32_t base
 template <int EMK, bool GRAD>
 int launchShade(const SceneView &S, uint32_t kindMask, const Queues &Q, int cur, uint32_t base, uint32_t npix,
                 uint32_t sample0, float *r, float *g, float *b, DevStats *stats, int grid, size_t smem,
-                const GradArgs &G, cudaStream_t st, bool pdl)
+                const GradArgs &G, cudaStream_t st, bool pdl, uint32_t pathLen)
 {
     int n = 0;
-    launchShadeKind<-1, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
+    launchShadeKind<-1, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n, pathLen);
     if (kindMask & (1u << kMatLambert))
-        launchShadeKind<kMatLambert, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
+        launchShadeKind<kMatLambert, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n, pathLen);
     if (kindMask & (1u << kMatGgxConductor))
-        launchShadeKind<kMatGgxConductor, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
+        launchShadeKind<kMatGgxConductor, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n, pathLen);
     if (kindMask & (1u << kMatGgxDielectric))
-        launchShadeKind<kMatGgxDielectric, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
+        launchShadeKind<kMatGgxDielectric, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n, pathLen);
     if (kindMask & (1u << kMatPhong))
-        launchShadeKind<kMatPhong, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
+        launchShadeKind<kMatPhong, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n, pathLen);
     if (kindMask & ((1u << kMatSmoothConductor) | (1u << kMatSmoothDielectric)))
-        launchShadeKind<kShadeSmooth, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n);
+        launchShadeKind<kShadeSmooth, EMK, GRAD>(S, Q, cur, base, npix, sample0, r, g, b, stats, grid, smem, G, st, pdl, n, pathLen);
     return n;
 }
 
@@ -371,13 +390,17 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
             const uint32_t b32 = (uint32_t)base;
             int shades;
             if (emk == kEmCdf)
-                shades = launchShade<kEmCdf, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
+                shades = launchShade<kEmCdf, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl,
+                                                                  bounce + 1);
             else if (emk == kEmSteerable)
-                shades = launchShade<kEmSteerable, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
+                shades = launchShade<kEmSteerable, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl,
+                                                                  bounce + 1);
             else if (emk == kEmSteerableAdaptive)
-                shades = launchShade<kEmSteerableAdaptive, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
+                shades = launchShade<kEmSteerableAdaptive, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl,
+                                                                  bounce + 1);
             else
-                shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl);
+                shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl,
+                                                                  bounce + 1);
             if (trav == 2) launchStage(pdl, shadowKernel<GRAD, 2>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
             else if (trav == 1) launchStage(pdl, shadowKernel<GRAD, 1>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
             else launchStage(pdl, shadowKernel<GRAD, 0>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);

@@ -170,7 +170,9 @@ class GpuPathTracer:
     def stats(self):
         s = _lib.Stats()
         _lib.check(self._L.pg3gpu_get_stats(self._ctx, ctypes.byref(s)), self._ctx)
-        return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+        out = {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+        out["length_histogram"] = list(s.length_histogram)
+        return out
 
     def reset_stats(self):
         _lib.check(self._L.pg3gpu_reset_stats(self._ctx), self._ctx)
@@ -320,7 +322,9 @@ class GpuBatch:
     def stats(self):
         s = _lib.Stats()
         self._check(self._L.pg3gpu_batch_get_stats(self._b, ctypes.byref(s)))
-        return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+        out = {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+        out["length_histogram"] = list(s.length_histogram)
+        return out
 
     def set_stream(self, stream):
         ptr = stream if isinstance(stream, int) else getattr(stream, "cuda_stream", stream)

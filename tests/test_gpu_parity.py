@@ -318,6 +318,33 @@ def test_stats_counts():
     assert st["terminated_by_max_limit"] > 0   # a closed box keeps many paths to the limit
 
 
+@pytest.mark.parametrize("maxpl,rr", [(8, 0), (12, 4), (0, 0)])
+def test_path_length_histogram(maxpl, rr):
+    # the reference's introspection data (src/renderer.hxx:80-118): every path ended by roulette,
+    # the background, a blocker or the length limit counts once, in bin floor(log2(length + 1))
+    scene = S.cornell_box(16, 16) if maxpl == 8 else S.cornell_env(16, 16, 64, 32)
+    with P.GpuPathTracer(_cfg(scene, maxpl, rr_min_path_length=rr), seed=3) as r:
+        r.RunIteration(P.renderer.kPathTracing, 0, 16)
+        st = r.stats()
+    hist = st["length_histogram"]
+    ended = (st["terminated_by_background"] + st["terminated_by_blocker"] + st["terminated_by_max_limit"]
+             + st["terminated_by_russian_roulette"])
+    assert sum(hist) == ended > 0
+    assert 1 <= st["min_path_length"] <= st["max_path_length"]
+    nz = [b for b, c in enumerate(hist) if c]
+    assert 2 ** nz[0] - 1 <= st["min_path_length"] and st["max_path_length"] <= 2 ** (nz[-1] + 1) - 2
+    if maxpl:
+        assert st["max_path_length"] == maxpl                        # paths reach the limit
+        assert hist[int(np.log2(maxpl + 1))] >= st["terminated_by_max_limit"]
+    else:
+        assert st["terminated_by_russian_roulette"] > 0 and st["max_path_length"] > 4
+    # the megakernel pipeline leaves the histogram empty
+    with P.GpuPathTracer(_cfg(scene, maxpl, rr_min_path_length=rr, pipeline=P.renderer.PIPELINE_MEGAKERNEL),
+                         seed=3) as r:
+        r.RunIteration(P.renderer.kPathTracing, 0, 2)
+        assert sum(r.stats()["length_histogram"]) == 0
+
+
 def test_chunked_launches_match_single_launch():
     scene = S.cornell_box(16, 16)
     outs = []
