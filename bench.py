@@ -53,7 +53,7 @@ BYTES_PER_PATH = 72 + 36
 # DRAM bytes (read + write) per camera path of one launch chunk, measured by ncu over all stage
 # kernels of one step of the 128x128 x 64 spp case of this workload (one chunk of 2^20 paths);
 # the chunk's traffic grows with its paths.
-NCU_TRAFFIC_PER_PATH = 1043.8
+NCU_TRAFFIC_PER_PATH = 1037.6
 
 
 def parse():
@@ -77,7 +77,8 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the batched (64 scenes), forward+adjoint and inverse-rendering measurements")
     ap.add_argument("--only-secondary", default=None,
-                    choices=["batched", "differentiable", "inverse_rendering", "mesh_bvh", "per_iteration"],
+                    choices=["batched", "differentiable", "inverse_rendering", "mesh_bvh", "per_iteration",
+                             "adaptive_sampler"],
                     help="run one secondary measurement alone and print its JSON (profiling captures)")
     ap.add_argument("--mesh-side", type=int, default=512, help="image side of the LBVH mesh measurement")
     ap.add_argument("--mesh-spp", type=int, default=64, help="samples per pixel of the LBVH mesh measurement")
@@ -193,6 +194,15 @@ def cpu_baseline(scene, sampler, threads=None, iters=1):
                 "sample": "%d spp of the %dx%d scene" % (spp, WIDTH, HEIGHT)}
 
 
+ADAPTIVE_DEFAULT = (4, 9, 5.0)   # the reference's default steerable build: levels 4-9, error 5
+
+
+def adaptive_kw(levels):
+    if not levels:
+        return {}
+    return dict(steer_subdiv_level=levels[0], steer_max_subdiv_level=levels[1], steer_max_approx_error=levels[2])
+
+
 def matched_quality(gpu_value, cpu_value, steer_weights, spps=(16, 256), renders=(16, 8)):
     """Per-sample quality of the two renderers on the headline scene (its full 1024x512 sky) at
     64x64 pixels: the relative MSE, mean over pixel channels of (x - c)^2 / (c^2 + 0.01), of
@@ -218,13 +228,17 @@ def matched_quality(gpu_value, cpu_value, steer_weights, spps=(16, 256), renders
     side = conv.shape[0]
     sc = S.cornell_env(side, side, EM_W, EM_H, em_seed=7)
     sc.env_map = golden["env_map"]   # the map the reference rendered (bit for bit)
-    gpu_cfgs = {"steerable_point": (R.EM_STEERABLE, R.STEER_WEIGHTS_POINT),
-                "steerable_projected": (R.EM_STEERABLE, R.STEER_WEIGHTS_PROJECTED), "cdf": (R.EM_CDF, 0)}
+    # the third entry: an adaptive triangulation with the reference's default build parameters
+    # (levels 4-9, error 5) instead of the uniform 1280 triangles
+    gpu_cfgs = {"steerable_point": (R.EM_STEERABLE, R.STEER_WEIGHTS_POINT, None),
+                "steerable_projected": (R.EM_STEERABLE, R.STEER_WEIGHTS_PROJECTED, None),
+                "steerable_adaptive_projected": (R.EM_STEERABLE, R.STEER_WEIGHTS_PROJECTED, ADAPTIVE_DEFAULT),
+                "cdf": (R.EM_CDF, 0, None)}
 
     def gpu_image(key, seed, n):
-        em, w = gpu_cfgs[key]
+        em, w, ad = gpu_cfgs[key]
         cfg = P.Config(scene=sc, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM, em_sampler=em,
-                       steer_weights=w)
+                       steer_weights=w, **adaptive_kw(ad))
         with P.GpuPathTracer(cfg, seed=seed) as r:
             r.RunIteration(R.kPathTracing, 0, n)
             return r.framebuffer()[0]
@@ -372,6 +386,22 @@ def run_gpu(args, rank, world, local_rank):
         e2e = {"value": round(whole_job_value(world, e2e_steps, paths_per_step, e2e_s), 3), "unit": UNIT,
                "h2d_bytes_per_step": int(desc_bytes), "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                "image_mean": [round(float(x), 5) for x in img.mean(axis=(0, 1))]}
+        # where an end-to-end step's time goes (measured after the timed loop, host clock): create
+        # (scene and map upload, sampler tables), render + framebuffer readback, destroy
+        parts = {"create_ms": [], "render_and_read_ms": [], "destroy_ms": []}
+        for k in range(2):
+            t0 = time.perf_counter()
+            rr = P.GpuPathTracer(cfg, device=local_rank)
+            t1 = time.perf_counter()
+            rr.RunIteration(R.kPathTracing, sample_base + k * SPP, SPP)
+            rr.GetFramebuffer()
+            t2 = time.perf_counter()
+            rr.close()
+            t3 = time.perf_counter()
+            parts["create_ms"].append((t1 - t0) * 1e3)
+            parts["render_and_read_ms"].append((t2 - t1) * 1e3)
+            parts["destroy_ms"].append((t3 - t2) * 1e3)
+        e2e["breakdown"] = {k: round(statistics.median(v), 3) for k, v in parts.items()}
 
     if rank != 0:
         return None
@@ -548,18 +578,23 @@ def differentiable_metric(steps=5):
     return out
 
 
+ENV_SMOOTHNESS = 1.0   # weight of the log-texel smoothness penalty in the third inverse-rendering run
+
+
 def inverse_metric():
     """The inverse-rendering configuration (128x128 x 16 spp forward + adjoint per iteration, 500
     Adam steps, one CUDA graph per iteration) three ways: map and materials jointly (the
     configuration), materials with the map at its hidden values (the materials are then
-    identifiable: albedo times illumination is a scale ambiguity), and jointly with a smoothness
-    penalty on the log texels."""
+    identifiable: albedo times illumination is a scale ambiguity), with the primal residual and the
+    adjoint on independent samples (the L2 loss of one noisy render favours darker renders), and
+    jointly with a smoothness penalty on the log texels."""
     from pg3render_gb300 import inverse
     r = inverse.run()
     r["metric"] = "inverse rendering: 500 Adam steps, one CUDA graph per iteration"
     r.pop("loss_trace", None)
     for key, kw in (("materials_with_hidden_map", dict(optimize_env=False)),
-                    ("joint_smooth_map", dict(env_smoothness=1e-3))):
+                    ("materials_with_hidden_map_decorrelated", dict(optimize_env=False, decorrelate=True)),
+                    ("joint_smooth_map_decorrelated", dict(env_smoothness=ENV_SMOOTHNESS, decorrelate=True))):
         x = inverse.run(**kw)
         r[key] = {k: x[k] for k in ("before", "after", "iteration_ms", "materials_true", "materials_found")}
         r[key]["errors_fall"] = {g: x["after"][g] < x["before"][g] for g in ("albedo_mae", "alpha_abs_err", "env_rel_l1")
@@ -656,11 +691,44 @@ def per_iteration_metric(iters=256, reps=3):
     return out
 
 
+def adaptive_sampler_metric(reps=3):
+    """The headline scene and workload (512x512 x 256 spp, max path length 12, roulette from length
+    4, the 1024x512 sky) with the steerable sampler over the reference's default adaptive
+    triangulation (levels 4-9, error 5, projected vertex weights) instead of 1280 uniform triangles;
+    device time of one call, median of reps; the triangulation's build is part of create."""
+    import torch
+    import pg3render_gb300 as P
+    R = P.renderer
+    sc = build_scene()
+    cfg = P.Config(scene=sc, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM, em_sampler=R.EM_STEERABLE,
+                   steer_weights=R.STEER_WEIGHTS_PROJECTED, **adaptive_kw(ADAPTIVE_DEFAULT))
+    t0 = time.perf_counter()
+    r = P.GpuPathTracer(cfg)
+    create_ms = (time.perf_counter() - t0) * 1e3
+    try:
+        r.RunIteration(R.kPathTracing, 0, SPP)
+        r.synchronize()
+        ts = []
+        for rep in range(reps):
+            a, b = _events()
+            a.record()
+            r.RunIteration(R.kPathTracing, (rep + 1) * SPP, SPP)
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+    finally:
+        r.close()
+    ms = statistics.median(ts)
+    return {"metric": "Msamples/s (adaptive steerable triangulation)", "levels": list(ADAPTIVE_DEFAULT),
+            "msamples_per_s": round(WIDTH * HEIGHT * SPP / ms / 1e3, 1), "ms_per_run": round(ms, 3),
+            "create_ms": round(create_ms, 2)}
+
+
 def secondary_metrics(only=None):
     out = {}
     for name, fn in (("batched", batched_metric), ("differentiable", differentiable_metric),
                      ("inverse_rendering", inverse_metric), ("mesh_bvh", mesh_metric),
-                     ("per_iteration", per_iteration_metric)):
+                     ("per_iteration", per_iteration_metric), ("adaptive_sampler", adaptive_sampler_metric)):
         if only and name != only:
             continue
         try:

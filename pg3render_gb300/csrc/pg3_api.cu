@@ -71,18 +71,77 @@ int upload(pg3gpu_ctx *ctx, T **p, const std::vector<T> &v)
     return PG3GPU_OK;
 }
 
+// The per-sample outputs and the wavefront queues of a context (hundreds of MB to 4.6 GiB) come
+// from a memory pool of the library per device that keeps up to kPoolKeepBytes of freed memory:
+// contexts created one after another (a render server, an end-to-end loop of create, render,
+// read, destroy) reuse the previous context's buffers instead of a device allocation and free of
+// that size each time. Stream-ordered on the context's stream; while that stream is being
+// captured into a graph, plain allocations are used.
+#ifndef PG3_QUEUE_POOL
+#define PG3_QUEUE_POOL 1
+#endif
+constexpr uint64_t kPoolKeepBytes = 8ull << 30;
+constexpr int kMaxPoolDevices = 64;
+cudaMemPool_t g_queuePools[kMaxPoolDevices] = {};
+std::mutex g_queuePoolMutex;
+
+cudaMemPool_t queuePool(int device)
+{
+    if (device < 0 || device >= kMaxPoolDevices) return nullptr;
+    std::lock_guard<std::mutex> lock(g_queuePoolMutex);
+    if (!g_queuePools[device]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        uint64_t keep = kPoolKeepBytes;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_queuePools[device] = pool;
+    }
+    return g_queuePools[device];
+}
+
+template <typename T>
+int bigAlloc(pg3gpu_ctx *ctx, T **p, size_t count)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaMemPool_t pool = PG3_QUEUE_POOL ? queuePool(ctx->device) : nullptr;
+    if (pool && cudaStreamIsCapturing(ctx->stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+        void *q = nullptr;
+        const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+        PG3_CUDA(ctx, cudaMallocFromPoolAsync(&q, bytes, pool, ctx->stream));
+        ctx->pooled.push_back(q);
+        *p = reinterpret_cast<T *>(q);
+        return PG3GPU_OK;
+    }
+    return devAlloc(ctx, p, count);
+}
+
+void bigFree(pg3gpu_ctx *ctx, void *p)
+{
+    if (!p) return;
+    auto it = std::find(ctx->pooled.begin(), ctx->pooled.end(), p);
+    if (it != ctx->pooled.end()) {
+        cudaFreeAsync(p, ctx->stream);
+        ctx->pooled.erase(it);
+    } else
+        ctxFree(ctx, p);
+}
+
 int ensureOutput(pg3gpu_ctx *ctx, uint64_t paths)
 {
     if (paths <= ctx->outCapacity) return PG3GPU_OK;
     for (auto &p : ctx->dOut) {
-        if (p) {
-            cudaFree(p);
-            ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), (void *)p), ctx->allocs.end());
-            p = nullptr;
-        }
+        bigFree(ctx, p);
+        p = nullptr;
     }
     for (auto &p : ctx->dOut) {
-        int st = devAlloc(ctx, &p, paths);
+        int st = bigAlloc(ctx, &p, paths);
         if (st) return st;
     }
     ctx->outCapacity = paths;
@@ -99,11 +158,11 @@ int ensureWave(pg3gpu_ctx *ctx, uint64_t paths)
     const uint64_t cap = ctx->opts.max_paths_in_flight ? ctx->opts.max_paths_in_flight : (1ull << 24);
     const uint64_t want = std::min<uint64_t>(cap, paths);
     if (ctx->dWave && ctx->waveCapacity >= want) return PG3GPU_OK;
-    ctxFree(ctx, ctx->dWave);
+    bigFree(ctx, ctx->dWave);
     ctx->dWave = nullptr;
     ctx->waveCapacity = 0;
     char *w = nullptr;
-    if (int st = devAlloc(ctx, &w, wavefrontBytes(want, false))) return st;
+    if (int st = bigAlloc(ctx, &w, wavefrontBytes(want, false))) return st;
     ctx->dWave = w;
     ctx->waveCapacity = want;
     return PG3GPU_OK;
@@ -370,6 +429,10 @@ int pg3gpu_destroy(pg3gpu_ctx *ctx)
     if (ctx->callGraphExec) cudaGraphExecDestroy(ctx->callGraphExec);
     if (ctx->callGraph) cudaGraphDestroy(ctx->callGraph);
     if (ctx->graphStream) cudaStreamDestroy(ctx->graphStream);
+    if (!ctx->pooled.empty()) {
+        for (void *p : ctx->pooled) cudaFreeAsync(p, ctx->stream);   // back to the library's pool
+        cudaStreamSynchronize(ctx->stream);
+    }
     for (void *p : ctx->allocs) cudaFree(p);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);

@@ -23,6 +23,7 @@ struct pg3gpu_ctx {
     pg3gpu_options opts{};
     SceneView view{};
     std::vector<void *> allocs;
+    std::vector<void *> pooled;          // allocations from the library's queue pool (pg3_api.cu)
     uint32_t W = 0, H = 0;
     uint32_t nmat = 0;
     uint32_t kindMask = 0;               // material kinds of the scene (bit per kind)

@@ -201,8 +201,9 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
                 uint32_t pathLen)
 {
     extern __shared__ float sGrad[];
-    stageEntry();
+    // the block's gradient sums read nothing the previous stage writes: cleared before the wait
     initBlockGrad<GRAD>(sGrad, S.nmat);
+    stageEntry();
     sample0 = sampleBase<GRAD>(sample0, G);
     constexpr int kBucket = bucketOfShade(K);
     const uint32_t n = Q.cnt->bucket[kBucket];
@@ -257,6 +258,7 @@ __global__ void __launch_bounds__(kWaveBlock, queryMinBlocks(TRAV)) shadowKernel
 {
     constexpr int SW = kShadowWords<GRAD>;
     extern __shared__ float sGrad[];
+    initBlockGrad<GRAD>(sGrad, S.nmat);   // before the wait: reads nothing the shade stage writes
     stageEntry();
     // this bounce's ray queue and buckets are consumed (extend and the shade kernels have
     // completed): their counters start at zero for the next bounce's appends. No stage of the
@@ -265,7 +267,6 @@ __global__ void __launch_bounds__(kWaveBlock, queryMinBlocks(TRAV)) shadowKernel
         if (threadIdx.x == 0) Q.cnt->ray[cur] = 0;
         else Q.cnt->bucket[threadIdx.x - 1] = 0;
     }
-    initBlockGrad<GRAD>(sGrad, S.nmat);
     const uint32_t n = Q.cnt->shadow;
     uint32_t cnt = 0;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -317,14 +318,17 @@ Queues carve(void *scratch, uint64_t cap, bool grad)
     return q;
 }
 
-// One shade kernel: grid = SMs x 1024 / kWaveBlock on entry; the kernel gets two waves of the
-// blocks it is compiled to keep resident per SM.
+// One shade kernel: grid = SMs x 1024 / kWaveBlock on entry; the kernel gets PG3_SHADE_WAVES waves
+// of the blocks it is compiled to keep resident per SM.
+#ifndef PG3_SHADE_WAVES
+#define PG3_SHADE_WAVES 1
+#endif
 template <int K, int EMK, bool GRAD>
 void launchShadeKind(const SceneView &S, const Queues &Q, int cur, uint32_t base, uint32_t npix, uint32_t sample0,
                      float *r, float *g, float *b, DevStats *stats, int grid, size_t smem, const GradArgs &G,
                      cudaStream_t st, bool pdl, int &launched, uint32_t pathLen)
 {
-    const int blocks = std::max(1, grid / (1024 / kWaveBlock)) * 2 * shadeMinBlocks(K);
+    const int blocks = std::max(1, grid / (1024 / kWaveBlock)) * PG3_SHADE_WAVES * shadeMinBlocks(K);
     launchStage(pdl, shadeKernel<K, EMK, GRAD>, blocks, smem, st, S, Q, cur, base, npix, sample0, r, g, b, stats, G,
                 pathLen);
     ++launched;

@@ -12,6 +12,12 @@ One view of the box does not determine a sky: albedo times illumination is a sca
 and the map absorbs the render noise. ``optimize_env=False`` keeps the map at its hidden values
 (the materials are then identifiable); ``env_smoothness`` adds a penalty on the squared
 differences of neighbouring log texels, which keeps the recovered map from fitting noise.
+
+The L2 loss of a noisy render is biased: E[(X - t)^2] = (E[X] - t)^2 + Var[X], and the variance
+term pulls the parameters towards darker, less noisy renders (albedos come out low). With
+``decorrelate`` every iteration renders a second, independent estimate for the residual and
+back-propagates 2 (X_a - t) dX_b/dparameters, whose expectation is the gradient of
+(E[X] - t)^2 alone (one forward pass more per iteration).
 """
 import math
 import time
@@ -35,7 +41,7 @@ def _hidden_scene(side, em, seed):
 
 
 def run(steps=500, lr=1e-2, side=128, spp=16, target_spp=1024, em=(256, 128), seed=0, max_path_length=12,
-        rr_min_path_length=4, eval_spp=256, optimize_env=True, env_smoothness=0.0, device=0):
+        rr_min_path_length=4, eval_spp=256, optimize_env=True, env_smoothness=0.0, decorrelate=False, device=0):
     """Returns a dict: losses against the hidden-parameter render, parameter errors before and
     after, and the device time per iteration. With optimize_env False the map keeps its hidden
     values and only the materials are recovered; env_smoothness > 0 weights the penalty on
@@ -75,13 +81,24 @@ def run(steps=500, lr=1e-2, side=128, spp=16, target_spp=1024, em=(256, 128), se
 
         def iteration():
             opt.zero_grad(set_to_none=False)
-            img = diff.render(dr, mats, torch.exp(theta) if optimize_env else None, iteration=0, spp=spp)
-            loss = ((img - target) ** 2).mean()
-            total = loss
+            env = torch.exp(theta) if optimize_env else None
+            if decorrelate:
+                with torch.no_grad():
+                    dr.set_params(mats.detach(), None if env is None else env.detach())
+                    img_a = torch.empty_like(target)
+                    dr.forward_into(img_a, 1 << 22, spp)   # samples disjoint from img's
+                img = diff.render(dr, mats, env, iteration=0, spp=spp)
+                resid = img_a - target
+                loss = (resid ** 2).mean()
+                total = (2.0 * resid * img).mean()         # its gradient: 2 (X_a - t) dX_b / dtheta
+            else:
+                img = diff.render(dr, mats, env, iteration=0, spp=spp)
+                loss = ((img - target) ** 2).mean()
+                total = loss
             if optimize_env and env_smoothness > 0:
                 dv = theta[1:] - theta[:-1]
                 du = theta[:, 1:] - theta[:, :-1]
-                total = loss + env_smoothness * ((dv ** 2).mean() + (du ** 2).mean())
+                total = total + env_smoothness * ((dv ** 2).mean() + (du ** 2).mean())
             total.backward()
             opt.step()
             with torch.no_grad():
@@ -127,7 +144,7 @@ def run(steps=500, lr=1e-2, side=128, spp=16, target_spp=1024, em=(256, 128), se
         after = evaluate()
         ms = t0.elapsed_time(t1) / max(1, steps - 3)
         return dict(steps=steps, side=side, spp=spp, target_spp=target_spp, env=list(e_true.shape),
-                    optimize_env=optimize_env, env_smoothness=env_smoothness,
+                    optimize_env=optimize_env, env_smoothness=env_smoothness, decorrelate=decorrelate,
                     iteration_ms=ms, wall_s=wall, before=before, after=after, loss_trace=losses,
                     materials_true=m_true[lam + ggx].tolist(), materials_found=mats.detach().cpu().numpy()[lam + ggx].tolist())
     finally:

@@ -305,8 +305,13 @@ def test_inverse_rendering_loop_recovers_parameters():
     # (the loss is evaluated with 256 spp against a 512-spp target: it keeps their noise)
     assert r["after"]["loss"] < 0.8 * r["before"]["loss"], r
     assert r["after"]["albedo_mae"] < 0.5 * r["before"]["albedo_mae"], r
-    assert r["after"]["alpha_abs_err"] < r["before"]["alpha_abs_err"], r
     assert np.isfinite(r["iteration_ms"]) and r["iteration_ms"] > 0
+    # with the residual and the adjoint on independent samples the noisy loss's pull towards
+    # darker renders is gone: albedos and roughnesses come out close to the hidden values
+    r = inverse.run(steps=200, side=48, spp=8, target_spp=512, em=(64, 32), lr=1e-2, eval_spp=256,
+                    optimize_env=False, decorrelate=True)
+    assert r["after"]["albedo_mae"] < 0.2 * r["before"]["albedo_mae"], r
+    assert r["after"]["alpha_abs_err"] < 0.5 * r["before"]["alpha_abs_err"], r
     # with the map as well, the loss against the hidden-parameter render still falls
     r = inverse.run(steps=200, side=48, spp=8, target_spp=512, em=(64, 32), lr=1e-2, eval_spp=256)
     assert r["after"]["loss"] < 0.8 * r["before"]["loss"], r
