@@ -430,6 +430,16 @@ def run_gpu(args, rank, world, local_rank):
                 line["cpu_baseline"]["matched_quality"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if world == 1 and not args.no_secondary:
         line["secondary"] = secondary_metrics()
+        # the same equal-quality figure for the adaptive triangulation: its own Msamples/s and its
+        # relative MSE at the benchmark's samples per pixel
+        mq = line.get("cpu_baseline", {}).get("matched_quality", {})
+        ad = line["secondary"].get("adaptive_sampler", {})
+        last = mq.get("rel_mse_at_%dspp" % SPP, {})
+        if ad.get("msamples_per_s") and last.get("gpu_steerable_adaptive_projected") and \
+                last.get("cpu_reference_steerable"):
+            ratio = last["cpu_reference_steerable"] / last["gpu_steerable_adaptive_projected"]
+            ad["rel_mse_ratio_cpu_over_gpu_at_%dspp" % SPP] = round(ratio, 4)
+            ad["equal_quality_speedup"] = round(ad["msamples_per_s"] / line["cpu_baseline"]["value"] * ratio, 2)
     return line
 
 

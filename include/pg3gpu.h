@@ -248,6 +248,11 @@ void pg3gpu_default_options(pg3gpu_options *opts);
  * Replaces AbstractRenderer's constructor (src/renderer.hxx:236-240). */
 int pg3gpu_create(const pg3gpu_scene *scene, const pg3gpu_options *opts, int device, pg3gpu_ctx **out);
 
+/* Frees the context. Its wavefront queues and per-sample outputs come from a device memory
+ * pool of the library (one per device) that keeps up to 8 GiB of freed memory for the next
+ * context, so a loop of create, render, destroy reuses them instead of allocating each time;
+ * that memory stays reserved on the device until the process ends (build option
+ * PG3_QUEUE_POOL=0 allocates and frees per context). */
 int pg3gpu_destroy(pg3gpu_ctx *ctx);
 
 /* All work of the context is issued on this CUDA stream (cudaStream_t as void*;
