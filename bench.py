@@ -21,7 +21,11 @@ A step renders the whole workload once (512*512*256 = 67,108,864 camera paths).
            scenes/s (64 seeded variants in one persistent launch vs a loop of
            single-scene launches), forward+adjoint ms/iteration with a
            finite-difference check of the gradient, and the inverse-rendering loop
-           (500 Adam steps, one CUDA graph per iteration).
+           (500 Adam steps, one CUDA graph per iteration); and the headline
+           workload's variants: the LBVH on a mesh, one call per iteration, the
+           adaptive triangulation, the CDF and cosine samplers, with the
+           equal-quality speedup of every GPU sampler against the reference's
+           steerable and CDF samplers.
 --impl reference times that CPU renderer alone as the main line.
 With N > 1 (torchrun) every rank renders its own sample range of the same
 workload (weak scaling, no collective on the data path).
@@ -78,7 +82,7 @@ def parse():
                     help="skip the batched (64 scenes), forward+adjoint and inverse-rendering measurements")
     ap.add_argument("--only-secondary", default=None,
                     choices=["batched", "differentiable", "inverse_rendering", "mesh_bvh", "per_iteration",
-                             "adaptive_sampler"],
+                             "adaptive_sampler", "samplers"],
                     help="run one secondary measurement alone and print its JSON (profiling captures)")
     ap.add_argument("--mesh-side", type=int, default=512, help="image side of the LBVH mesh measurement")
     ap.add_argument("--mesh-spp", type=int, default=64, help="samples per pixel of the LBVH mesh measurement")
@@ -233,7 +237,8 @@ def matched_quality(gpu_value, cpu_value, steer_weights, spps=(16, 256), renders
     gpu_cfgs = {"steerable_point": (R.EM_STEERABLE, R.STEER_WEIGHTS_POINT, None),
                 "steerable_projected": (R.EM_STEERABLE, R.STEER_WEIGHTS_PROJECTED, None),
                 "steerable_adaptive_projected": (R.EM_STEERABLE, R.STEER_WEIGHTS_PROJECTED, ADAPTIVE_DEFAULT),
-                "cdf": (R.EM_CDF, 0, None)}
+                "cdf": (R.EM_CDF, 0, None),
+                "cosine": (R.EM_COSINE, 0, None)}
 
     def gpu_image(key, seed, n):
         em, w, ad = gpu_cfgs[key]
@@ -422,6 +427,13 @@ def run_gpu(args, rank, world, local_rank):
     line["clocks"] = clk.summary()
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(scene, sampler, iters=args.cpu_iters)
+        if sampler == "steerable" and not args.no_secondary:
+            # the reference's CDF sampler on the same cores, for the per-sampler comparison
+            try:
+                line["cpu_baseline"]["cdf_value"] = cpu_baseline(scene, "cdf", iters=max(1, args.cpu_iters // 2))["value"]
+            except Exception as e:   # reported, never hidden
+                line["cpu_baseline"]["cdf_value"] = None
+                line["cpu_baseline"]["cdf_error"] = "%s: %s" % (type(e).__name__, e)
         if sampler == "steerable":
             try:
                 line["cpu_baseline"]["matched_quality"] = matched_quality(value, line["cpu_baseline"]["value"],
@@ -440,6 +452,8 @@ def run_gpu(args, rank, world, local_rank):
             ratio = last["cpu_reference_steerable"] / last["gpu_steerable_adaptive_projected"]
             ad["rel_mse_ratio_cpu_over_gpu_at_%dspp" % SPP] = round(ratio, 4)
             ad["equal_quality_speedup"] = round(ad["msamples_per_s"] / line["cpu_baseline"]["value"] * ratio, 2)
+        if "cpu_baseline" in line and sampler == "steerable":
+            line["secondary"]["sampler_comparison"] = sampler_comparison(line)
     return line
 
 
@@ -734,11 +748,67 @@ def adaptive_sampler_metric(reps=3):
             "create_ms": round(create_ms, 2)}
 
 
+def sampler_metric(reps=3):
+    """The headline workload (512x512 x 256 spp, max path length 12, roulette from length 4, the
+    1024x512 sky) with the CDF and the cosine environment-map samplers instead of the steerable one:
+    device time of one call, median of reps."""
+    import torch
+    import pg3render_gb300 as P
+    R = P.renderer
+    sc = build_scene()
+    out = {"metric": "Msamples/s per environment-map sampler (headline workload)"}
+    for name, em in (("cdf", R.EM_CDF), ("cosine", R.EM_COSINE)):
+        cfg = P.Config(scene=sc, max_path_length=MAX_PATH, rr_min_path_length=RR_FROM, em_sampler=em)
+        with P.GpuPathTracer(cfg) as r:
+            r.RunIteration(R.kPathTracing, 0, SPP)
+            r.synchronize()
+            ts = []
+            for rep in range(reps):
+                a, b = _events()
+                a.record()
+                r.RunIteration(R.kPathTracing, (rep + 1) * SPP, SPP)
+                b.record()
+                torch.cuda.synchronize()
+                ts.append(a.elapsed_time(b))
+        out[name] = {"msamples_per_s": round(WIDTH * HEIGHT * SPP / statistics.median(ts) / 1e3, 1)}
+    return out
+
+
+def sampler_comparison(line):
+    """Equal-quality speedups per sampler from the bench line's parts: each GPU sampler's
+    Msamples/s and relative MSE at the benchmark's samples per pixel against the reference's CPU
+    renderer with the same sampler (steerable, CDF) and with the configured steerable sampler."""
+    cb = line.get("cpu_baseline", {})
+    mq = cb.get("matched_quality", {})
+    last = mq.get("rel_mse_at_%dspp" % SPP, {})
+    sec = line.get("secondary", {})
+    gpu = {"steerable": line["value"],
+           "steerable_adaptive": sec.get("adaptive_sampler", {}).get("msamples_per_s"),
+           "cdf": sec.get("samplers", {}).get("cdf", {}).get("msamples_per_s"),
+           "cosine": sec.get("samplers", {}).get("cosine", {}).get("msamples_per_s")}
+    mse = {"steerable": last.get("gpu_steerable_" + line["config"].get("steer_weights", "projected")),
+           "steerable_adaptive": last.get("gpu_steerable_adaptive_projected"),
+           "cdf": last.get("gpu_cdf"), "cosine": last.get("gpu_cosine")}
+    cpu = {"steerable": (cb.get("value"), last.get("cpu_reference_steerable")),
+           "cdf": (cb.get("cdf_value"), last.get("cpu_reference_cdf"))}
+    out = {"gpu_msamples_per_s": gpu, "gpu_rel_mse": mse,
+           "cpu_msamples_per_s": {k: v[0] for k, v in cpu.items()},
+           "cpu_rel_mse": {k: v[1] for k, v in cpu.items()},
+           "equal_quality_speedup": {}}
+    for g in gpu:
+        for c in cpu:
+            if gpu[g] and mse[g] and cpu[c][0] and cpu[c][1]:
+                out["equal_quality_speedup"]["gpu_%s_vs_cpu_%s" % (g, c)] = round(
+                    gpu[g] / cpu[c][0] * cpu[c][1] / mse[g], 1)
+    return out
+
+
 def secondary_metrics(only=None):
     out = {}
     for name, fn in (("batched", batched_metric), ("differentiable", differentiable_metric),
                      ("inverse_rendering", inverse_metric), ("mesh_bvh", mesh_metric),
-                     ("per_iteration", per_iteration_metric), ("adaptive_sampler", adaptive_sampler_metric)):
+                     ("per_iteration", per_iteration_metric), ("adaptive_sampler", adaptive_sampler_metric),
+                     ("samplers", sampler_metric)):
         if only and name != only:
             continue
         try:

@@ -49,8 +49,9 @@ def build(force=False, verbose=False, extra_flags=(), out_dir=None):
         cmd = [nvcc] + ARCH + NVCC_FLAGS + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
             # host code without floating-point contraction: the same results on x86 and Arm hosts
-            cmd = [nvcc] + NVCC_FLAGS + ["-Xcompiler", "-ffp-contract=off", "-x", "c++", "-c",
-                                         os.path.join(CSRC, src), "-o", obj]
+            # (build options given as -D reach the host sources too: some tables are shared)
+            cmd = [nvcc] + NVCC_FLAGS + [f for f in extra_flags if f.startswith("-D")] + \
+                ["-Xcompiler", "-ffp-contract=off", "-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr[-8000:]))

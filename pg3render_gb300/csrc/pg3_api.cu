@@ -527,8 +527,10 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     const SteerGeom &g = *gp;
     const uint32_t nLeaf = g.numLeaves();
     const bool uniformOk = !g.adaptive && nLeaf == (20ull << (2 * g.level)) && g.leafGrid == (4u << g.level) &&
-                           g.leafCells.size() == 6ull * g.leafGrid * g.leafGrid;
-    const bool adaptiveOk = g.adaptive && g.qtree.size() >= 5 && g.leafGrid == 0;
+                           g.leafCells.size() == 6ull * g.leafGrid * g.leafGrid &&
+                           g.startCells.size() == 6ull * kSteerUniformStartGrid * kSteerUniformStartGrid;
+    const bool adaptiveOk = g.adaptive && g.qtree.size() >= 5 && g.leafGrid == 0 &&
+                            g.startCells.size() == 6ull * kSteerStartGrid * kSteerStartGrid;
     if ((!uniformOk && !adaptiveOk) || g.leafTri.size() != nLeaf || g.leafPlane.size() != nLeaf ||
         g.leafEdge.size() != 3ull * nLeaf || g.leafArea.size() != nLeaf || g.layerStart.size() < 2 ||
         g.layerStart.size() > kSteerMaxLayers + 1 || g.tri.size() < 20 || g.levelOffset.size() < 2)
@@ -561,6 +563,7 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     if ((st = upload(ctx, (int4 **)&sv.leafTri, g.leafTri))) return keep(st);
     if ((st = upload(ctx, (int4 **)&sv.faceCells, g.faceCells))) return keep(st);
     if (g.adaptive && (st = upload(ctx, (int4 **)&sv.qtree, g.qtree))) return keep(st);
+    if (!g.startCells.empty() && (st = upload(ctx, (int **)&sv.startCells, g.startCells))) return keep(st);
     float *rootW = reinterpret_cast<float *>(const_cast<float4 *>(sv.leafPlane) + rootAt);
     sv.numLeaves = nLeaf;
     sv.leafGrid = g.leafGrid;

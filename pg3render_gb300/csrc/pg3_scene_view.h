@@ -81,6 +81,8 @@ struct SteerView {
     const int4 *faceCells;    // cube-map cells: up to 4 candidate level-0 faces (-1 none)
     const int4 *leafTri;      // per leaf: vertex ids (w: subdivision level)
     const int4 *qtree;        // adaptive: face codes and the subdivided triangles (pg3_steerable.h)
+    const int *startCells;    // adaptive: per cube-map cell the quadtree code where point location
+                              // starts (INT_MIN: at the level-0 face); null for uniform levels
     uint32_t numLeaves, leafGrid;
     uint32_t level;           // leaf subdivision level (adaptive: the deepest leaf's); uniform levels keep
                               // the triangles of every level in `tri`, level l from 20 (4^l - 1) / 3 on

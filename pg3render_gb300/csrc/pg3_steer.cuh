@@ -26,6 +26,14 @@ namespace pg3 {
 
 constexpr int kSteerCellsDev = 8;   // must equal kSteerCells of the host build
 constexpr uint32_t kSteerMaxAdaptiveDepth = 12;   // must equal kSteerMaxAdaptiveLevel of the host build
+#ifndef PG3_STEER_START_GRID
+#define PG3_STEER_START_GRID 256
+#endif
+constexpr int kSteerStartGridDev = PG3_STEER_START_GRID;   // must equal kSteerStartGrid of the host build
+#ifndef PG3_STEER_UNIFORM_START_GRID
+#define PG3_STEER_UNIFORM_START_GRID 256
+#endif
+constexpr int kSteerUniformStartGridDev = PG3_STEER_UNIFORM_START_GRID;   // kSteerUniformStartGrid
 
 PG3_DI void steerCoeffs(float3 n, float c[9])
 {
@@ -167,13 +175,22 @@ PG3_DI int steerLocateFaces(const SteerView &T, float3 w)
     return local;
 }
 
-// Leaf containing direction w in an adaptive triangulation: its face, then the quadtree of the
-// face's subdivided triangles down to a leaf (bounded by the deepest level).
+// Leaf containing direction w in an adaptive triangulation: the quadtree of the subdivided
+// triangles down to a leaf (bounded by the deepest level), from the deepest triangle that holds w's
+// start cell, or from w's level-0 face where the cell lies on several faces.
 PG3_DI int steerLocateAdaptive(const SteerView &T, float3 w)
 {
-    const int f = steerFace(T, w);
-    const int4 fc = __ldg(&T.qtree[f >> 2]);
-    int code = (f & 3) == 0 ? fc.x : (f & 3) == 1 ? fc.y : (f & 3) == 2 ? fc.z : fc.w;
+    int code = INT_MIN;
+    if (T.startCells) {
+        float fu, fv;
+        const int cf = cubeFace(w, fu, fv);
+        code = __ldg(&T.startCells[cubeCell(cf, fu, fv, kSteerStartGridDev)]);
+    }
+    if (code == INT_MIN) {
+        const int f = steerFace(T, w);
+        const int4 fc = __ldg(&T.qtree[f >> 2]);
+        code = (f & 3) == 0 ? fc.x : (f & 3) == 1 ? fc.y : (f & 3) == 2 ? fc.z : fc.w;
+    }
     for (uint32_t depth = 0; depth <= kSteerMaxAdaptiveDepth && code >= 0; ++depth) {
         const int4 mid = __ldg(&T.qtree[5 + 2 * code]);
         const int4 ch = __ldg(&T.qtree[5 + 2 * code + 1]);
@@ -183,13 +200,18 @@ PG3_DI int steerLocateAdaptive(const SteerView &T, float3 w)
     return code < 0 ? ~code : 0;
 }
 
-// Leaf containing direction w: the leaf-locator cell lists every leaf that can touch it, so
-// the one whose three edge planes all face w is among them (the face hierarchy decides for
-// cells with more than eight candidates, and if rounding puts w outside all candidates).
+// Leaf containing direction w: the start cell names it where one leaf holds the whole cell;
+// otherwise the leaf-locator cell lists every leaf that can touch it, so the one whose three edge
+// planes all face w is among them (the face hierarchy decides for cells with more than eight
+// candidates, and if rounding puts w outside all candidates).
 PG3_DI int steerLocate(const SteerView &T, float3 w)
 {
     float fu, fv;
     const int face = cubeFace(w, fu, fv);
+    if (kSteerUniformStartGridDev > 0 && T.startCells) {   // the cell lies in one leaf
+        const int s = __ldg(&T.startCells[cubeCell(face, fu, fv, kSteerUniformStartGridDev)]);
+        if (s != INT_MIN) return ~s;
+    }
     const uint4 cell = __ldg(&steerCells(T)[cubeCell(face, fu, fv, (int)steerGrid(T))]);
     if (cell.x != 0xfffefffeu) {
         const uint32_t words[4] = {cell.x, cell.y, cell.z, cell.w};

@@ -2,6 +2,7 @@
 #include "pg3_steerable.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <climits>
 #include <cmath>
@@ -149,6 +150,77 @@ bool buildFaceLocator(SteerGeom &out, std::string &err)
     return true;
 }
 
+// Corners of cell (iu, iv) of face f of a cube map with G x G cells per face (the device's
+// cubeFace / cubeCell mapping: face f has axis f / 2 and sign -1 for odd f, u and v on the next
+// two axes).
+void cubeCellCorners(int f, uint32_t iu, uint32_t iv, uint32_t G, D3 q[4])
+{
+    const int ax = f / 2, bx = (ax + 1) % 3, cx = (ax + 2) % 3;
+    const double sg = (f & 1) ? -1.0 : 1.0;
+    auto dirOf = [&](double u, double v) {
+        double p[3];
+        p[ax] = sg; p[bx] = u; p[cx] = v;
+        return nrm({p[0], p[1], p[2]});
+    };
+    const double u0 = -1.0 + 2.0 * iu / G, u1 = -1.0 + 2.0 * (iu + 1) / G;
+    const double v0 = -1.0 + 2.0 * iv / G, v1 = -1.0 + 2.0 * (iv + 1) / G;
+    q[0] = dirOf(u0, v0);
+    q[1] = dirOf(u1, v0);
+    q[2] = dirOf(u0, v1);
+    q[3] = dirOf(u1, v1);
+}
+
+// A convex spherical polygon lies in a spherical triangle (great-circle edges) when its corners do.
+// Each corner must lie at least kStartMargin (radians) inside every edge (unit inward normals),
+// which covers the float rounding of the device's cell index and of its edge and child tests.
+constexpr double kStartMargin = 1e-5;
+bool cornersInside(const D3 q[4], const D3 e[3])
+{
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 3; ++k)
+            if (dt(q[i], e[k]) < kStartMargin) return false;
+    return true;
+}
+
+// Start cells of a uniform level (kSteerUniformStartGrid^2 cells per face; none when 0): ~leaf
+// where one leaf contains the whole cell, INT32_MIN elsewhere (the leaf-locator lists serve). A
+// leaf that contains the cell contains its centre, so it is among the leaf-locator candidates of
+// the centre's cell.
+void buildUniformStartCells(SteerGeom &out)
+{
+    const uint32_t G = kSteerUniformStartGrid;
+    out.startCells.clear();
+    if (G == 0) return;
+    const uint32_t nLeaf = out.numLeaves(), LG = out.leafGrid;
+    out.startCells.assign((size_t)6 * G * G, INT_MIN);
+    parallelFor(6 * G, [&](uint32_t row) {
+        const int f = (int)(row / G);
+        const uint32_t iv = row % G;
+        for (uint32_t iu = 0; iu < G; ++iu) {
+            D3 q[4];
+            cubeCellCorners(f, iu, iv, G, q);
+            // the centre's cell of the leaf locator (same face, same position on it)
+            const uint32_t lu = (uint32_t)(((double)iu + 0.5) * LG / G), lv = (uint32_t)(((double)iv + 0.5) * LG / G);
+            const uint4 cell = out.leafCells[((size_t)f * LG + lv) * LG + lu];
+            if (cell.x == 0xfffefffeu) continue;   // more than 8 candidates: the face locator serves
+            const uint32_t words[4] = {cell.x, cell.y, cell.z, cell.w};
+            for (uint32_t k = 0; k < 8; ++k) {
+                const uint32_t id = (words[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
+                if (id == kSteerLeafNone || id >= nLeaf) break;
+                D3 e[3];
+                for (int j = 0; j < 3; ++j) {
+                    const float4 E = out.leafEdge[3 * (size_t)id + j];
+                    e[j] = D3{E.x, E.y, E.z};
+                }
+                if (cornersInside(q, e)) {
+                    out.startCells[((size_t)f * G + iv) * G + iu] = ~(int)id;
+                    break;
+                }
+            }
+        }
+    });
+}
+
 bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
 {
     out = SteerGeom();
@@ -231,18 +303,20 @@ bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
     out.minLevel = out.maxLevel = level;
     leafTables(out);
     buildTree(out);
-    const uint32_t nLeaf = out.numLeaves();
     auto fdir = [&](int id) { return D3{out.vdir[id].x, out.vdir[id].y, out.vdir[id].z}; };
 
     // leaf locator: for every cell of a finer cube map the leaves whose bounding cap meets the
-    // cell's bounding cap (a superset of the leaves that touch the cell); cells with more than
-    // 8 keep the face locator. Caps meet when the angle between their centres is at most the
-    // sum of their radii (plus a margin), i.e. when the cosine of that angle is at least
-    // cos(rLeaf + rCell).
-    std::vector<D3> capC(nLeaf);
-    std::vector<double> capCos(nLeaf), capSin(nLeaf);
-    for (uint32_t i = 0; i < nLeaf; ++i) {
-        const int4 T = cur[i];
+    // cell's bounding cap, found down the subdivision hierarchy (a triangle's children are
+    // visited when its own cap meets the cell's: a leaf is kept only if the caps of all its
+    // ancestors meet the cell's too, which every leaf that touches the cell satisfies); cells
+    // with more than 8 keep the face locator. Caps meet when the angle between their centres is
+    // at most the sum of their radii (plus a margin), i.e. when the cosine of that angle is at
+    // least cos(r_triangle + r_cell).
+    const size_t nTri = out.tri.size();
+    std::vector<D3> capC(nTri);
+    std::vector<double> capCos(nTri), capSin(nTri);
+    for (size_t i = 0; i < nTri; ++i) {
+        const int4 T = out.tri[i];
         const D3 a = fdir(T.x), b = fdir(T.y), c = fdir(T.z);
         capC[i] = nrm(add(add(a, b), c));
         const double r = std::acos(std::fmin(1.0, std::fmin(dt(capC[i], a), std::fmin(dt(capC[i], b), dt(capC[i], c)))));
@@ -262,6 +336,7 @@ bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
             p[ax] = sg; p[bx] = u; p[cx] = vv;
             return nrm({p[0], p[1], p[2]});
         };
+        std::vector<uint32_t> set, next;   // local indices within the current level
         for (uint32_t iu = 0; iu < LG; ++iu) {
             const double u0 = -1.0 + 2.0 * iu / LG, u1 = -1.0 + 2.0 * (iu + 1) / LG;
             const double v0 = -1.0 + 2.0 * iv / LG, v1 = -1.0 + 2.0 * (iv + 1) / LG;
@@ -271,17 +346,25 @@ bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
                 rc = std::fmax(rc, std::acos(std::fmin(1.0, dt(cc, q))));
             rc += 1e-4;
             const double cCos = std::cos(rc), cSin = std::sin(rc);
+            // cos(r_triangle + r_cell); both radii are far below pi/2 at every level
+            auto meets = [&](size_t t) { return dt(cc, capC[t]) >= capCos[t] * cCos - capSin[t] * cSin; };
+            set.clear();
+            for (uint32_t t = 0; t < 20; ++t)
+                if (meets(t)) set.push_back(t);
+            for (uint32_t l = 0; l < level; ++l) {
+                next.clear();
+                for (uint32_t t : set)
+                    for (uint32_t k = 0; k < 4; ++k)
+                        if (meets(out.levelOffset[l + 1] + 4 * t + k)) next.push_back(4 * t + k);
+                set.swap(next);
+            }
             uint32_t ids[8];
             int n = 0;
             bool many = false;
-            for (uint32_t i = 0; i < nLeaf && !many; ++i) {
-                // cos(rLeaf + rCell); both radii are far below pi/2 at every level
-                const double lim = capCos[i] * cCos - capSin[i] * cSin;
-                if (dt(cc, capC[i]) >= lim) {
-                    // (leaf ids from 0xfffe on do not fit the 16-bit lists: the face locator serves)
-                    if (n == 8 || i >= kSteerLeafMany) many = true;
-                    else ids[n++] = i;
-                }
+            for (uint32_t i : set) {   // ascending leaf ids
+                // (leaf ids from 0xfffe on do not fit the 16-bit lists: the face locator serves)
+                if (n == 8 || i >= kSteerLeafMany) { many = true; break; }
+                ids[n++] = i;
             }
             uint4 &cell = out.leafCells[((size_t)f * LG + iv) * LG + iu];
             if (many) {
@@ -297,7 +380,9 @@ bool buildGeometry(uint32_t level, SteerGeom &out, std::string &err)
         }
     });
 
-    return buildFaceLocator(out, err);
+    if (!buildFaceLocator(out, err)) return false;
+    buildUniformStartCells(out);
+    return true;
 }
 
 }  // namespace
@@ -526,6 +611,47 @@ struct Hier {
     }
 };
 
+// Start cells of an adaptive triangulation: for every cell of a cube map (kSteerStartGrid^2 cells
+// per face), the deepest triangle of the hierarchy that contains the whole cell (cornersInside),
+// so that the device's point location starts there instead of at the level-0 face. A cell whose
+// corners no single face contains keeps INT_MIN.
+void buildStartCells(const Hier &h, const std::vector<int> &code, SteerGeom &g)
+{
+    const size_t nt = h.tri.size();
+    auto dir = [&](int v) { return D3{h.V[(size_t)v].x, h.V[(size_t)v].y, h.V[(size_t)v].z}; };
+    std::vector<std::array<D3, 3>> edge(nt);   // unit inward normals of every triangle's edges
+    for (size_t t = 0; t < nt; ++t) {
+        const D3 a = dir(h.tri[t][0]), b = dir(h.tri[t][1]), c = dir(h.tri[t][2]);
+        edge[t] = {nrm(crs(a, b)), nrm(crs(b, c)), nrm(crs(c, a))};
+    }
+    const uint32_t G = kSteerStartGrid;
+    g.startCells.assign((size_t)6 * G * G, INT_MIN);
+    parallelFor(6 * G, [&](uint32_t row) {
+        const int f = (int)(row / G);
+        const uint32_t iv = row % G;
+        for (uint32_t iu = 0; iu < G; ++iu) {
+            D3 q[4];
+            cubeCellCorners(f, iu, iv, G, q);
+            auto holds = [&](size_t t) { return cornersInside(q, edge[t].data()); };
+            int t = -1;
+            for (int fi = 0; fi < 20 && t < 0; ++fi)
+                if (holds((size_t)fi)) t = fi;
+            if (t < 0) continue;
+            for (bool deeper = true; deeper && h.firstChild[(size_t)t] >= 0;) {
+                deeper = false;
+                const int c0 = h.firstChild[(size_t)t];
+                for (int k = 0; k < 4; ++k)
+                    if (holds((size_t)(c0 + k))) {
+                        t = c0 + k;
+                        deeper = true;
+                        break;
+                    }
+            }
+            g.startCells[((size_t)f * G + iv) * G + iu] = code[(size_t)t];
+        }
+    });
+}
+
 // Leaves in depth-first order (face 0's subtree first, children in order), the quadtree codes and
 // the common tables.
 std::shared_ptr<SteerGeom> finishAdaptive(const Hier &h, const SteerGeom &g0, uint32_t minLevel, uint32_t maxLevel,
@@ -581,6 +707,7 @@ std::shared_ptr<SteerGeom> finishAdaptive(const Hier &h, const SteerGeom &g0, ui
     buildTree(*g);
     g->leafGrid = 0;   // no leaf-locator cube map: the quadtree serves
     if (!buildFaceLocator(*g, err)) return nullptr;
+    buildStartCells(h, code, *g);
     return g;
 }
 

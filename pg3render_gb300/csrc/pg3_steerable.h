@@ -71,12 +71,26 @@ struct SteerGeom {
     std::vector<uint4> leafCells;      // cube-map cells (6 x leafGrid^2): up to 8 candidate leaves as
                                        // 16-bit ids (0xffff none); all 0xfffe: more, use the face locator
     uint32_t leafGrid = 0;
+    std::vector<int> startCells;       // cube-map cells where point location starts. Adaptive (6 x
+                                       // kSteerStartGrid^2): the quadtree code (>= 0 subdivided triangle,
+                                       // < 0 ~leaf) of the deepest triangle that contains the whole cell,
+                                       // INT32_MIN where no level-0 face does. Uniform (6 x
+                                       // kSteerUniformStartGrid^2, empty when 0): ~leaf where one leaf
+                                       // contains the whole cell, else INT32_MIN
     int root = 0;
     uint32_t numLeaves() const { return (uint32_t)leafArea.size(); }
     uint32_t numNodes() const { return (uint32_t)(nodeChild.size() / 8); }
 };
 
 constexpr int kSteerCells = 8;         // cube-map resolution of the face locator
+#ifndef PG3_STEER_START_GRID
+#define PG3_STEER_START_GRID 256
+#endif
+constexpr uint32_t kSteerStartGrid = PG3_STEER_START_GRID;   // cube-map resolution of the adaptive start cells
+#ifndef PG3_STEER_UNIFORM_START_GRID
+#define PG3_STEER_UNIFORM_START_GRID 256
+#endif
+constexpr uint32_t kSteerUniformStartGrid = PG3_STEER_UNIFORM_START_GRID;   // of the uniform levels' (0: none)
 constexpr uint32_t kSteerLeafNone = 0xffffu, kSteerLeafMany = 0xfffeu;
 
 // The geometry of subdivision level `level` (<= 7), built on first use and kept for the life of
