@@ -586,6 +586,7 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     a.numLayers = (uint32_t)g.layerStart.size() - 1;
     for (uint32_t l = 0; l <= a.numLayers; ++l) a.layerStart[l] = g.layerStart[l];
     if ((st = devAlloc(ctx, &a.vw, 12 * (size_t)a.numVertices))) return keep(st);
+    if ((st = devAlloc(ctx, &a.vlum, (size_t)a.numVertices))) return keep(st);
     a.projected = (ctx->opts.steer_weights == PG3GPU_STEER_WEIGHTS_PROJECTED) ? 1 : 0;
     unsigned char *proj = nullptr;
     if (a.projected && (st = devAlloc(ctx, &proj, projScratchBytes(a.numVertices)))) return keep(st);
@@ -593,7 +594,7 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     if ((st = devAlloc(ctx, &a.leafW, 9 * (size_t)nLeaf))) return keep(st);
     if ((st = devAlloc(ctx, &a.nodeW, 72 * (size_t)g.numNodes()))) return keep(st);
     a.rootW = rootW;
-    sv.vw = a.vw;
+    sv.vlum = a.vlum;
     sv.nodeW = a.nodeW;
     a.locator = sv;      // geometry and locator tables (vw / nodeW are outputs of this build)
     keep(PG3GPU_OK);

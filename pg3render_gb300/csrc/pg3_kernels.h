@@ -61,6 +61,7 @@ struct SteerWeightArgs {
     uint32_t layerStart[kSteerMaxLayers + 1];    // tree layers bottom-up, node ranges
     uint32_t numLayers;
     float *vw, *leafW, *nodeW, *rootW;           // outputs (12 / 9 / 72 floats per item, 9)
+    float2 *vlum;                                // output: per vertex (L(d_v), L(-d_v)) (pg3_steer.cuh)
     // projected vertex luminance (PG3GPU_STEER_WEIGHTS_PROJECTED): the map projected onto the
     // triangulation's piecewise-linear hat functions; scratch of projScratchBytes(numVertices)
     // bytes and the leaf locator (the geometry part of the scene's SteerView)
@@ -70,7 +71,8 @@ struct SteerWeightArgs {
 };
 size_t projScratchBytes(uint32_t numVertices);
 cudaError_t launchSteerWeights(const SteerWeightArgs &args, cudaStream_t stream);
-// The leaf, node and whole-sphere weights from the vertex weights already in args.vw.
+// The leaf, node and whole-sphere weights from vertex weights already in args.vw (read from a
+// file), through their luminance.
 cudaError_t launchSteerTreeWeights(const SteerWeightArgs &args, cudaStream_t stream);
 
 // pg3_probe.cu (sampler probes for tests)

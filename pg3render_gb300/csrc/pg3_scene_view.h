@@ -71,7 +71,8 @@ struct BvhNode4 {
 // Steerable sampler tables (host build in pg3_steerable.cpp, sampling in pg3_steer.cuh).
 struct SteerView {
     const float4 *vdir;       // per vertex: unit direction xyz (w: the antipodal vertex, uniform levels)
-    const float *vw;          // per vertex: 9 SH basis values scaled by the map's luminance (padded to 12)
+    const float2 *vlum;       // per vertex: the map's luminance at the vertex and at its antipode
+                              // (uniform levels; 0 for adaptive triangulations)
     const int4 *tri;          // vertex ids of the triangles of every subdivision level (adaptive: level 0)
     const float *nodeW;       // per 6-ary tree node: 9 coefficients x 8 child slots of summed weights
     const int *nodeChild;     // per node: 8 child slots (>= 0 node, < 0 ~leaf, INT_MIN none)

@@ -79,17 +79,42 @@ PG3_DI const float *steerRootW(const SteerView &T)
 PG3_DI float steerTotal(const SteerView &T, const float c[9]) { return fmaxf(dot9(steerRootW(T), c), 0.f); }
 
 PG3_DI float3 vdir(const SteerView &T, int v) { return xyz(__ldg(&T.vdir[v])); }
-// a vertex's value: its 9 weights (padded to 12 floats, three vector loads) dotted with c
-PG3_DI float vval(const SteerView &T, int v, const float c[9])
+
+// A vertex's value is its weights (the map's luminance L times the 9 SH basis values Y(d) at its
+// direction d) dotted with c: L (c . Y(d)). With c fixed by the normal, c . Y(d) is a quadratic
+// form in d, set up once per normal, so a vertex costs its direction (loaded anyway) and one
+// 8-byte pair (L(d), L(-d)) instead of 9 weights; the form's even part (quadratic terms and
+// constant) is the same at -d and its odd part (linear terms) changes sign, which gives the
+// antipodal vertex of a uniform level as well.
+struct SteerQuad {
+    float a, bx, by, bz, m8, mzz, mxy, myz, mxz;   // m8: of x^2 - y^2
+};
+PG3_DI SteerQuad steerQuad(const float c[9])
 {
-    const float4 *w = reinterpret_cast<const float4 *>(T.vw) + 3 * v;
-    const float4 a = __ldg(&w[0]), b = __ldg(&w[1]), d = __ldg(&w[2]);
-    float s = 0.f;
-    s += a.x * c[0]; s += a.y * c[1]; s += a.z * c[2]; s += a.w * c[3];
-    s += b.x * c[4]; s += b.y * c[5]; s += b.z * c[6]; s += b.w * c[7];
-    s += d.x * c[8];
-    return fmaxf(s, 0.f);
+    // Y: 0.282095; 0.488603 (y, z, x); 1.092548 (xy, yz); 0.315392 (3z^2 - 1); 1.092548 xz;
+    // 0.546274 (x^2 - y^2) -- the basis of the build (pg3_steer_build.cu)
+    SteerQuad q;
+    q.a = 0.282095f * c[0] - 0.315392f * c[6];
+    q.by = 0.488603f * c[1];
+    q.bz = 0.488603f * c[2];
+    q.bx = 0.488603f * c[3];
+    q.mxy = 1.092548f * c[4];
+    q.myz = 1.092548f * c[5];
+    q.mzz = 3.f * 0.315392f * c[6];
+    q.mxz = 1.092548f * c[7];
+    q.m8 = 0.546274f * c[8];
+    return q;
 }
+// the values of vertex v and of its antipode
+PG3_DI float2 vvalPair(const SteerView &T, const SteerQuad &q, int v, float3 d)
+{
+    const float2 L = __ldg(&T.vlum[v]);
+    const float even = q.a + d.x * (q.m8 * d.x + q.mxy * d.y + q.mxz * d.z) + d.y * (q.myz * d.z - q.m8 * d.y) +
+                       d.z * (q.mzz * d.z);
+    const float odd = q.bx * d.x + q.by * d.y + q.bz * d.z;
+    return make_float2(L.x * fmaxf(even + odd, 0.f), L.y * fmaxf(even - odd, 0.f));
+}
+PG3_DI float vval(const SteerView &T, const SteerQuad &q, int v, float3 d) { return vvalPair(T, q, v, d).x; }
 
 // base density of the point p = b0 A + b1 B + b2 C of leaf `leaf` (vertex values v).
 PG3_DI float steerLeafPdf(const SteerView &T, int leaf, float3 p, float g, float Z)
@@ -232,11 +257,9 @@ PG3_DI int steerLocate(const SteerView &T, float3 w)
     return steerLocateFaces(T, w);
 }
 
-PG3_DI int antipode(float4 v) { return __float_as_int(v.w); }
-
 // base(w) of one direction: its leaf, the point where w meets the leaf's plane, the linear
 // interpolation of the leaf's vertex values there.
-PG3_DI float steerBasePdf(const SteerView &T, int leaf, float3 w, const float c[9], float Z)
+PG3_DI float steerBasePdf(const SteerView &T, int leaf, float3 w, const SteerQuad &q, float Z)
 {
     const int4 tri = __ldg(&T.leafTri[leaf]);
     const float4 pl = __ldg(&T.leafPlane[leaf]);
@@ -249,33 +272,33 @@ PG3_DI float steerBasePdf(const SteerView &T, int leaf, float3 w, const float c[
     const float b0 = dot(cross(B - p, C - p), n) / nn;
     const float b1 = dot(cross(C - p, A - p), n) / nn;
     const float b2 = 1.f - b0 - b1;
-    const float g = b0 * vval(T, tri.x, c) + b1 * vval(T, tri.y, c) + b2 * vval(T, tri.z, c);
+    const float g = b0 * vval(T, q, tri.x, A) + b1 * vval(T, q, tri.y, B) + b2 * vval(T, q, tri.z, C);
     return steerLeafPdf(T, leaf, p, g, Z);
 }
 
 // base(w) + base(-w). Uniform levels: w's leaf, w's barycentric coordinates there, and the values
 // of the leaf's vertices and of their antipodes. Adaptive: -w is located in its own leaf.
 template <bool ADAPTIVE>
-PG3_DI float steerPairPdf(const SteerView &T, float3 w, const float c[9], float Z)
+PG3_DI float steerPairPdf(const SteerView &T, float3 w, const SteerQuad &q, float Z)
 {
     if (ADAPTIVE)
-        return steerBasePdf(T, steerLocateAdaptive(T, w), w, c, Z) + steerBasePdf(T, steerLocateAdaptive(T, -w), -w, c, Z);
+        return steerBasePdf(T, steerLocateAdaptive(T, w), w, q, Z) + steerBasePdf(T, steerLocateAdaptive(T, -w), -w, q, Z);
     const int leaf = steerLocate(T, w);
     const int4 tri = __ldg(&T.leafTri[leaf]);
     const float4 pl = __ldg(&T.leafPlane[leaf]);
     const float3 nT = xyz(pl);
     const float dw = dot(nT, w);
     if (!(dw > 0.f)) return 0.f;
-    const float4 A4 = __ldg(&T.vdir[tri.x]), B4 = __ldg(&T.vdir[tri.y]), C4 = __ldg(&T.vdir[tri.z]);
-    const float3 A = xyz(A4), B = xyz(B4), C = xyz(C4);
+    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
     const float3 p = w * (pl.w / dw);            // w meets the leaf's plane
     const float3 n = cross(B - A, C - A);
     const float nn = dot(n, n);
     const float b0 = dot(cross(B - p, C - p), n) / nn;
     const float b1 = dot(cross(C - p, A - p), n) / nn;
     const float b2 = 1.f - b0 - b1;
-    const float g = b0 * vval(T, tri.x, c) + b1 * vval(T, tri.y, c) + b2 * vval(T, tri.z, c);
-    const float ga = b0 * vval(T, antipode(A4), c) + b1 * vval(T, antipode(B4), c) + b2 * vval(T, antipode(C4), c);
+    const float2 va = vvalPair(T, q, tri.x, A), vb = vvalPair(T, q, tri.y, B), vc = vvalPair(T, q, tri.z, C);
+    const float g = b0 * va.x + b1 * vb.x + b2 * vc.x;
+    const float ga = b0 * va.y + b1 * vb.y + b2 * vc.y;
     return steerLeafPdf(T, leaf, p, g, Z) + steerLeafPdf(T, leaf, p, ga, Z);
 }
 
@@ -288,7 +311,7 @@ PG3_DI float steerPdf(const SteerView &T, float3 w, float3 n)
     steerCoeffs(n, c);
     const float Z = steerTotal(T, c);
     if (!(Z > 0.f)) return 0.f;
-    return steerPairPdf<ADAPTIVE>(T, w, c, Z);
+    return steerPairPdf<ADAPTIVE>(T, w, steerQuad(c), Z);
 }
 
 // Samples a direction in the upper hemisphere of n. Returns false when the map is black.
@@ -357,7 +380,9 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     // 3b^2 - 2b^3), the other two uniformly along the remaining segment
     const int4 tri = __ldg(&T.leafTri[leaf]);
     const float4 A4 = __ldg(&T.vdir[tri.x]), B4 = __ldg(&T.vdir[tri.y]), C4 = __ldg(&T.vdir[tri.z]);
-    const float v0 = vval(T, tri.x, c), v1 = vval(T, tri.y, c), v2 = vval(T, tri.z, c);
+    const SteerQuad q = steerQuad(c);
+    const float2 va = vvalPair(T, q, tri.x, xyz(A4)), vb = vvalPair(T, q, tri.y, xyz(B4)), vc = vvalPair(T, q, tri.z, xyz(C4));
+    const float v0 = va.x, v1 = vb.x, v2 = vc.x;
     const float vs = v0 + v1 + v2;
     const float ts = u * vs;
     const int corner = (vs > 0.f) ? ((ts < v0) ? 0 : ((ts < v0 + v1) ? 1 : 2)) : min((int)(u * 3.f), 2);
@@ -373,10 +398,10 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     if (ADAPTIVE) {
         // -w0 lies in a leaf of its own
         pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) +
-              steerBasePdf(T, steerLocateAdaptive(T, -w0), -w0, c, Z);
+              steerBasePdf(T, steerLocateAdaptive(T, -w0), -w0, q, Z);
     } else {
         // -w0 lies in the antipodal leaf at the same barycentric coordinates
-        const float ga = b0 * vval(T, antipode(A4), c) + b1 * vval(T, antipode(B4), c) + b2 * vval(T, antipode(C4), c);
+        const float ga = b0 * va.y + b1 * vb.y + b2 * vc.y;
         pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) + steerLeafPdf(T, leaf, p, ga, Z);
     }
     float cosIn = dot(w0, n);

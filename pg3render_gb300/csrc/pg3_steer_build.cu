@@ -19,6 +19,12 @@
 // function covers no texel centre keeps its point sample.
 // Layouts for vector loads: a vertex's 9 weights padded to 12 floats (three float4), a node's
 // weights coefficient-major over 8 child slots (9 x 8 floats, two float4 per coefficient).
+// The sampler reads a vertex's value as L(d_v) times c(n) . Y(d_v), evaluated from the vertex
+// direction (pg3_steer.cuh), so besides the weights the build writes per vertex the pair
+// (L(d_v), L(-d_v)) (vlum; the antipode's luminance for the mirrored term of a uniform level),
+// and the leaf weights are summed from L(d_v) Y(d_v) with the same float arithmetic as the vertex
+// weights. Weights read from a file (launchSteerTreeWeights) enter through their luminance
+// L = w_0 / Y_0; the reference's files hold weights of that form (tests/test_emssd.py).
 #include <algorithm>
 #include <climits>
 
@@ -112,8 +118,23 @@ __global__ void projectLumKernel(const float4 *em, uint32_t W, uint32_t H, Steer
     }
 }
 
+// L Y_k(d) for the 9 real SH basis functions (the vertex weight of luminance L at direction d)
+__device__ void shWeights(float L, float4 d, float *o)
+{
+    const float x = d.x, y = d.y, z = d.z;
+    o[0] = L * 0.282095f;
+    o[1] = L * 0.488603f * y;
+    o[2] = L * 0.488603f * z;
+    o[3] = L * 0.488603f * x;
+    o[4] = L * 1.092548f * x * y;
+    o[5] = L * 1.092548f * y * z;
+    o[6] = L * 0.315392f * (3.f * z * z - 1.f);
+    o[7] = L * 1.092548f * x * z;
+    o[8] = L * 0.546274f * (x * x - y * y);
+}
+
 __global__ void vertexWeightsKernel(const float4 *em, uint32_t W, uint32_t H, const float4 *vdir, uint32_t nv,
-                                    ProjScratch proj, int useProj, float *vw)
+                                    ProjScratch proj, int useProj, float *vw, float2 *vlum)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
@@ -137,30 +158,41 @@ __global__ void vertexWeightsKernel(const float4 *em, uint32_t W, uint32_t H, co
         const double m = (double)proj.mass[i] / projScale(W, H, maxOmega);
         L = (float)(a / m);
     }
-    const float x = d.x, y = d.y, z = d.z;
     float *o = vw + 12 * (size_t)i;
-    o[0] = L * 0.282095f;
-    o[1] = L * 0.488603f * y;
-    o[2] = L * 0.488603f * z;
-    o[3] = L * 0.488603f * x;
-    o[4] = L * 1.092548f * x * y;
-    o[5] = L * 1.092548f * y * z;
-    o[6] = L * 0.315392f * (3.f * z * z - 1.f);
-    o[7] = L * 1.092548f * x * z;
-    o[8] = L * 0.546274f * (x * x - y * y);
+    shWeights(L, d, o);
     o[9] = o[10] = o[11] = 0.f;
+    vlum[i].x = L;
 }
 
-__global__ void leafWeightsKernel(const int4 *leafTri, const float *leafArea, uint32_t nLeaf, const float *vw,
-                                  float *lw)
+// The luminance of weights read from a file: w_0 = L Y_0.
+__global__ void lumFromWeightsKernel(const float *vw, uint32_t nv, float2 *vlum)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nv) vlum[i].x = vw[12 * (size_t)i] / 0.282095f;
+}
+
+// The antipode's luminance (uniform levels: vdir.w holds the antipodal vertex; adaptive: -1).
+__global__ void antipodeLumKernel(const float4 *vdir, uint32_t nv, float2 *vlum)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const int a = __float_as_int(vdir[i].w);
+    vlum[i].y = (a >= 0 && (uint32_t)a < nv) ? vlum[a].x : 0.f;
+}
+
+__global__ void leafWeightsKernel(const int4 *leafTri, const float *leafArea, uint32_t nLeaf, const float4 *vdir,
+                                  const float2 *vlum, float *lw)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nLeaf) return;
     const int4 t = leafTri[i];
     const float a = leafArea[i] * (1.f / 3.f);
+    float wa[9], wb[9], wc[9];
+    shWeights(vlum[t.x].x, vdir[t.x], wa);
+    shWeights(vlum[t.y].x, vdir[t.y], wb);
+    shWeights(vlum[t.z].x, vdir[t.z], wc);
 #pragma unroll
-    for (int k = 0; k < 9; ++k)
-        lw[9 * (size_t)i + k] = a * (vw[12 * (size_t)t.x + k] + vw[12 * (size_t)t.y + k] + vw[12 * (size_t)t.z + k]);
+    for (int k = 0; k < 9; ++k) lw[9 * (size_t)i + k] = a * (wa[k] + wb[k] + wc[k]);
 }
 
 // One tree layer: every child slot of nodes [n0, n1) gets its child's summed weight (a leaf's
@@ -214,6 +246,11 @@ __global__ void rootWeightsKernel(const float *lw, uint32_t nLeaf, float *rootW)
 
 size_t projScratchBytes(uint32_t numVertices) { return 16 * (size_t)numVertices + 16; }
 
+namespace {
+// The antipodes' luminance, the leaf, node and whole-sphere weights from the vertex luminance.
+cudaError_t treeWeights(const SteerWeightArgs &a, cudaStream_t st);
+}  // namespace
+
 cudaError_t launchSteerWeights(const SteerWeightArgs &a, cudaStream_t st)
 {
     if (!a.em || !a.vdir || !a.vw || (a.projected && !a.projScratch)) return cudaErrorInvalidValue;
@@ -231,16 +268,26 @@ cudaError_t launchSteerWeights(const SteerWeightArgs &a, cudaStream_t st)
         projectLumKernel<<<(texels + 255) / 256, 256, 0, st>>>(a.em, a.emW, a.emH, a.locator, P);
     }
     vertexWeightsKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.em, a.emW, a.emH, a.vdir, a.numVertices,
-                                                                     P, a.projected, a.vw);
-    return launchSteerTreeWeights(a, st);
+                                                                     P, a.projected, a.vw, a.vlum);
+    return treeWeights(a, st);
 }
 
 cudaError_t launchSteerTreeWeights(const SteerWeightArgs &a, cudaStream_t st)
 {
-    if (!a.leafTri || !a.leafArea || !a.nodeChild || !a.vw || !a.leafW || !a.nodeW || !a.rootW || a.numLayers == 0 ||
-        a.numLayers > kSteerMaxLayers)
+    if (!a.vw || !a.vlum) return cudaErrorInvalidValue;
+    lumFromWeightsKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.vw, a.numVertices, a.vlum);
+    return treeWeights(a, st);
+}
+
+namespace {
+cudaError_t treeWeights(const SteerWeightArgs &a, cudaStream_t st)
+{
+    if (!a.leafTri || !a.leafArea || !a.nodeChild || !a.vdir || !a.vlum || !a.leafW || !a.nodeW || !a.rootW ||
+        a.numLayers == 0 || a.numLayers > kSteerMaxLayers)
         return cudaErrorInvalidValue;
-    leafWeightsKernel<<<(a.numLeaves + 127) / 128, 128, 0, st>>>(a.leafTri, a.leafArea, a.numLeaves, a.vw, a.leafW);
+    antipodeLumKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.vdir, a.numVertices, a.vlum);
+    leafWeightsKernel<<<(a.numLeaves + 127) / 128, 128, 0, st>>>(a.leafTri, a.leafArea, a.numLeaves, a.vdir, a.vlum,
+                                                                a.leafW);
     for (uint32_t l = 0; l < a.numLayers; ++l) {
         const uint32_t n0 = a.layerStart[l], n1 = a.layerStart[l + 1];
         if (n1 <= n0) return cudaErrorInvalidValue;
@@ -249,5 +296,6 @@ cudaError_t launchSteerTreeWeights(const SteerWeightArgs &a, cudaStream_t st)
     rootWeightsKernel<<<1, 256, 0, st>>>(a.leafW, a.numLeaves, a.rootW);
     return cudaGetLastError();
 }
+}  // namespace
 
 }  // namespace pg3
