@@ -535,6 +535,17 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
         g.leafEdge.size() != 3ull * nLeaf || g.leafArea.size() != nLeaf || g.layerStart.size() < 2 ||
         g.layerStart.size() > kSteerMaxLayers + 1 || g.tri.size() < 20 || g.levelOffset.size() < 2)
         return fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: unexpected leaf count, grid or tree depth");
+    // the descent takes a node's children as consecutive ids from its first child (pg3_steer.cuh)
+    for (uint32_t n = 0; n < g.numNodes(); ++n) {
+        const int first = g.nodeChild[8 * (size_t)n];
+        for (int i = 0; i < 8; ++i) {
+            const int id = g.nodeChild[8 * (size_t)n + i];
+            if (id != INT_MIN && (i >= 6 || id != (first >= 0 ? first + i : first - i)))
+                return fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: a tree node's children are not consecutive");
+            if (id == INT_MIN && i + 1 < 8 && g.nodeChild[8 * (size_t)n + i + 1] != INT_MIN)
+                return fail(ctx, PG3GPU_ERR_CUDA, "steerable tables: a tree node's children are not consecutive");
+        }
+    }
     // the previous tables of this context (an adaptive file replaces the triangulation)
     for (void *p : ctx->steerAllocs) ctxFree(ctx, p);
     ctx->steerAllocs.clear();
@@ -592,7 +603,7 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     if (a.projected && (st = devAlloc(ctx, &proj, projScratchBytes(a.numVertices)))) return keep(st);
     a.projScratch = proj;
     if ((st = devAlloc(ctx, &a.leafW, 9 * (size_t)nLeaf))) return keep(st);
-    if ((st = devAlloc(ctx, &a.nodeW, 72 * (size_t)g.numNodes()))) return keep(st);
+    if ((st = devAlloc(ctx, &a.nodeW, 4 * (size_t)kSteerNodeVec4 * g.numNodes()))) return keep(st);
     a.rootW = rootW;
     sv.vlum = a.vlum;
     sv.nodeW = a.nodeW;
@@ -661,7 +672,12 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
     if ((st = upload(ctx, (float4 **)&v.em, hs.em))) return bail(st);
     if ((st = upload(ctx, (float **)&v.emMarg, hs.emMarg))) return bail(st);
     if ((st = upload(ctx, (float **)&v.emCond, hs.emCond))) return bail(st);
-    if ((st = upload(ctx, (float **)&v.bgShL, hs.bgShL))) return bail(st);
+    {
+        // padded to 12 floats: the device reads the 9 coefficients as three float4 (dot9)
+        std::vector<float> sh = hs.bgShL;
+        if (!sh.empty()) sh.resize(12, 0.f);
+        if ((st = upload(ctx, (float **)&v.bgShL, sh))) return bail(st);
+    }
     if (hs.hasSteer) {
         // geometry from the host build; the map-dependent weights are built on the device
         if ((st = uploadSteer(ctx, hs.steer, nullptr))) return bail(st);

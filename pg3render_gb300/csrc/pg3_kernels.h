@@ -60,7 +60,7 @@ struct SteerWeightArgs {
     const int *nodeChild;
     uint32_t layerStart[kSteerMaxLayers + 1];    // tree layers bottom-up, node ranges
     uint32_t numLayers;
-    float *vw, *leafW, *nodeW, *rootW;           // outputs (12 / 9 / 72 floats per item, 9)
+    float *vw, *leafW, *nodeW, *rootW;           // outputs (12 / 9 / 56 floats per item, 9)
     float2 *vlum;                                // output: per vertex (L(d_v), L(-d_v)) (pg3_steer.cuh)
     // projected vertex luminance (PG3GPU_STEER_WEIGHTS_PROJECTED): the map projected onto the
     // triangulation's piecewise-linear hat functions; scratch of projScratchBytes(numVertices)

@@ -69,12 +69,16 @@ struct BvhNode4 {
 };
 
 // Steerable sampler tables (host build in pg3_steerable.cpp, sampling in pg3_steer.cuh).
+constexpr int kSteerNodeVec4 = 14;   // float4 per 6-ary tree node: 6 children x 9 weights, padded
+
 struct SteerView {
     const float4 *vdir;       // per vertex: unit direction xyz (w: the antipodal vertex, uniform levels)
     const float2 *vlum;       // per vertex: the map's luminance at the vertex and at its antipode
                               // (uniform levels; 0 for adaptive triangulations)
     const int4 *tri;          // vertex ids of the triangles of every subdivision level (adaptive: level 0)
-    const float *nodeW;       // per 6-ary tree node: 9 coefficients x 8 child slots of summed weights
+    const float *nodeW;       // per 6-ary tree node: 9 coefficients x 6 children of summed weights,
+                              // coefficient-major (54 floats), then the first child and the child
+                              // count (int bits): kSteerNodeVec4 float4
     const int *nodeChild;     // per node: 8 child slots (>= 0 node, < 0 ~leaf, INT_MIN none)
     const float4 *leafPlane;  // per leaf: unit plane normal, distance from the origin; followed in the
                               // same allocation by the leaf-locator tables and the whole-sphere

@@ -30,6 +30,7 @@ constexpr uint32_t kSteerMaxAdaptiveDepth = 12;   // must equal kSteerMaxAdaptiv
 #define PG3_STEER_START_GRID 256
 #endif
 constexpr int kSteerStartGridDev = PG3_STEER_START_GRID;   // must equal kSteerStartGrid of the host build
+
 #ifndef PG3_STEER_UNIFORM_START_GRID
 #define PG3_STEER_UNIFORM_START_GRID 256
 #endif
@@ -49,11 +50,15 @@ PG3_DI void steerCoeffs(float3 n, float c[9])
     c[8] = c1 * (n.x * n.x - n.y * n.y);
 }
 
+// w: 9 weights padded to 12 floats, 16-byte aligned (three vector loads)
 PG3_DI float dot9(const float *__restrict__ w, const float c[9])
 {
+    const float4 *w4 = reinterpret_cast<const float4 *>(w);
+    const float4 a = __ldg(&w4[0]), b = __ldg(&w4[1]), d = __ldg(&w4[2]);
     float s = 0.f;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) s += __ldg(&w[k]) * c[k];
+    s += a.x * c[0]; s += a.y * c[1]; s += a.z * c[2]; s += a.w * c[3];
+    s += b.x * c[4]; s += b.y * c[5]; s += b.z * c[6]; s += b.w * c[7];
+    s += d.x * c[8];
     return s;
 }
 
@@ -329,19 +334,28 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     float u = u0;
     int leaf = -1;
     for (int depth = 0; depth < 32; ++depth) {
-        // a node: 8 child slots (two int4) and its weights coefficient-major (9 x two float4)
-        const int4 *ch4 = reinterpret_cast<const int4 *>(T.nodeChild) + 2 * node;
-        const int4 ia = __ldg(&ch4[0]), ib = __ldg(&ch4[1]);
-        const int ids[6] = {ia.x, ia.y, ia.z, ia.w, ib.x, ib.y};
-        const float4 *w4 = reinterpret_cast<const float4 *>(T.nodeW) + 18 * node;
+        // a node: the 6 children's weights coefficient-major, packed (54 floats in 14 float4,
+        // element 6 k + i: coefficient k of child i), then its first child and child count
+        const float4 *w4 = reinterpret_cast<const float4 *>(T.nodeW) + kSteerNodeVec4 * node;
         float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float4 tail;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const float4 a = __ldg(&w4[2 * k]);
-            const float2 b = __ldg(reinterpret_cast<const float2 *>(&w4[2 * k + 1]));
-            acc[0] += a.x * c[k]; acc[1] += a.y * c[k]; acc[2] += a.z * c[k]; acc[3] += a.w * c[k];
-            acc[4] += b.x * c[k]; acc[5] += b.y * c[k];
+        for (int j = 0; j < kSteerNodeVec4; ++j) {
+            const float4 a = __ldg(&w4[j]);
+            const float v[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int e = 4 * j + t;
+                if (e < 54) acc[e % 6] += v[t] * c[e / 6];
+            }
+            if (j == kSteerNodeVec4 - 1) tail = a;
         }
+        // a node's children are consecutive nodes, or consecutive leaves (codes ~leaf), so the
+        // record's tail names them all (no load of the node's child slots)
+        int ids[6];
+        const int first = __float_as_int(tail.z), count = __float_as_int(tail.w);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) ids[i] = (i < count) ? ((first >= 0) ? first + i : first - i) : INT_MIN;
         float val[6], cum = 0.f;
 #pragma unroll
         for (int i = 0; i < 6; ++i) {

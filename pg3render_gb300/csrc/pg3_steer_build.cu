@@ -18,7 +18,7 @@
 // stay exactly the ones of pg3_steer.cuh, only the vertex values change. A vertex whose hat
 // function covers no texel centre keeps its point sample.
 // Layouts for vector loads: a vertex's 9 weights padded to 12 floats (three float4), a node's
-// weights coefficient-major over 8 child slots (9 x 8 floats, two float4 per coefficient).
+// weights coefficient-major over its 6 children, packed (54 floats padded to 14 float4).
 // The sampler reads a vertex's value as L(d_v) times c(n) . Y(d_v), evaluated from the vertex
 // direction (pg3_steer.cuh), so besides the weights the build writes per vertex the pair
 // (L(d_v), L(-d_v)) (vlum; the antipode's luminance for the mirrored term of a uniform level),
@@ -195,6 +195,8 @@ __global__ void leafWeightsKernel(const int4 *leafTri, const float *leafArea, ui
     for (int k = 0; k < 9; ++k) lw[9 * (size_t)i + k] = a * (wa[k] + wb[k] + wc[k]);
 }
 
+constexpr int kNodeFloats = 4 * kSteerNodeVec4;   // a tree node's weights (pg3_steer.cuh)
+
 // One tree layer: every child slot of nodes [n0, n1) gets its child's summed weight (a leaf's
 // weight, or the sum of a lower node's child slots, written by the previous launch).
 __global__ void treeLayerKernel(const int *nodeChild, uint32_t n0, uint32_t n1, const float *lw, float *nodeW)
@@ -202,6 +204,7 @@ __global__ void treeLayerKernel(const int *nodeChild, uint32_t n0, uint32_t n1, 
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= 8 * (n1 - n0)) return;
     const uint32_t n = n0 + j / 8, c = j % 8;
+    if (c >= 6) return;   // slots 6 and 7 are never used (6-ary tree)
     const int ch = nodeChild[8 * (size_t)n + c];
     float w[9];
 #pragma unroll
@@ -211,13 +214,21 @@ __global__ void treeLayerKernel(const int *nodeChild, uint32_t n0, uint32_t n1, 
 #pragma unroll
             for (int k = 0; k < 9; ++k) w[k] = lw[9 * (size_t)(~ch) + k];
         } else {
-            for (int cc = 0; cc < 8; ++cc)
+            for (int cc = 0; cc < 6; ++cc)
 #pragma unroll
-                for (int k = 0; k < 9; ++k) w[k] += nodeW[72 * (size_t)ch + 8 * k + cc];
+                for (int k = 0; k < 9; ++k) w[k] += nodeW[kNodeFloats * (size_t)ch + 6 * k + cc];
         }
     }
 #pragma unroll
-    for (int k = 0; k < 9; ++k) nodeW[72 * (size_t)n + 8 * k + c] = w[k];
+    for (int k = 0; k < 9; ++k) nodeW[kNodeFloats * (size_t)n + 6 * k + c] = w[k];
+    if (c == 0) {
+        // the record's tail: the first child and the number of children (the tree is built over
+        // consecutive items, so the children are first, first + 1, ... or ~first, ~first - 1, ...)
+        int count = 0;
+        for (int cc = 0; cc < 6; ++cc) count += nodeChild[8 * (size_t)n + cc] != INT_MIN;
+        nodeW[kNodeFloats * (size_t)n + 54] = __int_as_float(ch);
+        nodeW[kNodeFloats * (size_t)n + 55] = __int_as_float(count);
+    }
 }
 
 // Whole-sphere weights: one block, fp64 partial sums over all leaves.
