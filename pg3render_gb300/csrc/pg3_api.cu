@@ -571,7 +571,8 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     const size_t rootAt = aux.size();
     aux.resize(rootAt + 3, make_float4(0.f, 0.f, 0.f, 0.f));
     if ((st = upload(ctx, (float4 **)&sv.leafPlane, aux))) return keep(st);
-    if ((st = upload(ctx, (int4 **)&sv.leafTri, g.leafTri))) return keep(st);
+    int4 *leafTri = nullptr;
+    if ((st = upload(ctx, &leafTri, g.leafTri))) return keep(st);
     if ((st = upload(ctx, (int4 **)&sv.faceCells, g.faceCells))) return keep(st);
     if (g.adaptive && (st = upload(ctx, (int4 **)&sv.qtree, g.qtree))) return keep(st);
     if (!g.startCells.empty() && (st = upload(ctx, (int **)&sv.startCells, g.startCells))) return keep(st);
@@ -590,7 +591,7 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     a.emH = v.emH;
     a.vdir = sv.vdir;
     a.numVertices = (uint32_t)g.vdir.size();
-    a.leafTri = sv.leafTri;
+    a.leafTri = leafTri;
     a.numLeaves = nLeaf;
     if ((st = upload(ctx, (float **)&a.leafArea, g.leafArea))) return keep(st);
     a.nodeChild = sv.nodeChild;
@@ -598,6 +599,7 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     for (uint32_t l = 0; l <= a.numLayers; ++l) a.layerStart[l] = g.layerStart[l];
     if ((st = devAlloc(ctx, &a.vw, 12 * (size_t)a.numVertices))) return keep(st);
     if ((st = devAlloc(ctx, &a.vlum, (size_t)a.numVertices))) return keep(st);
+    if ((st = devAlloc(ctx, &a.leafRec, 5 * (size_t)nLeaf))) return keep(st);
     a.projected = (ctx->opts.steer_weights == PG3GPU_STEER_WEIGHTS_PROJECTED) ? 1 : 0;
     unsigned char *proj = nullptr;
     if (a.projected && (st = devAlloc(ctx, &proj, projScratchBytes(a.numVertices)))) return keep(st);
@@ -606,6 +608,7 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     if ((st = devAlloc(ctx, &a.nodeW, 4 * (size_t)kSteerNodeVec4 * g.numNodes()))) return keep(st);
     a.rootW = rootW;
     sv.vlum = a.vlum;
+    sv.leafRec = a.leafRec;
     sv.nodeW = a.nodeW;
     a.locator = sv;      // geometry and locator tables (vw / nodeW are outputs of this build)
     keep(PG3GPU_OK);

@@ -62,6 +62,7 @@ struct SteerWeightArgs {
     uint32_t numLayers;
     float *vw, *leafW, *nodeW, *rootW;           // outputs (12 / 9 / 56 floats per item, 9)
     float2 *vlum;                                // output: per vertex (L(d_v), L(-d_v)) (pg3_steer.cuh)
+    float4 *leafRec;                             // output: per leaf 5 float4 (SteerView::leafRec)
     // projected vertex luminance (PG3GPU_STEER_WEIGHTS_PROJECTED): the map projected onto the
     // triangulation's piecewise-linear hat functions; scratch of projScratchBytes(numVertices)
     // bytes and the leaf locator (the geometry part of the scene's SteerView)

@@ -84,7 +84,9 @@ struct SteerView {
                               // same allocation by the leaf-locator tables and the whole-sphere
                               // weights (pg3_steer.cuh)
     const int4 *faceCells;    // cube-map cells: up to 4 candidate level-0 faces (-1 none)
-    const int4 *leafTri;      // per leaf: vertex ids (w: subdivision level)
+    const float4 *leafRec;    // per leaf 5 float4: corners A, B, C with the map's luminance there in w;
+                              // the luminance at -A, -B, -C (uniform levels); the leaf's plane
+                              // (unit normal, distance from the origin)
     const int4 *qtree;        // adaptive: face codes and the subdivided triangles (pg3_steerable.h)
     const int *startCells;    // adaptive: per cube-map cell the quadtree code where point location
                               // starts (INT_MIN: at the level-0 face); null for uniform levels

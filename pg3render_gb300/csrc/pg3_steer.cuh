@@ -110,21 +110,37 @@ PG3_DI SteerQuad steerQuad(const float c[9])
     q.m8 = 0.546274f * c[8];
     return q;
 }
-// the values of vertex v and of its antipode
-PG3_DI float2 vvalPair(const SteerView &T, const SteerQuad &q, int v, float3 d)
+// the values of a vertex at direction d with luminance L and of its antipode (luminance La)
+PG3_DI float2 vvalPair(const SteerQuad &q, float3 d, float L, float La)
 {
-    const float2 L = __ldg(&T.vlum[v]);
     const float even = q.a + d.x * (q.m8 * d.x + q.mxy * d.y + q.mxz * d.z) + d.y * (q.myz * d.z - q.m8 * d.y) +
                        d.z * (q.mzz * d.z);
     const float odd = q.bx * d.x + q.by * d.y + q.bz * d.z;
-    return make_float2(L.x * fmaxf(even + odd, 0.f), L.y * fmaxf(even - odd, 0.f));
+    return make_float2(L * fmaxf(even + odd, 0.f), La * fmaxf(even - odd, 0.f));
 }
-PG3_DI float vval(const SteerView &T, const SteerQuad &q, int v, float3 d) { return vvalPair(T, q, v, d).x; }
 
-// base density of the point p = b0 A + b1 B + b2 C of leaf `leaf` (vertex values v).
-PG3_DI float steerLeafPdf(const SteerView &T, int leaf, float3 p, float g, float Z)
+// A leaf's record (SteerView::leafRec): corners with their luminance, the antipodes' luminance
+// (read only when ANTI), the plane.
+template <bool ANTI>
+struct SteerLeaf {
+    float4 A, B, C, anti, plane;
+};
+template <bool ANTI>
+PG3_DI SteerLeaf<ANTI> steerLeaf(const SteerView &T, int leaf)
 {
-    const float d = __ldg(&T.leafPlane[leaf].w);
+    const float4 *r = T.leafRec + 5 * (size_t)leaf;
+    SteerLeaf<ANTI> L;
+    L.A = __ldg(&r[0]);
+    L.B = __ldg(&r[1]);
+    L.C = __ldg(&r[2]);
+    L.anti = ANTI ? __ldg(&r[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    L.plane = __ldg(&r[4]);
+    return L;
+}
+
+// base density of the point p of a leaf's plane at distance d from the origin (value g there).
+PG3_DI float steerLeafPdf(float d, float3 p, float g, float Z)
+{
     const float r = length(p);
     return (Z > 0.f) ? fmaxf(g, 0.f) / Z * (r * r * r / d) : 0.f;
 }
@@ -266,19 +282,19 @@ PG3_DI int steerLocate(const SteerView &T, float3 w)
 // interpolation of the leaf's vertex values there.
 PG3_DI float steerBasePdf(const SteerView &T, int leaf, float3 w, const SteerQuad &q, float Z)
 {
-    const int4 tri = __ldg(&T.leafTri[leaf]);
-    const float4 pl = __ldg(&T.leafPlane[leaf]);
-    const float dw = dot(xyz(pl), w);
+    const SteerLeaf<false> L = steerLeaf<false>(T, leaf);
+    const float dw = dot(xyz(L.plane), w);
     if (!(dw > 0.f)) return 0.f;
-    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
-    const float3 p = w * (pl.w / dw);
+    const float3 A = xyz(L.A), B = xyz(L.B), C = xyz(L.C);
+    const float3 p = w * (L.plane.w / dw);
     const float3 n = cross(B - A, C - A);
     const float nn = dot(n, n);
     const float b0 = dot(cross(B - p, C - p), n) / nn;
     const float b1 = dot(cross(C - p, A - p), n) / nn;
     const float b2 = 1.f - b0 - b1;
-    const float g = b0 * vval(T, q, tri.x, A) + b1 * vval(T, q, tri.y, B) + b2 * vval(T, q, tri.z, C);
-    return steerLeafPdf(T, leaf, p, g, Z);
+    const float g = b0 * vvalPair(q, A, L.A.w, 0.f).x + b1 * vvalPair(q, B, L.B.w, 0.f).x +
+                    b2 * vvalPair(q, C, L.C.w, 0.f).x;
+    return steerLeafPdf(L.plane.w, p, g, Z);
 }
 
 // base(w) + base(-w). Uniform levels: w's leaf, w's barycentric coordinates there, and the values
@@ -289,22 +305,21 @@ PG3_DI float steerPairPdf(const SteerView &T, float3 w, const SteerQuad &q, floa
     if (ADAPTIVE)
         return steerBasePdf(T, steerLocateAdaptive(T, w), w, q, Z) + steerBasePdf(T, steerLocateAdaptive(T, -w), -w, q, Z);
     const int leaf = steerLocate(T, w);
-    const int4 tri = __ldg(&T.leafTri[leaf]);
-    const float4 pl = __ldg(&T.leafPlane[leaf]);
-    const float3 nT = xyz(pl);
-    const float dw = dot(nT, w);
+    const SteerLeaf<true> L = steerLeaf<true>(T, leaf);
+    const float dw = dot(xyz(L.plane), w);
     if (!(dw > 0.f)) return 0.f;
-    const float3 A = vdir(T, tri.x), B = vdir(T, tri.y), C = vdir(T, tri.z);
-    const float3 p = w * (pl.w / dw);            // w meets the leaf's plane
+    const float3 A = xyz(L.A), B = xyz(L.B), C = xyz(L.C);
+    const float3 p = w * (L.plane.w / dw);       // w meets the leaf's plane
     const float3 n = cross(B - A, C - A);
     const float nn = dot(n, n);
     const float b0 = dot(cross(B - p, C - p), n) / nn;
     const float b1 = dot(cross(C - p, A - p), n) / nn;
     const float b2 = 1.f - b0 - b1;
-    const float2 va = vvalPair(T, q, tri.x, A), vb = vvalPair(T, q, tri.y, B), vc = vvalPair(T, q, tri.z, C);
+    const float2 va = vvalPair(q, A, L.A.w, L.anti.x), vb = vvalPair(q, B, L.B.w, L.anti.y),
+                 vc = vvalPair(q, C, L.C.w, L.anti.z);
     const float g = b0 * va.x + b1 * vb.x + b2 * vc.x;
     const float ga = b0 * va.y + b1 * vb.y + b2 * vc.y;
-    return steerLeafPdf(T, leaf, p, g, Z) + steerLeafPdf(T, leaf, p, ga, Z);
+    return steerLeafPdf(L.plane.w, p, g, Z) + steerLeafPdf(L.plane.w, p, ga, Z);
 }
 
 // Pdf of the mirrored-hemisphere sampler for a direction above the surface (front side).
@@ -392,10 +407,11 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     // exact sample of the linear density on the planar triangle: pick corner i with
     // probability v_i / sum, then barycentric b_i from its marginal 6b(1-b) (inverse of
     // 3b^2 - 2b^3), the other two uniformly along the remaining segment
-    const int4 tri = __ldg(&T.leafTri[leaf]);
-    const float4 A4 = __ldg(&T.vdir[tri.x]), B4 = __ldg(&T.vdir[tri.y]), C4 = __ldg(&T.vdir[tri.z]);
+    const SteerLeaf<!ADAPTIVE> L = steerLeaf<!ADAPTIVE>(T, leaf);
+    const float4 A4 = L.A, B4 = L.B, C4 = L.C;
     const SteerQuad q = steerQuad(c);
-    const float2 va = vvalPair(T, q, tri.x, xyz(A4)), vb = vvalPair(T, q, tri.y, xyz(B4)), vc = vvalPair(T, q, tri.z, xyz(C4));
+    const float2 va = vvalPair(q, xyz(A4), A4.w, L.anti.x), vb = vvalPair(q, xyz(B4), B4.w, L.anti.y),
+                 vc = vvalPair(q, xyz(C4), C4.w, L.anti.z);
     const float v0 = va.x, v1 = vb.x, v2 = vc.x;
     const float vs = v0 + v1 + v2;
     const float ts = u * vs;
@@ -411,12 +427,12 @@ PG3_DI bool steerSample(const SceneView &S, float3 n, float u0, float u1, float 
     const float3 w0 = normalize(p);
     if (ADAPTIVE) {
         // -w0 lies in a leaf of its own
-        pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) +
+        pdf = steerLeafPdf(L.plane.w, p, b0 * v0 + b1 * v1 + b2 * v2, Z) +
               steerBasePdf(T, steerLocateAdaptive(T, -w0), -w0, q, Z);
     } else {
         // -w0 lies in the antipodal leaf at the same barycentric coordinates
         const float ga = b0 * va.y + b1 * vb.y + b2 * vc.y;
-        pdf = steerLeafPdf(T, leaf, p, b0 * v0 + b1 * v1 + b2 * v2, Z) + steerLeafPdf(T, leaf, p, ga, Z);
+        pdf = steerLeafPdf(L.plane.w, p, b0 * v0 + b1 * v1 + b2 * v2, Z) + steerLeafPdf(L.plane.w, p, ga, Z);
     }
     float cosIn = dot(w0, n);
     wig = w0;

@@ -78,7 +78,8 @@ __device__ double projScale(uint32_t W, uint32_t H, double bound)
     return 1e18 / ((double)W * (double)H * fmax(bound, 1e-30));
 }
 
-__global__ void projectLumKernel(const float4 *em, uint32_t W, uint32_t H, SteerView T, ProjScratch P)
+__global__ void projectLumKernel(const float4 *em, uint32_t W, uint32_t H, SteerView T, const int4 *leafTri,
+                                 ProjScratch P)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= W * H) return;
@@ -94,7 +95,7 @@ __global__ void projectLumKernel(const float4 *em, uint32_t W, uint32_t H, Steer
     const float lum = texelLumAt(em, i);
     const int leaf = T.qtree ? steerLocateAdaptive(T, d) : steerLocate(T, d);
     if (leaf < 0 || (uint32_t)leaf >= T.numLeaves) return;
-    const int4 tri = T.leafTri[leaf];
+    const int4 tri = leafTri[leaf];
     const float3 A = xyz(T.vdir[tri.x]), B = xyz(T.vdir[tri.y]), C = xyz(T.vdir[tri.z]);
     const float3 n = cross(B - A, C - A);
     const float nn = dot(n, n);
@@ -169,6 +170,23 @@ __global__ void lumFromWeightsKernel(const float *vw, uint32_t nv, float2 *vlum)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nv) vlum[i].x = vw[12 * (size_t)i] / 0.282095f;
+}
+
+// Leaf records: the corners with their luminance, the antipodes' luminance, the plane.
+__global__ void leafRecordKernel(const int4 *leafTri, const float4 *vdir, const float2 *vlum, const float4 *leafPlane,
+                                 uint32_t nLeaf, float4 *rec)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nLeaf) return;
+    const int4 t = leafTri[i];
+    const float2 la = vlum[t.x], lb = vlum[t.y], lc = vlum[t.z];
+    const float4 A = vdir[t.x], B = vdir[t.y], C = vdir[t.z];
+    float4 *r = rec + 5 * (size_t)i;
+    r[0] = make_float4(A.x, A.y, A.z, la.x);
+    r[1] = make_float4(B.x, B.y, B.z, lb.x);
+    r[2] = make_float4(C.x, C.y, C.z, lc.x);
+    r[3] = make_float4(la.y, lb.y, lc.y, 0.f);
+    r[4] = leafPlane[i];
 }
 
 // The antipode's luminance (uniform levels: vdir.w holds the antipodal vertex; adaptive: -1).
@@ -276,7 +294,7 @@ cudaError_t launchSteerWeights(const SteerWeightArgs &a, cudaStream_t st)
         if (e != cudaSuccess) return e;
         const uint32_t texels = a.emW * a.emH;
         maxLumKernel<<<std::min<uint32_t>((texels + 255) / 256, 1024), 256, 0, st>>>(a.em, texels, P.maxLumBits);
-        projectLumKernel<<<(texels + 255) / 256, 256, 0, st>>>(a.em, a.emW, a.emH, a.locator, P);
+        projectLumKernel<<<(texels + 255) / 256, 256, 0, st>>>(a.em, a.emW, a.emH, a.locator, a.leafTri, P);
     }
     vertexWeightsKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.em, a.emW, a.emH, a.vdir, a.numVertices,
                                                                      P, a.projected, a.vw, a.vlum);
@@ -293,10 +311,12 @@ cudaError_t launchSteerTreeWeights(const SteerWeightArgs &a, cudaStream_t st)
 namespace {
 cudaError_t treeWeights(const SteerWeightArgs &a, cudaStream_t st)
 {
-    if (!a.leafTri || !a.leafArea || !a.nodeChild || !a.vdir || !a.vlum || !a.leafW || !a.nodeW || !a.rootW ||
-        a.numLayers == 0 || a.numLayers > kSteerMaxLayers)
+    if (!a.leafTri || !a.leafArea || !a.nodeChild || !a.vdir || !a.vlum || !a.leafRec || !a.locator.leafPlane ||
+        !a.leafW || !a.nodeW || !a.rootW || a.numLayers == 0 || a.numLayers > kSteerMaxLayers)
         return cudaErrorInvalidValue;
     antipodeLumKernel<<<(a.numVertices + 127) / 128, 128, 0, st>>>(a.vdir, a.numVertices, a.vlum);
+    leafRecordKernel<<<(a.numLeaves + 127) / 128, 128, 0, st>>>(a.leafTri, a.vdir, a.vlum, a.locator.leafPlane,
+                                                               a.numLeaves, a.leafRec);
     leafWeightsKernel<<<(a.numLeaves + 127) / 128, 128, 0, st>>>(a.leafTri, a.leafArea, a.numLeaves, a.vdir, a.vlum,
                                                                 a.leafW);
     for (uint32_t l = 0; l < a.numLayers; ++l) {
