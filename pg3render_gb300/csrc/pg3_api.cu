@@ -607,7 +607,6 @@ int pg3::uploadSteer(pg3gpu_ctx *ctx, std::shared_ptr<const SteerGeom> gp, const
     if ((st = devAlloc(ctx, &a.leafW, 9 * (size_t)nLeaf))) return keep(st);
     if ((st = devAlloc(ctx, &a.nodeW, 4 * (size_t)kSteerNodeVec4 * g.numNodes()))) return keep(st);
     a.rootW = rootW;
-    sv.vlum = a.vlum;
     sv.leafRec = a.leafRec;
     sv.nodeW = a.nodeW;
     a.locator = sv;      // geometry and locator tables (vw / nodeW are outputs of this build)

@@ -809,13 +809,16 @@ PG3_DI bool occludedList(const SceneView &S, float3 pt, float3 dir, float dist)
 }
 
 // Hit attributes: geometric normal (triangle) or outward normal (sphere), material.
+// After the 3 float4 per triangle: per triangle (normal, material as int bits), one load per hit.
+PG3_DI const float4 *triShade(const SceneView &S) { return S.tri + 3 * (size_t)S.ntri; }
+
 PG3_DI void hitAttributes(const SceneView &S, const Hit &h, float3 org, float3 dir, float3 &pt, float3 &n, int &mat)
 {
     pt = org + dir * h.t;
     if ((uint32_t)h.prim < S.ntri) {
-        const uint32_t i = (uint32_t)h.prim;
-        n = make_float3(__ldg(&S.tri[3 * i].w), __ldg(&S.tri[3 * i + 1].w), __ldg(&S.tri[3 * i + 2].w));
-        mat = __ldg(&S.triMat[i]);
+        const float4 r = __ldg(&triShade(S)[h.prim]);
+        n = xyz(r);
+        mat = __float_as_int(r.w);
     } else {
         const uint32_t i = (uint32_t)h.prim - S.ntri;
         const float4 s = __ldg(&S.sph[i]);

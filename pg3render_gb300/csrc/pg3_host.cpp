@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 
 namespace pg3 {
 
@@ -272,6 +273,12 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         out.tri[3 * i + 1] = make_float4(p1.x, p1.y, p1.z, nrm.y);
         out.tri[3 * i + 2] = make_float4(p2.x, p2.y, p2.z, nrm.z);
         out.triMat[i] = t.material;
+    }
+    // after the vertices, per triangle its normal and material (int bits): what a hit reads
+    for (uint32_t i = 0; i < sc.num_triangles; ++i) {
+        float m;
+        std::memcpy(&m, &out.triMat[i], sizeof m);
+        out.tri.push_back(make_float4(out.tri[3 * i].w, out.tri[3 * i + 1].w, out.tri[3 * i + 2].w, m));
     }
     out.sph.resize(sc.num_spheres);
     out.sphMat.resize(sc.num_spheres);

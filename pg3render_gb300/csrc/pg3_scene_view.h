@@ -73,8 +73,6 @@ constexpr int kSteerNodeVec4 = 14;   // float4 per 6-ary tree node: 6 children x
 
 struct SteerView {
     const float4 *vdir;       // per vertex: unit direction xyz (w: the antipodal vertex, uniform levels)
-    const float2 *vlum;       // per vertex: the map's luminance at the vertex and at its antipode
-                              // (uniform levels; 0 for adaptive triangulations)
     const int4 *tri;          // vertex ids of the triangles of every subdivision level (adaptive: level 0)
     const float *nodeW;       // per 6-ary tree node: 9 coefficients x 6 children of summed weights,
                               // coefficient-major (54 floats), then the first child and the child

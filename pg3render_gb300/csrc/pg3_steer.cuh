@@ -87,10 +87,10 @@ PG3_DI float3 vdir(const SteerView &T, int v) { return xyz(__ldg(&T.vdir[v])); }
 
 // A vertex's value is its weights (the map's luminance L times the 9 SH basis values Y(d) at its
 // direction d) dotted with c: L (c . Y(d)). With c fixed by the normal, c . Y(d) is a quadratic
-// form in d, set up once per normal, so a vertex costs its direction (loaded anyway) and one
-// 8-byte pair (L(d), L(-d)) instead of 9 weights; the form's even part (quadratic terms and
-// constant) is the same at -d and its odd part (linear terms) changes sign, which gives the
-// antipodal vertex of a uniform level as well.
+// form in d, set up once per normal, so a vertex costs its direction and luminance (both in the
+// leaf's record) instead of 9 weights; the form's even part (quadratic terms and constant) is the
+// same at -d and its odd part (linear terms) changes sign, which gives the antipodal vertex of a
+// uniform level as well (its luminance is in the record too).
 struct SteerQuad {
     float a, bx, by, bz, m8, mzz, mxy, myz, mxz;   // m8: of x^2 - y^2
 };

@@ -467,7 +467,8 @@ PG3_DI int extendOne(const SceneView &S, const Queues &Q, const float4 *rq, uint
     const bool hit = intersectClosest<TRAV>(S, xyz(r0), xyz(r1), r0.w, h);
     Q.hit[i] = make_float2(h.t, __int_as_float(h.prim));
     if (!hit) return kBucketMiss;
-    const int mat = ((uint32_t)h.prim < S.ntri) ? __ldg(&S.triMat[h.prim]) : __ldg(&S.sphMat[h.prim - S.ntri]);
+    const int mat = ((uint32_t)h.prim < S.ntri) ? __float_as_int(__ldg(&triShade(S)[h.prim]).w)
+                                                : __ldg(&S.sphMat[h.prim - S.ntri]);
     return bucketOfKind(__ldg(&S.mats[mat].kind));
 }
 
