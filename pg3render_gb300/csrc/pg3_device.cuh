@@ -7,6 +7,10 @@
 // virtual dispatch (materials are a switch over a 64-byte record).
 #pragma once
 
+#ifndef PG3_FAST_HIT_DIV
+#define PG3_FAST_HIT_DIV 0
+#endif
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -749,7 +753,11 @@ PG3_DI bool hitTriangle(float4 a, float4 b, float4 c, float3 org, float3 dir, fl
     const float d0 = dot(v0, dir), d1 = dot(v1, dir), d2 = dot(v2, dir);
     if ((d0 < 0.f && d1 < 0.f && d2 < 0.f) || (d0 >= 0.f && d1 >= 0.f && d2 >= 0.f)) {
         const float3 n = make_float3(a.w, b.w, c.w);
+#if PG3_FAST_HIT_DIV
+        const float dist = __fdividef(dot(n, ao), dot(n, dir));
+#else
         const float dist = dot(n, ao) / dot(n, dir);
+#endif
         if ((dist > tmin) & (dist < tmax)) { tmax = dist; return true; }
     }
     return false;
