@@ -7,8 +7,16 @@
 // virtual dispatch (materials are a switch over a 64-byte record).
 #pragma once
 
+// The triangle test's plane distance by the fast division (__fdividef, within 2 ulp of the
+// IEEE quotient for the denominators that occur, |n . dir| <= 1) instead of the IEEE one (+1.9% on
+// the environment-map benchmark). Every query (list, binary and 4-wide BVH, batch) uses the same
+// test, so they still agree bit for bit.
 #ifndef PG3_FAST_HIT_DIV
-#define PG3_FAST_HIT_DIV 0
+#define PG3_FAST_HIT_DIV 1
+#endif
+// The sphere test's divisions likewise (|dir|^2 = 1 to float rounding).
+#ifndef PG3_FAST_SPHERE_DIV
+#define PG3_FAST_SPHERE_DIV 1
 #endif
 
 #include <cstdint>
@@ -772,14 +780,24 @@ PG3_DI bool hitSphere(float4 s, float3 org, float3 dir, float tmin, float &tmax)
 {
     const float3 o = org - xyz(s);
     const float A = dot(dir, dir);
+#if PG3_FAST_SPHERE_DIV
+    const float invA = __fdividef(1.f, A);
+    const float b = dot(dir, o) * invA;               // half of B / A
+#else
+    const float invA = 1.f / A;
     const float b = dot(dir, o) / A;                  // half of B / A
+#endif
     const float3 l = o - dir * b;
     const float disc = s.w * s.w - dot(l, l);
     if (disc < 0.f) return false;
     const float C = dot(o, o) - s.w * s.w;
-    const float q = (b >= 0.f) ? (-b - sqrtf(disc * (1.f / A)) ) : (-b + sqrtf(disc * (1.f / A)));
+    const float q = (b >= 0.f) ? (-b - sqrtf(disc * invA)) : (-b + sqrtf(disc * invA));
     float t0 = q;
+#if PG3_FAST_SPHERE_DIV
+    float t1 = (fabsf(q) > 0.1f) ? __fdividef(C, A * q) : t0;
+#else
     float t1 = (fabsf(q) > 0.1f) ? (C / (A * q)) : t0;
+#endif
     if (t0 > t1) { const float t = t0; t0 = t1; t1 = t; }
     if (t0 > tmin && t0 < tmax) { tmax = t0; return true; }
     if (t1 > tmin && t1 < tmax) { tmax = t1; return true; }
