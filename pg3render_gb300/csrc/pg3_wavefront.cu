@@ -111,10 +111,10 @@ __global__ void __launch_bounds__(kWaveBlock) raygenKernel(const __grid_constant
 #ifndef PG3_QUERY_MIN_BLOCKS
 #define PG3_QUERY_MIN_BLOCKS 6
 #endif
-// ... for the binary LBVH, and for the 4-wide BVH, whose node records and sorted children need
-// more registers
+// ... for the binary LBVH (5: its traversal stack and node boxes fit 48 registers without spill),
+// and for the 4-wide BVH, whose node records and sorted children need more registers
 #ifndef PG3_LBVH_QUERY_MIN_BLOCKS
-#define PG3_LBVH_QUERY_MIN_BLOCKS 6
+#define PG3_LBVH_QUERY_MIN_BLOCKS 5
 #endif
 #ifndef PG3_BVH4_QUERY_MIN_BLOCKS
 #define PG3_BVH4_QUERY_MIN_BLOCKS 4
