@@ -450,12 +450,22 @@ PG3_DI void cameraRay(const SceneView &S, uint32_t pixel, uint32_t sample, float
 }
 
 // State of a camera ray at position pos of ray queue q.
-PG3_DI void initPathState(const Queues &Q, int q, uint32_t pos)
+// A camera path's state before its first vertex: throughput 1, no previous BSDF pdf or
+// contribution, path length 1, finite, reflectance to compute.
+PG3_DI void initialPathState(float4 st[3])
 {
-    float4 *st = stQ(Q, q) + 3 * (size_t)pos;
     st[0] = make_float4(1.f, 1.f, 1.f, 0.f);
     st[1] = make_float4(0.f, 0.f, 0.f, 0.f);
     st[2] = make_float4(0.f, 0.f, 1.f, __uint_as_float(1u | kFlagFinite | kFlagRefl));
+}
+PG3_DI void initPathState(const Queues &Q, int q, uint32_t pos)
+{
+    float4 init[3];
+    initialPathState(init);
+    float4 *st = stQ(Q, q) + 3 * (size_t)pos;
+    st[0] = init[0];
+    st[1] = init[1];
+    st[2] = init[2];
 }
 
 // Closest hit of one ray and its material bucket (-1 none). TRAV: the traversal (intersectClosest).

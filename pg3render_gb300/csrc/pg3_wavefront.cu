@@ -71,6 +71,12 @@ void launchStage(bool pdl, void (*kernel)(Params...), int grid, size_t smem, cud
     cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
 }
 
+// The first bounce's shade kernels take the camera paths' initial state from registers instead of
+// the state queue, so raygen writes no state (48 bytes per path less to write and to read).
+#ifndef PG3_FIRST_STATE_CONST
+#define PG3_FIRST_STATE_CONST 1
+#endif
+
 // The first sample index of a launch: sample0, plus a device word when one is given (a captured
 // graph replays with a new word: a differentiable-rendering graph, a per-call render graph).
 template <bool GRAD>
@@ -94,7 +100,10 @@ __global__ void __launch_bounds__(kWaveBlock) raygenKernel(const __grid_constant
         cameraRay(S, pixel, sample, dir);
         Q.ray[0][2 * i] = make_float4(S.camPos.x, S.camPos.y, S.camPos.z, 0.f);
         Q.ray[0][2 * i + 1] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(i));
+        // (no path state: the first bounce's shade kernels start from the initial one)
+#if !PG3_FIRST_STATE_CONST
         initPathState(Q, 0, i);
+#endif
         if (GRAD) Q.pend[i] = make_float2(__int_as_float(-1), 0.f);
         outR[i] = 0.f;
         outG[i] = 0.f;
@@ -218,11 +227,18 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
         if (j < n) {
             const uint32_t idx = nextIdx;
             NextEntry nx;
+            const bool first = PG3_FIRST_STATE_CONST && pathLen == 1;   // camera rays: the initial state
             if (j + stride < n) {
                 nextIdx = Q.bucket[kBucket][j + stride];
                 nx.ray = rq + 2 * (size_t)nextIdx;
                 nx.hit = Q.hit + nextIdx;
-                nx.st = stQ(Q, cur) + 3 * (size_t)nextIdx;
+                nx.st = first ? nullptr : stQ(Q, cur) + 3 * (size_t)nextIdx;
+            }
+            float4 st0[3];
+            const float4 *stp = stQ(Q, cur) + 3 * (size_t)idx;
+            if (first) {
+                initialPathState(st0);
+                stp = st0;
             }
             const float4 r0 = rq[2 * idx], r1 = rq[2 * idx + 1];
             const uint32_t slot = __float_as_uint(r1.w) & kSlotMask;
@@ -231,8 +247,7 @@ __global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
             float3 acc = f3(0.f);
             if (GRAD && G.adjoint) acc = make_float3(outR[slot], outG[slot], outB[slot]);
             float3 L;
-            shadeVertex<K, EMK, GRAD>(S, Q, idx, r0, r1, stQ(Q, cur) + 3 * (size_t)idx, slot, slot, pixel, sample, pc, o,
-                                      L, G, sGrad, acc, nx);
+            shadeVertex<K, EMK, GRAD>(S, Q, idx, r0, r1, stp, slot, slot, pixel, sample, pc, o, L, G, sGrad, acc, nx);
             if (!isZero(L)) {
                 outR[slot] += L.x;
                 outG[slot] += L.y;
