@@ -57,7 +57,7 @@ BYTES_PER_PATH = 72 + 36
 # DRAM bytes (read + write) per camera path of one launch chunk, measured by ncu over all stage
 # kernels of one step of the 128x128 x 64 spp case of this workload (one chunk of 2^20 paths);
 # the chunk's traffic grows with its paths.
-NCU_TRAFFIC_PER_PATH = 1045.2
+NCU_TRAFFIC_PER_PATH = 954.4
 
 
 def parse():
