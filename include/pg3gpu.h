@@ -82,6 +82,11 @@ enum { PG3GPU_EM_CDF = 0, PG3GPU_EM_COSINE = 1, PG3GPU_EM_STEERABLE = 2 };
  * the binary LBVH built on the device; BVH4 the 4-wide BVH collapsed from it (same hits; about 3%
  * slower than the binary tree on a 40968-triangle mesh; batches use the binary tree). */
 enum { PG3GPU_TRAVERSAL_AUTO = 0, PG3GPU_TRAVERSAL_LIST = 1, PG3GPU_TRAVERSAL_BVH = 2, PG3GPU_TRAVERSAL_BVH4 = 3 };
+/* Pipelines of the path tracers: AUTO (= WAVEFRONT) runs one kernel per stage and bounce over
+ * queues of rays, the throughput choice for calls of many samples; MEGAKERNEL traces whole paths
+ * per thread in one launch, faster for calls of one sample per pixel (the reference's
+ * per-iteration pattern: about 10% at 512x512) and leaving the path-length histogram empty. The
+ * splitting and clipping options always run as a megakernel. */
 enum { PG3GPU_PIPELINE_AUTO = 0, PG3GPU_PIPELINE_MEGAKERNEL = 1, PG3GPU_PIPELINE_WAVEFRONT = 2 };
 
 /* ---- scene description (copied at create time) ------------------------- */
