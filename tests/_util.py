@@ -29,7 +29,7 @@ def zscores(mean_a, var_a, mean_b, var_b):
 
 
 def z_ok(z, frac_limit=0.999, zmax=4.0, stochastic=None):
-    """Fraction of |z| <= zmax at least frac_limit (the spec gate), plus the mean and
+    """Fraction of |z| <= zmax at least frac_limit (the image parity bar), plus the mean and
     standard deviation of z (systematic bias would shift the mean). stochastic (optional mask):
     the entries with sampling variance; deterministic pixels (a constant background seen
     directly, an emitter) have z = 0 and are left out of the two moments."""

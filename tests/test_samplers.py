@@ -1,4 +1,4 @@
-"""Sampler checks on the GPU (the spec correctness gates 2 and 3):
+"""Sampler checks on the GPU (the sampler parity bars: pdf consistency and goodness of fit):
 
 * every sampler's returned pdf equals the pdf its evaluation path computes for
   the same direction to 1e-5 relative (median 1e-6), and
