@@ -80,6 +80,10 @@ int upload(pg3gpu_ctx *ctx, T **p, const std::vector<T> &v)
 #ifndef PG3_QUEUE_POOL
 #define PG3_QUEUE_POOL 1
 #endif
+// Framebuffer accumulation of a multi-chunk call overlapped with the next chunk's rendering.
+#ifndef PG3_ACC_OVERLAP
+#define PG3_ACC_OVERLAP 1
+#endif
 constexpr uint64_t kPoolKeepBytes = 8ull << 30;
 constexpr int kMaxPoolDevices = 64;
 cudaMemPool_t g_queuePools[kMaxPoolDevices] = {};
@@ -133,20 +137,21 @@ void bigFree(pg3gpu_ctx *ctx, void *p)
         ctxFree(ctx, p);
 }
 
-int ensureOutput(pg3gpu_ctx *ctx, uint64_t paths)
+int ensureOutputSet(pg3gpu_ctx *ctx, float *(&out)[3], uint64_t &capacity, uint64_t paths)
 {
-    if (paths <= ctx->outCapacity) return PG3GPU_OK;
-    for (auto &p : ctx->dOut) {
+    if (paths <= capacity) return PG3GPU_OK;
+    for (auto &p : out) {
         bigFree(ctx, p);
         p = nullptr;
     }
-    for (auto &p : ctx->dOut) {
+    for (auto &p : out) {
         int st = bigAlloc(ctx, &p, paths);
         if (st) return st;
     }
-    ctx->outCapacity = paths;
+    capacity = paths;
     return PG3GPU_OK;
 }
+int ensureOutput(pg3gpu_ctx *ctx, uint64_t paths) { return ensureOutputSet(ctx, ctx->dOut, ctx->outCapacity, paths); }
 
 // Wavefront queues for launches of `paths` paths: max_paths_in_flight slots (default 2^24, the
 // slot-index limit: 292 bytes per slot, 4.6 GiB at most), fewer when a launch has fewer paths;
@@ -218,12 +223,14 @@ int checkRenderable(pg3gpu_ctx *ctx, int algorithm)
 
 // algorithm: 7 runs on the wavefront pipeline (unless the megakernel was chosen), the others
 // on the megakernel
-int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passes)
+// out: the per-sample output set (second: ctx->dOut2)
+int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passes, bool second = false)
 {
     if (int st = checkRenderable(ctx, algorithm)) return st;
     const uint32_t npix = ctx->W * ctx->H;
     const uint64_t paths = (uint64_t)passes * npix;
-    int st = ensureOutput(ctx, paths);
+    int st = second ? ensureOutputSet(ctx, ctx->dOut2, ctx->out2Capacity, paths) : ensureOutput(ctx, paths);
+    float *const *out = second ? ctx->dOut2 : ctx->dOut;
     const bool tree = algorithm == PG3GPU_ALG_PATH_TRACING && ctx->view.treeMode;
     const bool wave = ctx->useWavefront && algorithm == PG3GPU_ALG_PATH_TRACING && !tree;
     if (!st && wave) st = ensureWave(ctx, paths);
@@ -239,10 +246,10 @@ int renderChunk(pg3gpu_ctx *ctx, int algorithm, uint32_t sample0, uint32_t passe
     uint64_t launches = 1;
     if (wave) {
         launches = 0;
-        e = launchWavefront(ctx->view, ctx->kindMask, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
+        e = launchWavefront(ctx->view, ctx->kindMask, sample0, paths, npix, out[0], out[1], out[2],
                             ctx->dStats, ctx->dWave, ctx->waveCapacity, ctx->waveGrid, ctx->stream, &launches);
     } else
-        e = launchMegakernel(ctx->view, algorithm, sample0, paths, npix, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2],
+        e = launchMegakernel(ctx->view, algorithm, sample0, paths, npix, out[0], out[1], out[2],
                              ctx->dStats, tree ? ctx->treeGrid : ctx->megaGrid, ctx->stream, ctx->dTree,
                              ctx->treeDepth);
     if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "path kernel launch: %s", cudaGetErrorString(e));
@@ -425,6 +432,13 @@ int pg3gpu_destroy(pg3gpu_ctx *ctx)
     if (!ctx) return PG3GPU_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->accStream) {
+        cudaStreamSynchronize(ctx->accStream);
+        cudaStreamDestroy(ctx->accStream);
+    }
+    for (cudaEvent_t ev : {ctx->evRendered[0], ctx->evRendered[1], ctx->evAccumulated[0], ctx->evAccumulated[1],
+                           ctx->evAccJoin})
+        if (ev) cudaEventDestroy(ev);
     if (ctx->graphStream) cudaStreamSynchronize(ctx->graphStream);
     if (ctx->callGraphExec) cudaGraphExecDestroy(ctx->callGraphExec);
     if (ctx->callGraph) cudaGraphDestroy(ctx->callGraph);
@@ -782,14 +796,45 @@ int pg3gpu_run_iteration(pg3gpu_ctx *ctx, int32_t algorithm, uint32_t iteration,
     const uint32_t npix = ctx->W * ctx->H;
     const uint32_t per = passesPerChunk(ctx, spp);
     PG3_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-    for (uint32_t done = 0; done < spp; done += per) {
+    // A call of several chunks accumulates each chunk on a side stream while the next one renders
+    // into the other output set; chunks are accumulated in order (one side stream), an output set
+    // is rendered into again only after its accumulation, and the context's stream joins the side
+    // stream at the end. Not while the stream is being captured.
+    bool overlap = PG3_ACC_OVERLAP && spp > per;
+    if (overlap) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        overlap = cudaStreamIsCapturing(ctx->stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone;
+    }
+    if (overlap && !ctx->accStream) {
+        PG3_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->accStream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            PG3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->evRendered[k], cudaEventDisableTiming));
+            PG3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->evAccumulated[k], cudaEventDisableTiming));
+        }
+        PG3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->evAccJoin, cudaEventDisableTiming));
+    }
+    uint32_t chunk = 0;
+    for (uint32_t done = 0; done < spp; done += per, ++chunk) {
         const uint32_t passes = std::min(per, spp - done);
-        int st = renderChunk(ctx, algorithm, iteration + done, passes);
+        const int set = overlap ? (int)(chunk & 1) : 0;
+        if (overlap && chunk >= 2) PG3_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->evAccumulated[set], 0));
+        int st = renderChunk(ctx, algorithm, iteration + done, passes, set == 1);
         if (st) return st;
-        cudaError_t e = launchAccumulate(npix, passes, ctx->dOut[0], ctx->dOut[1], ctx->dOut[2], ctx->dSum,
-                                         ctx->dSumsq, ctx->stream);
+        float *const *out = set ? ctx->dOut2 : ctx->dOut;
+        cudaStream_t accSt = ctx->stream;
+        if (overlap) {
+            PG3_CUDA(ctx, cudaEventRecord(ctx->evRendered[set], ctx->stream));
+            PG3_CUDA(ctx, cudaStreamWaitEvent(ctx->accStream, ctx->evRendered[set], 0));
+            accSt = ctx->accStream;
+        }
+        cudaError_t e = launchAccumulate(npix, passes, out[0], out[1], out[2], ctx->dSum, ctx->dSumsq, accSt);
         if (e != cudaSuccess) return fail(ctx, PG3GPU_ERR_CUDA, "accumulate: %s", cudaGetErrorString(e));
+        if (overlap) PG3_CUDA(ctx, cudaEventRecord(ctx->evAccumulated[set], ctx->accStream));
         ctx->allLaunches += 1;
+    }
+    if (overlap) {
+        PG3_CUDA(ctx, cudaEventRecord(ctx->evAccJoin, ctx->accStream));
+        PG3_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->evAccJoin, 0));
     }
     PG3_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->timed = true;

@@ -33,6 +33,12 @@ struct pg3gpu_ctx {
     double *dSum = nullptr, *dSumsq = nullptr;
     float *dOut[3] = {nullptr, nullptr, nullptr};
     uint64_t outCapacity = 0;            // paths per launch chunk
+    // a second set of per-sample outputs and a side stream: a call of several chunks accumulates
+    // chunk k into the framebuffer while chunk k + 1 renders (pg3gpu_run_iteration)
+    float *dOut2[3] = {nullptr, nullptr, nullptr};
+    uint64_t out2Capacity = 0;
+    cudaStream_t accStream = nullptr;
+    cudaEvent_t evRendered[2] = {nullptr, nullptr}, evAccumulated[2] = {nullptr, nullptr}, evAccJoin = nullptr;
     void *dWave = nullptr;               // wavefront queues
     uint64_t waveCapacity = 0;
     DevStats *dStats = nullptr;
