@@ -55,6 +55,23 @@ def test_wavefront_small_capacity_chunks():
     assert _match(a, b) >= 0.995
 
 
+def test_multi_chunk_call_accumulates_every_chunk():
+    # chunks of 2 samples per pixel: the call accumulates chunk k on a side stream while chunk
+    # k + 1 renders into the other output set; the framebuffer is the mean of the same samples
+    scene = S.cornell_box(16, 16)
+    cfg = P.Config(scene=scene, max_path_length=8, max_paths_in_flight=2 * 16 * 16)
+    with P.GpuPathTracer(cfg, seed=13) as r:
+        samples = r.render_samples(R.kPathTracing, 0, 10)
+        r.RunIteration(R.kPathTracing, 0, 10)
+        r.RunIteration(R.kPathTracing, 10, 6)       # a second call reuses both output sets
+        mean, var, n = r.framebuffer(with_variance=True)
+        tail = r.render_samples(R.kPathTracing, 10, 6)
+    assert n == 16
+    want = np.concatenate([samples, tail]).astype(np.float64)
+    assert np.allclose(mean, want.mean(axis=0), rtol=1e-6, atol=1e-7)
+    assert np.allclose(var, want.var(axis=0, ddof=1), rtol=1e-4, atol=1e-7)
+
+
 @pytest.mark.parametrize("name", ["cornell_area_32", "cornell_env_32_cdf"])
 def test_wavefront_against_reference_golden(name):
     d, text, td = load_golden(name)
