@@ -685,7 +685,21 @@ int pg3::createContext(const pg3gpu_scene *scene, const pg3gpu_options *opts, in
     if ((st = upload(ctx, (DevMaterial **)&v.mats, hs.mats))) return bail(st);
     if ((st = upload(ctx, (int **)&v.mat2light, hs.mat2light))) return bail(st);
     if ((st = upload(ctx, (DevAreaLight **)&v.lights, hs.lights))) return bail(st);
-    if ((st = upload(ctx, (float4 **)&v.em, hs.em))) return bail(st);
+    if (hs.emTexels) {
+        // the caller's RGB texels to the device (a quarter less to copy than float4) and widened
+        // there; the staging copy is freed once the kernel has run
+        float4 *em = nullptr;
+        float *rgb = nullptr;
+        if ((st = devAlloc(ctx, &em, hs.emTexels))) return bail(st);
+        if (cudaMalloc(&rgb, 3 * sizeof(float) * hs.emTexels) != cudaSuccess)
+            return bail(fail(ctx, PG3GPU_ERR_OUT_OF_MEMORY, "environment map staging allocation failed"));
+        cudaError_t e = cudaMemcpy(rgb, hs.emRgb, 3 * sizeof(float) * hs.emTexels, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launchEmFromRgb(rgb, (uint32_t)hs.emTexels, em, nullptr);
+        const cudaError_t ef = cudaFree(rgb);   // (waits for the kernel)
+        if (e == cudaSuccess) e = ef;
+        if (e != cudaSuccess) return bail(fail(ctx, PG3GPU_ERR_CUDA, "environment map upload: %s", cudaGetErrorString(e)));
+        v.em = em;
+    }
     if ((st = upload(ctx, (float **)&v.emMarg, hs.emMarg))) return bail(st);
     if ((st = upload(ctx, (float **)&v.emCond, hs.emCond))) return bail(st);
     {

@@ -341,13 +341,17 @@ int prepareScene(const pg3gpu_scene &sc, const pg3gpu_options &o, HostScene &out
         if (!sc.env_map || sc.env_width < 2 || sc.env_height < 2 || (uint64_t)sc.env_width * sc.env_height > (1ull << 26))
             return bad(PG3GPU_ERR_INVALID_ARGUMENT, "environment map needs data and 2 <= size <= 2^26 pixels");
         const size_t np = (size_t)sc.env_width * sc.env_height;
-        out.em.resize(np);
-        for (size_t i = 0; i < np; ++i) {
-            const float *p = sc.env_map + 3 * i;
-            if (!finite3(p) || p[0] < 0.f || p[1] < 0.f || p[2] < 0.f)
-                return bad(PG3GPU_ERR_INVALID_ARGUMENT, "environment map texels must be finite and non-negative");
-            out.em[i] = make_float4(p[0], p[1], p[2], 0.f);
+        // every component finite and non-negative, tested on the bit patterns (a vectorised pass):
+        // finite non-negative floats are 0x00000000-0x7F7FFFFF, and -0 (0x80000000) counts as 0
+        uint32_t invalid = 0;
+        for (size_t i = 0; i < 3 * np; ++i) {
+            uint32_t u;
+            std::memcpy(&u, sc.env_map + i, sizeof u);
+            invalid |= (uint32_t)(u > 0x7F7FFFFFu) & (uint32_t)(u != 0x80000000u);
         }
+        if (invalid) return bad(PG3GPU_ERR_INVALID_ARGUMENT, "environment map texels must be finite and non-negative");
+        out.emRgb = sc.env_map;   // uploaded as RGB and widened to float4 on the device
+        out.emTexels = np;
         // the CDF tables serve the CDF sampler only (the device rebuilds them on map updates)
         if (o.em_sampler == PG3GPU_EM_CDF) buildEmCdf(sc.env_map, sc.env_width, sc.env_height, out.emMarg, out.emCond);
         v.emW = sc.env_width;

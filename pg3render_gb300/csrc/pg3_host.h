@@ -23,7 +23,8 @@ struct HostScene {
     std::vector<DevMaterial> mats;
     std::vector<int> mat2light;
     std::vector<DevAreaLight> lights;
-    std::vector<float4> em;
+    const float *emRgb = nullptr;        // the caller's map (RGB, validated); widened to float4 on the device
+    size_t emTexels = 0;
     std::vector<float> emMarg, emCond;
     std::vector<float> bgShL;            // 9 SH coefficients of the map's luminance (picking estimate)
     std::shared_ptr<const SteerGeom> steer;   // steerable sampler geometry (uniform levels: the shared,

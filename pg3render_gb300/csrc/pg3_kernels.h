@@ -29,6 +29,8 @@ cudaError_t launchAccumulate(uint32_t npix, uint32_t passes, const float *r, con
 // One thread stores `value` to *dst (the head node of a captured render graph, whose parameter
 // each replay sets to the call's first sample index).
 cudaError_t launchSetWord(uint32_t *dst, uint32_t value, cudaStream_t stream);
+// n RGB texels (3 floats each) to float4 texels (alpha 0)
+cudaError_t launchEmFromRgb(const float *rgb, uint32_t n, float4 *em, cudaStream_t stream);
 const void *setWordKernelFunction();
 
 // pg3_lbvh.cu

@@ -87,6 +87,21 @@ cudaError_t launchSetWord(uint32_t *dst, uint32_t value, cudaStream_t stream)
 
 const void *setWordKernelFunction() { return reinterpret_cast<const void *>(setWordKernel); }
 
+// RGB texels (3 floats each, as the caller passes them) to the float4 texels the kernels read.
+__global__ void emFromRgbKernel(const float *rgb, uint32_t n, float4 *em)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        em[i] = make_float4(rgb[3 * (size_t)i], rgb[3 * (size_t)i + 1], rgb[3 * (size_t)i + 2], 0.f);
+}
+
+cudaError_t launchEmFromRgb(const float *rgb, uint32_t n, float4 *em, cudaStream_t stream)
+{
+    if (n == 0) return cudaSuccess;
+    const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 4096);
+    emFromRgbKernel<<<blocks, 256, 0, stream>>>(rgb, n, em);
+    return cudaGetLastError();
+}
+
 cudaError_t launchMegakernel(const SceneView &S, int algorithm, uint32_t sample0, uint64_t numPaths, uint32_t npix,
                              float *outR, float *outG, float *outB, DevStats *stats, int gridBlocks,
                              cudaStream_t stream, TreeFrame *tree, uint32_t treeDepth)

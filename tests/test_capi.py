@@ -88,9 +88,14 @@ def test_scene_validation():
     s.env_map = np.ones((4, 8, 3), np.float32)               # environment map + area lights: valid
     st, err = _create(s)
     assert st == _lib.ERR_CUDA and "device" in err           # (validation passed; no GPU here)
+    for bad in (np.nan, np.inf, -1e-30):                     # map texels: finite and non-negative
+        s = S.cornell_env(8, 8, 16, 8)
+        s.env_map[3, 5, 1] = bad
+        assert _create(s)[0] == _lib.ERR_INVALID_ARGUMENT, bad
     s = S.cornell_env(8, 8, 16, 8)
-    s.env_map[0, 0, 0] = np.nan
-    assert _create(s)[0] == _lib.ERR_INVALID_ARGUMENT
+    s.env_map[3, 5, 1] = -0.0                                # negative zero is zero
+    st, err = _create(s)
+    assert st == _lib.ERR_CUDA and "device" in err
     s = S.cornell_box(0, 8)
     assert _create(s)[0] == _lib.ERR_INVALID_ARGUMENT
 
