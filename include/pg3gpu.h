@@ -371,8 +371,9 @@ int pg3gpu_steer_triangulate(const float *rgb, uint32_t width, uint32_t height, 
  * sumsq_rgb (width*height*3 doubles each; sum and sum of squares; never cleared by
  * this call) instead of the context's framebuffer. It always runs the megakernel
  * pipeline (one kernel per path; the wavefront pipeline's queues would need device
- * memory): on the 512x512 environment-map benchmark about a third of the throughput of
- * pg3gpu_run_iteration, which runs algorithm 7 on the wavefront pipeline. The
+ * memory): on the 512x512 environment-map benchmark under half the throughput of
+ * pg3gpu_run_iteration (which runs algorithm 7 on the wavefront pipeline) for calls of many
+ * samples per pixel, and above it for one sample per pixel per call. The
  * per-sample radiance lives in a scratch area compiled into the library:
  * PG3GPU_NOALLOC_MAX_PATHS paths (12 MiB); a GPU holds it from the first
  * pg3gpu_create on that device until the process exits, because pg3gpu_create looks up
