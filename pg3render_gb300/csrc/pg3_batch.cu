@@ -188,12 +188,13 @@ __global__ void __launch_bounds__(kWaveBlock) batchExtend(const SceneView *views
     countWarp(&stats->extRays, rays);
 }
 
-#ifndef PG3_SHADE_MIN_BLOCKS
-#define PG3_SHADE_MIN_BLOCKS 2
+// resident 256-thread blocks per SM the batch shade kernels are compiled for (128 registers)
+#ifndef PG3_BATCH_SHADE_MIN_BLOCKS
+#define PG3_BATCH_SHADE_MIN_BLOCKS 2
 #endif
 
 template <int K, int EMK>
-__global__ void __launch_bounds__(kWaveBlock, PG3_SHADE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kWaveBlock, PG3_BATCH_SHADE_MIN_BLOCKS)
     batchShade(const SceneView *views, const BatchInst *inst, uint32_t ninst, BatchQ B, BatchCtl *ctl,
                DevStats *stats)
 {

@@ -56,11 +56,12 @@ PG3_DI void stageEntry()
 }
 
 template <typename... Params, typename... Args>
-void launchStage(bool pdl, void (*kernel)(Params...), int grid, size_t smem, cudaStream_t st, Args... args)
+void launchStage(bool pdl, void (*kernel)(Params...), int grid, int threads, size_t smem, cudaStream_t st,
+                 Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(kWaveBlock);
+    cfg.blockDim = dim3((unsigned)threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
@@ -162,16 +163,25 @@ __global__ void __launch_bounds__(kWaveBlock, queryMinBlocks(TRAV)) extendKernel
     countWarp(&stats->extRays, rays);
 }
 
-// Resident blocks per SM each shade kernel is compiled and launched for (register budget
-// 65536 / (256 x N)): the miss (background) kernel holds no material code and fits 4.
+// Block shape each shade kernel is compiled and launched for: threads per block and resident
+// blocks per SM (register budget 65536 / (threads x blocks)). The material kernels take 256 x 2
+// (128 registers), the miss (background) kernel, which holds no material code, 256 x 4 (64). The
+// Lambert kernel of the render paths fits 96 registers with at most 4 bytes of spill: 128 x 5
+// keeps 20 warps per SM where 256-thread blocks hold 16. Measured on the environment-map
+// benchmark, that is faster with the steerable and CDF samplers and slower with the cosine
+// sampler, which keeps 256 x 2; so does the gradient instantiation, which spills over 100 bytes
+// at 96 registers with the adjoint's sums.
 #ifndef PG3_SHADE_MIN_BLOCKS
 #define PG3_SHADE_MIN_BLOCKS 2
 #endif
 #ifndef PG3_MISS_MIN_BLOCKS
 #define PG3_MISS_MIN_BLOCKS 4
 #endif
+#ifndef PG3_LAMBERT_THREADS
+#define PG3_LAMBERT_THREADS 128
+#endif
 #ifndef PG3_LAMBERT_MIN_BLOCKS
-#define PG3_LAMBERT_MIN_BLOCKS PG3_SHADE_MIN_BLOCKS
+#define PG3_LAMBERT_MIN_BLOCKS 5
 #endif
 #ifndef PG3_CONDUCTOR_MIN_BLOCKS
 #define PG3_CONDUCTOR_MIN_BLOCKS PG3_SHADE_MIN_BLOCKS
@@ -179,10 +189,16 @@ __global__ void __launch_bounds__(kWaveBlock, queryMinBlocks(TRAV)) extendKernel
 #ifndef PG3_DIELECTRIC_MIN_BLOCKS
 #define PG3_DIELECTRIC_MIN_BLOCKS PG3_SHADE_MIN_BLOCKS
 #endif
-constexpr int shadeMinBlocks(int K)
+constexpr bool lambertShape(int K, int EMK, bool GRAD) { return K == kMatLambert && EMK != kEmCosine && !GRAD; }
+constexpr int shadeThreads(int K, int EMK, bool GRAD)
 {
-    return K < 0                      ? PG3_MISS_MIN_BLOCKS
-           : K == kMatLambert         ? PG3_LAMBERT_MIN_BLOCKS
+    return lambertShape(K, EMK, GRAD) ? PG3_LAMBERT_THREADS : kWaveBlock;
+}
+constexpr int shadeMinBlocks(int K, int EMK, bool GRAD)
+{
+    return K < 0                         ? PG3_MISS_MIN_BLOCKS
+           : lambertShape(K, EMK, GRAD)  ? PG3_LAMBERT_MIN_BLOCKS
+           : K == kMatLambert         ? PG3_SHADE_MIN_BLOCKS
            : K == kMatGgxConductor    ? PG3_CONDUCTOR_MIN_BLOCKS
            : K == kMatGgxDielectric   ? PG3_DIELECTRIC_MIN_BLOCKS
                                       : PG3_SHADE_MIN_BLOCKS;
@@ -204,7 +220,7 @@ PG3_DI void countLengths(DevStats *st, uint32_t len, uint32_t n)
 
 // pathLen: the length of the paths whose vertices this bounce shades (bounce + 1)
 template <int K, int EMK, bool GRAD>
-__global__ void __launch_bounds__(kWaveBlock, shadeMinBlocks(K))
+__global__ void __launch_bounds__(shadeThreads(K, EMK, GRAD), shadeMinBlocks(K, EMK, GRAD))
     shadeKernel(const __grid_constant__ SceneView S, Queues Q, int cur, uint32_t base0, uint32_t npix,
                 uint32_t sample0, float *outR, float *outG, float *outB, DevStats *stats, GradArgs G,
                 uint32_t pathLen)
@@ -343,8 +359,8 @@ void launchShadeKind(const SceneView &S, const Queues &Q, int cur, uint32_t base
                      float *r, float *g, float *b, DevStats *stats, int grid, size_t smem, const GradArgs &G,
                      cudaStream_t st, bool pdl, int &launched, uint32_t pathLen)
 {
-    const int blocks = std::max(1, grid / (1024 / kWaveBlock)) * PG3_SHADE_WAVES * shadeMinBlocks(K);
-    launchStage(pdl, shadeKernel<K, EMK, GRAD>, blocks, smem, st, S, Q, cur, base, npix, sample0, r, g, b, stats, G,
+    const int blocks = std::max(1, grid / (1024 / kWaveBlock)) * PG3_SHADE_WAVES * shadeMinBlocks(K, EMK, GRAD);
+    launchStage(pdl, shadeKernel<K, EMK, GRAD>, blocks, shadeThreads(K, EMK, GRAD), smem, st, S, Q, cur, base, npix, sample0, r, g, b, stats, G,
                 pathLen);
     ++launched;
 }
@@ -402,9 +418,9 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
         for (uint32_t bounce = 0; bounce < maxBounces; ++bounce) {
             const int cur = bounce & 1;
             const bool pdl = capturing == cudaStreamCaptureStatusNone || pdlInCapture;
-            if (trav == 2) launchStage(pdl, extendKernel<2>, queryGrid, 0, stream, S, Q, cur, stats);
-            else if (trav == 1) launchStage(pdl, extendKernel<1>, queryGrid, 0, stream, S, Q, cur, stats);
-            else launchStage(pdl, extendKernel<0>, queryGrid, 0, stream, S, Q, cur, stats);
+            if (trav == 2) launchStage(pdl, extendKernel<2>, queryGrid, kWaveBlock, 0, stream, S, Q, cur, stats);
+            else if (trav == 1) launchStage(pdl, extendKernel<1>, queryGrid, kWaveBlock, 0, stream, S, Q, cur, stats);
+            else launchStage(pdl, extendKernel<0>, queryGrid, kWaveBlock, 0, stream, S, Q, cur, stats);
             const int emk = (S.bgKind == kBgEnvMap) ? S.emSampler : kEmCosine;   // no map: constant/area paths
             const uint32_t b32 = (uint32_t)base;
             int shades;
@@ -420,9 +436,9 @@ cudaError_t runWavefront(const SceneView &S, uint32_t kindMask, uint32_t sample0
             else
                 shades = launchShade<kEmCosine, GRAD>(S, kindMask, Q, cur, b32, npix, sample0, r, g, b, stats, gridBlocks, smem, G, stream, pdl,
                                                                   bounce + 1);
-            if (trav == 2) launchStage(pdl, shadowKernel<GRAD, 2>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
-            else if (trav == 1) launchStage(pdl, shadowKernel<GRAD, 1>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
-            else launchStage(pdl, shadowKernel<GRAD, 0>, queryGrid, smem, stream, S, Q, cur, r, g, b, stats, G);
+            if (trav == 2) launchStage(pdl, shadowKernel<GRAD, 2>, queryGrid, kWaveBlock, smem, stream, S, Q, cur, r, g, b, stats, G);
+            else if (trav == 1) launchStage(pdl, shadowKernel<GRAD, 1>, queryGrid, kWaveBlock, smem, stream, S, Q, cur, r, g, b, stats, G);
+            else launchStage(pdl, shadowKernel<GRAD, 0>, queryGrid, kWaveBlock, smem, stream, S, Q, cur, r, g, b, stats, G);
             *launches += 2 + shades;
             if (S.maxPL == 0 && (bounce & 7) == 7 && capturing == cudaStreamCaptureStatusNone) {
                 // roulette-ended paths: stop once the queue is empty (checked every 8 bounces)
