@@ -163,19 +163,21 @@ __global__ void __launch_bounds__(kWaveBlock, queryMinBlocks(TRAV)) extendKernel
     countWarp(&stats->extRays, rays);
 }
 
-// Block shape each shade kernel is compiled and launched for: threads per block and resident
-// blocks per SM (register budget 65536 / (threads x blocks)). The material kernels take 256 x 2
-// (128 registers), the miss (background) kernel, which holds no material code, 256 x 4 (64). The
-// Lambert kernel of the render paths fits 96 registers with at most 4 bytes of spill: 128 x 5
-// keeps 20 warps per SM where 256-thread blocks hold 16. Measured on the environment-map
-// benchmark, that is faster with the steerable and CDF samplers and slower with the cosine
-// sampler, which keeps 256 x 2; so does the gradient instantiation, which spills over 100 bytes
-// at 96 registers with the adjoint's sums.
+// Block shape each shade kernel of the render paths is compiled and launched for: threads per
+// block and resident blocks per SM (register budget 65536 / (threads x blocks), taken per quarter
+// SM: 17-20 warps per SM leave 96 registers a thread, 16 leave 128). The material kernels take
+// 256 x 2 (128 registers; at 96 the conductor and dielectric spill about 100 bytes and ran 0.6%
+// slower). The Lambert kernel fits 96 registers with at most 4 bytes of spill: 128 x 5 keeps 20
+// warps per SM where 256-thread blocks hold 16, faster with the steerable and CDF samplers and
+// slower with the cosine sampler, which keeps 256 x 2. The miss (background) kernel, which holds
+// no material code, takes 128 x 9 (36 warps, 56 registers, at most 12 bytes of spill; 256 x 4
+// held 32). The gradient instantiations keep 256 x 2 and 256 x 4 for the miss kernel: with the
+// adjoint's sums the Lambert kernel spills over 100 bytes at 96 registers.
 #ifndef PG3_SHADE_MIN_BLOCKS
 #define PG3_SHADE_MIN_BLOCKS 2
 #endif
 #ifndef PG3_MISS_MIN_BLOCKS
-#define PG3_MISS_MIN_BLOCKS 4
+#define PG3_MISS_MIN_BLOCKS 9
 #endif
 #ifndef PG3_LAMBERT_THREADS
 #define PG3_LAMBERT_THREADS 128
@@ -189,14 +191,28 @@ __global__ void __launch_bounds__(kWaveBlock, queryMinBlocks(TRAV)) extendKernel
 #ifndef PG3_DIELECTRIC_MIN_BLOCKS
 #define PG3_DIELECTRIC_MIN_BLOCKS PG3_SHADE_MIN_BLOCKS
 #endif
+#ifndef PG3_CONDUCTOR_THREADS
+#define PG3_CONDUCTOR_THREADS 256
+#endif
+#ifndef PG3_DIELECTRIC_THREADS
+#define PG3_DIELECTRIC_THREADS 256
+#endif
+#ifndef PG3_MISS_THREADS
+#define PG3_MISS_THREADS 128
+#endif
 constexpr bool lambertShape(int K, int EMK, bool GRAD) { return K == kMatLambert && EMK != kEmCosine && !GRAD; }
 constexpr int shadeThreads(int K, int EMK, bool GRAD)
 {
-    return lambertShape(K, EMK, GRAD) ? PG3_LAMBERT_THREADS : kWaveBlock;
+    return lambertShape(K, EMK, GRAD) ? PG3_LAMBERT_THREADS
+           : GRAD ? kWaveBlock
+           : K < 0 ? PG3_MISS_THREADS
+           : K == kMatGgxConductor ? PG3_CONDUCTOR_THREADS
+           : K == kMatGgxDielectric ? PG3_DIELECTRIC_THREADS : kWaveBlock;
 }
 constexpr int shadeMinBlocks(int K, int EMK, bool GRAD)
 {
-    return K < 0                         ? PG3_MISS_MIN_BLOCKS
+    return GRAD                          ? (K < 0 ? 4 : 2)   // 256-thread blocks: 64 / 128 registers
+           : K < 0                       ? PG3_MISS_MIN_BLOCKS
            : lambertShape(K, EMK, GRAD)  ? PG3_LAMBERT_MIN_BLOCKS
            : K == kMatLambert         ? PG3_SHADE_MIN_BLOCKS
            : K == kMatGgxConductor    ? PG3_CONDUCTOR_MIN_BLOCKS
