@@ -79,13 +79,13 @@ enum { PG3GPU_BG_NONE = 0, PG3GPU_BG_CONSTANT = 1, PG3GPU_BG_ENVMAP = 2 };
 enum { PG3GPU_EM_CDF = 0, PG3GPU_EM_COSINE = 1, PG3GPU_EM_STEERABLE = 2 };
 /* Ray queries: AUTO takes the primitive list up to 32 primitives and the binary LBVH above; LIST
  * tests every primitive in order (the reference's GeometryList, src/scene_graph.hxx:33-82); BVH
- * the binary LBVH built on the device; BVH4 the 4-wide BVH collapsed from it (same hits; about 3%
+ * the binary LBVH built on the device; BVH4 the 4-wide BVH collapsed from it (same hits; about 6%
  * slower than the binary tree on a 40968-triangle mesh; batches use the binary tree). */
 enum { PG3GPU_TRAVERSAL_AUTO = 0, PG3GPU_TRAVERSAL_LIST = 1, PG3GPU_TRAVERSAL_BVH = 2, PG3GPU_TRAVERSAL_BVH4 = 3 };
 /* Pipelines of the path tracers: AUTO (= WAVEFRONT) runs one kernel per stage and bounce over
  * queues of rays, the throughput choice for calls of many samples; MEGAKERNEL traces whole paths
  * per thread in one launch, faster for calls of one sample per pixel (the reference's
- * per-iteration pattern: about 10% at 512x512) and leaving the path-length histogram empty. The
+ * per-iteration pattern: about 9% at 512x512) and leaving the path-length histogram empty. The
  * splitting and clipping options always run as a megakernel. */
 enum { PG3GPU_PIPELINE_AUTO = 0, PG3GPU_PIPELINE_MEGAKERNEL = 1, PG3GPU_PIPELINE_WAVEFRONT = 2 };
 
